@@ -1,0 +1,12 @@
+"""GB300-native simulated-bifurcation Ising solver (drop-in for strongshih/Annealing SB/CUDA_GPU).
+
+The solver is the C ABI in include/sb.h, implemented by annealing_gb300/libsbsolve.so (CUDA
+kernels for sm_103a + C++ host code). This package holds the ctypes binding (sb.py), the in-tree
+build (_build.py) and the synthetic instance generators (instances.py).
+"""
+from .sb import (ASB, BSB, DSB, FIELD_AUTO, FIELD_FP32, FIELD_TC, INIT_REFERENCE, INIT_UNIFORM,
+                 Context, Params, Plan, Problem, Result, SBError, lib, pump)
+
+__all__ = ["ASB", "BSB", "DSB", "FIELD_AUTO", "FIELD_FP32", "FIELD_TC", "INIT_REFERENCE",
+           "INIT_UNIFORM", "Context", "Params", "Plan", "Problem", "Result", "SBError", "lib",
+           "pump"]

@@ -1,0 +1,115 @@
+"""In-tree build of the native parts: the solver library, its CLI, and the CPU oracle.
+
+Everything is compiled with plain nvcc / gcc calls (no cmake), object files in parallel:
+  annealing_gb300/libsbsolve.so   CUDA kernels (sm_103a) + C ABI (include/sb.h)
+  annealing_gb300/sb              command-line drop-in for the reference's `./opt <graph>`
+  oracle/libsboracle.so           CPU oracle + multithreaded CPU baseline (test infrastructure)
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "annealing_gb300")
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+ORACLE = os.path.join(ROOT, "oracle")
+
+GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+LIB_SOURCES = ["sb_plain.cu", "sb_tc.cu", "sb_api.cpp", "sb_problem.cpp", "sb_serve.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + proc.stdout)
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def _headers() -> list[str]:
+    hs = [os.path.join(INCLUDE, "sb.h")]
+    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    return hs
+
+
+def build_library(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+    hdrs = _headers()
+    objs, jobs = [], []
+    for src in LIB_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or not _newer(o, [s] + hdrs):
+            if src.endswith(".cu"):
+                cmd = [nvcc, *GENCODE, "-lineinfo", *common, "-c", s, "-o", o]
+            else:
+                cmd = [nvcc, *common, "-c", s, "-o", o]
+            jobs.append(cmd)
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for f in [ex.submit(_run, j) for j in jobs]:
+            f.result()
+    lib = os.path.join(PKG, "libsbsolve.so")
+    if force or jobs or not os.path.exists(lib):
+        _run([nvcc, *GENCODE, "-shared", "-o", lib, *objs, "-lpthread"])
+    cli = os.path.join(PKG, "sb")
+    cli_src = os.path.join(CSRC, "sb_cli.cpp")
+    if force or not _newer(cli, [cli_src, lib] + hdrs):
+        _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", cli,
+              "-L" + PKG, "-lsbsolve", "-Wl,-rpath,$ORIGIN"])
+    return lib
+
+
+def build_oracle(force: bool = False) -> str:
+    out_dir = os.path.join(ORACLE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exact = os.path.join(ORACLE, "sb_oracle.c")
+    base = os.path.join(ORACLE, "sb_cpu_baseline.c")
+    o1 = os.path.join(out_dir, "sb_oracle.o")
+    o2 = os.path.join(out_dir, "sb_cpu_baseline.o")
+    lib = os.path.join(ORACLE, "libsboracle.so")
+    jobs = []
+    if force or not _newer(o1, [exact]):
+        jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                     "-c", exact, "-o", o1])
+    if force or not _newer(o2, [base]):
+        jobs.append(["gcc", "-O3", "-std=gnu11", "-fPIC", "-ffp-contract=fast", "-pthread",
+                     "-c", base, "-o", o2])
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        for f in [ex.submit(_run, j) for j in jobs]:
+            f.result()
+    if force or jobs or not os.path.exists(lib):
+        _run(["gcc", "-shared", "-o", lib, o1, o2, "-lm", "-pthread"])
+    return lib
+
+
+def build_all(force: bool = False) -> None:
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        fl = ex.submit(build_library, force)
+        fo = ex.submit(build_oracle, force)
+        fl.result()
+        fo.result()
+
+
+if __name__ == "__main__":
+    build_all(force=True)
+    print("built", os.path.join(PKG, "libsbsolve.so"))

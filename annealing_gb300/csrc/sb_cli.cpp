@@ -1,0 +1,154 @@
+// `sb` — drop-in command line for the reference program `./opt <graph>` (SB/CUDA_GPU/Makefile:
+// 8-12, m2_opt.cu:100-221).
+//
+// With no options it runs what m2_opt.cu runs: aSB, STEP = 100, one trial (TIMES = 1), the
+// reference's xorshift initial state, xi = 0.01565, and writes output.txt with one energy per trial
+// (m2_opt.cu:206-210). Options select bSB / dSB, replicas, schedule and field precision, and add
+// best_spins.txt (one +1/-1 per line) and a JSON summary on stdout.
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "sb.h"
+
+static void usage() {
+  printf(
+      "Usage:\n"
+      "  sb <graph> [--variant asb|bsb|dsb] [--steps S] [--replicas R] [--seed X]\n"
+      "             [--dt DT] [--a0 A0] [--c0 C0] [--xi XI] [--mts-m M]\n"
+      "             [--field auto|fp32|tc] [--init uniform|reference]\n"
+      "             [--n N] [--index-base 0|1] [--strict] [--trace] [--device D]\n"
+      "             [--out output.txt] [--spins best_spins.txt] [--json]\n"
+      "Graph file: N [E] then lines 'i j J_ij' (i != j) and optional 'i i h_i'.\n");
+}
+
+int main(int argc, char **argv) {
+  if (argc < 2) {
+    usage();
+    return 0;
+  }
+  const char *path = nullptr;
+  std::string out_path = "output.txt", spins_path = "best_spins.txt";
+  bool json = false;
+  int device = 0;
+  sb_graph_opts go;
+  sb_graph_opts_default(&go);
+  int variant = SB_ASB;
+  // first pass: variant (it sets the defaults)
+  for (int i = 1; i < argc; ++i)
+    if (!strcmp(argv[i], "--variant") && i + 1 < argc) {
+      const char *v = argv[i + 1];
+      variant = !strcmp(v, "bsb") ? SB_BSB : !strcmp(v, "dsb") ? SB_DSB : SB_ASB;
+    }
+  sb_params p;
+  sb_params_default(&p, variant);
+  for (int i = 1; i < argc; ++i) {
+    const char *a = argv[i];
+    auto next = [&](void) -> const char * {
+      if (i + 1 >= argc) {
+        fprintf(stderr, "missing value for %s\n", a);
+        exit(2);
+      }
+      return argv[++i];
+    };
+    if (!strcmp(a, "--variant")) next();
+    else if (!strcmp(a, "--steps")) p.steps = atoi(next());
+    else if (!strcmp(a, "--replicas") || !strcmp(a, "--trials")) p.replicas = atoi(next());
+    else if (!strcmp(a, "--seed")) p.seed = strtoull(next(), nullptr, 10);
+    else if (!strcmp(a, "--dt")) p.dt = (float)atof(next());
+    else if (!strcmp(a, "--a0")) p.a0 = (float)atof(next());
+    else if (!strcmp(a, "--c0")) p.c0 = (float)atof(next());
+    else if (!strcmp(a, "--xi")) p.xi = (float)atof(next());
+    else if (!strcmp(a, "--mts-m")) p.mts_m = atoi(next());
+    else if (!strcmp(a, "--field")) {
+      const char *v = next();
+      p.field_mode = !strcmp(v, "fp32") ? SB_FIELD_FP32 : !strcmp(v, "tc") ? SB_FIELD_TC : SB_FIELD_AUTO;
+    } else if (!strcmp(a, "--init")) {
+      p.init_mode = !strcmp(next(), "reference") ? SB_INIT_REFERENCE : SB_INIT_UNIFORM;
+    } else if (!strcmp(a, "--n")) go.n_override = atoi(next());
+    else if (!strcmp(a, "--index-base")) go.index_base = atoi(next());
+    else if (!strcmp(a, "--strict")) go.strict = 1;
+    else if (!strcmp(a, "--trace")) p.trace = 1;
+    else if (!strcmp(a, "--device")) device = atoi(next());
+    else if (!strcmp(a, "--out")) out_path = next();
+    else if (!strcmp(a, "--spins")) spins_path = next();
+    else if (!strcmp(a, "--json")) json = true;
+    else if (!strcmp(a, "-h") || !strcmp(a, "--help")) {
+      usage();
+      return 0;
+    } else if (a[0] == '-') {
+      fprintf(stderr, "unknown option %s\n", a);
+      return 2;
+    } else path = a;
+  }
+  if (!path) {
+    usage();
+    return 2;
+  }
+  sb_problem prob;
+  sb_status s = sb_load_graph_ex(path, &go, &prob);
+  if (s != SB_OK) {
+    fprintf(stderr, "sb: %s: %s (%s)\n", path, sb_status_string(s), sb_last_error(nullptr));
+    return 1;
+  }
+  sb_device_opts dopt;
+  memset(&dopt, 0, sizeof(dopt));
+  dopt.device = device;
+  sb_ctx *ctx = nullptr;
+  s = sb_create(&ctx, &dopt);
+  if (s != SB_OK) {
+    fprintf(stderr, "sb: %s (%s)\n", sb_status_string(s), sb_last_error(nullptr));
+    sb_problem_free(&prob);
+    return 1;
+  }
+  std::vector<int8_t> spins((size_t)prob.n);
+  std::vector<double> energies((size_t)p.replicas);
+  std::vector<double> trace(p.trace ? (size_t)p.steps + 1 : 0);
+  sb_result r;
+  memset(&r, 0, sizeof(r));
+  r.best_spins = spins.data();
+  r.replica_energies = energies.data();
+  r.energy_trace = p.trace ? trace.data() : nullptr;
+  s = sb_solve(ctx, &prob, &p, &r);
+  if (s != SB_OK) {
+    fprintf(stderr, "sb: solve failed: %s (%s)\n", sb_status_string(s), sb_last_error(ctx));
+    sb_destroy(ctx);
+    sb_problem_free(&prob);
+    return 1;
+  }
+  if (p.trace)
+    for (int t = 0; t <= p.steps; ++t) printf("%d %.17g\n", t, trace[t]);
+  FILE *f = fopen(out_path.c_str(), "w");
+  if (f) {
+    for (int k = 0; k < p.replicas; ++k) {
+      if (prob.integer_valued)
+        fprintf(f, "%lld\n", (long long)energies[k]);
+      else
+        fprintf(f, "%.17g\n", energies[k]);
+    }
+    fclose(f);
+  }
+  f = fopen(spins_path.c_str(), "w");
+  if (f) {
+    for (int i = 0; i < prob.n; ++i) fprintf(f, "%d\n", (int)spins[i]);
+    fclose(f);
+  }
+  if (json) {
+    printf(
+        "{\"n\": %d, \"replicas\": %d, \"steps\": %d, \"variant\": %d, \"best_energy\": %.17g, "
+        "\"best_energy_i64\": %lld, \"energy_check_ok\": %d, \"field_mode\": %d, \"field_dtype\": %d, "
+        "\"device_ms\": %.6f, \"total_ms\": %.6f, \"spin_updates_per_s\": %.6e}\n",
+        prob.n, p.replicas, p.steps, p.variant, r.best_energy, (long long)r.best_energy_i64,
+        r.energy_check_ok, r.field_mode_used, r.field_dtype_used, r.device_ms, r.total_ms,
+        r.spin_updates_per_s);
+  } else {
+    printf("best energy %.17g (replica %d), %.3f ms on device, %.4e spin-updates/s\n",
+           r.best_energy, r.best_replica, r.device_ms, r.spin_updates_per_s);
+  }
+  sb_destroy(ctx);
+  sb_problem_free(&prob);
+  return 0;
+}

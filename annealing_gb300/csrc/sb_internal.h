@@ -1,0 +1,63 @@
+// Internal declarations shared by the host library (sb_api.cpp) and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sb.h"
+
+namespace sbk {
+
+// Error bits a kernel ORs into its status word instead of trapping.
+enum : uint32_t {
+  kErrWaitTimeout = 1u,     // a bounded mbarrier / flag wait gave up
+  kErrBadShape = 2u,        // launch shape does not match the arguments
+  kErrTmemAlloc = 4u,       // TMEM allocation failed
+};
+
+// Row pitch (elements) of the padded state and coupling layouts.
+inline int pitch_for(int n, int align) { return (n + align - 1) / align * align; }
+
+// ---------------------------------------------------------------------------------------------
+// Plain FP32 path: one fused launch per SB step.
+// Layouts: J [n][jp] float (row pitch jp, zero padded); x, y [R][xp] float (replica-major).
+struct PlainStep {
+  int variant;             // 0 aSB, 1 bSB, 2 dSB
+  int n, R, jp, xp, rb;    // rb: replicas per CTA (grid.y = ceil(R / rb))
+  const float *J, *h;      // h may be null
+  const float *x_in;
+  float *x_out, *y;        // y is updated in place (each element has one owner)
+  float pump, c0, dt, dta0;            // bSB / dSB
+  float coeff, amp_next, mts_dt, detune, kerr;  // aSB kick and the next step's local update
+  int m, do_local;
+  double *energy;          // [R] energy of s(x_in) (dSB only; may be null)
+  uint32_t *status;
+};
+
+struct PlainEnergy {
+  int n, R, jp, xp, rb;
+  const float *J, *h;
+  const float *x;
+  double *energy;          // [R] += energy of s(x)
+  uint32_t *status;
+};
+
+// Sets kernel attributes (dynamic shared memory limits) once per process; call before any capture.
+void init_kernel_attributes();
+cudaError_t launch_plain_step(const PlainStep &a, cudaStream_t st);
+cudaError_t launch_plain_energy(const PlainEnergy &a, bool fp64, cudaStream_t st);
+
+// Initial state, elementwise helpers.
+cudaError_t launch_init_uniform(float *x, float *y, int n, int R, int xp, uint64_t seed,
+                                cudaStream_t st);
+cudaError_t launch_init_reference(float *x, float *y, int n, int R, int xp, cudaStream_t st);
+cudaError_t launch_asb_local(float *x, float *y, int n, int R, int xp, float amp, int m,
+                             float mts_dt, float detune, float kerr, cudaStream_t st);
+// Copy a dense host-layout J [n][n] (already on the device) into the padded [n][jp] FP32 layout.
+cudaError_t launch_pad_rows_f32(const float *src, float *dst, int n, int jp, cudaStream_t st);
+
+// ---------------------------------------------------------------------------------------------
+// Tensor-core (tcgen05) path. See sb_tc.cu.
+enum TcDtype : int { kTcFp8 = 1, kTcBf16 = 2, kTcBf16Split = 3 };
+
+struct TcPlanInfo;  // opaque, defined in sb_tc.cu
+}  // namespace sbk

@@ -1,0 +1,408 @@
+// Plain FP32 SB path: one fused kernel per step, plus initial-state and energy kernels.
+//
+// Replaces, per step, the reference's two launches UpdateTwice<<<N/64,64>>> + cublasSgemv
+// (SB/CUDA_GPU/m2_opt.cu:168-169) with one kernel that computes the field and the update:
+//   * each CTA owns 8 rows of J (one warp per row) and up to 8 replicas;
+//   * the CTA's J rows are staged into shared memory by bulk TMA copies (cp.async.bulk) in
+//     512-float chunks through a two-stage mbarrier ring, the multiplied vector chunk
+//     (x, or sign(x) for dSB) is staged beside it with 128-bit loads;
+//   * each warp forms its row's dot products with float4 shared-memory reads and a shuffle
+//     reduction, then one lane per replica applies the SB update and writes x (ping-pong) and y
+//     (in place: every element has exactly one owner);
+//   * dSB also reduces -1/2 s_i f_i - h_i s_i per replica (block reduction + one atomic per
+//     replica), which is the energy of s(t) and costs nothing extra because f = J s(t).
+// Every wait is bounded: a timeout sets a status bit and the kernel returns.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sb_internal.h"
+#include "sb_ptx.cuh"
+
+namespace sbk {
+namespace {
+
+constexpr int kRows = 8;
+constexpr int kThreads = 256;
+constexpr int kChunk = 512;  // floats per row per stage
+constexpr int kMaxRB = 8;
+constexpr size_t kSmemBytes = (size_t)(2 * kRows * kChunk + kMaxRB * kChunk) * sizeof(float);
+
+__device__ __forceinline__ float sgn(float v) { return v > 0.0f ? 1.0f : -1.0f; }
+
+// The dSB / bSB update, the exact operation order the CPU oracle restates.
+__device__ __forceinline__ void sb_update(float f, float hv, float pump, float c0, float dt,
+                                          float dta0, float &x, float &y) {
+  float fv = __fadd_rn(f, hv);
+  float g = __fmul_rn(c0, fv);
+  float force = __fmaf_rn(-pump, x, g);
+  y = __fmaf_rn(dt, force, y);
+  x = __fmaf_rn(dta0, y, x);
+  if (fabsf(x) > 1.0f) {
+    x = copysignf(1.0f, x);
+    y = 0.0f;
+  }
+}
+
+// aSB local sub-steps (UpdateTwice, SB/CUDA_GPU/m2_opt.cu:66-71): the reference evaluates them in
+// double because its constants are double literals; explicit _rn ops keep the order fixed.
+__device__ __forceinline__ void asb_local(float &x, float &y, float amp, int m, float mts_dt,
+                                          float detune, float kerr) {
+  double dd = detune, dk = kerr, dh = mts_dt, da = amp;
+  for (int s = 0; s < m; ++s) {
+    x = (float)__dadd_rn((double)x, __dmul_rn(__dmul_rn(dd, (double)y), dh));
+    double lx = (double)x;
+    double x3 = __dmul_rn(__dmul_rn(__dmul_rn(dk, lx), lx), lx);
+    double lin = __dmul_rn(__dadd_rn(dd, -da), lx);
+    y = (float)__dadd_rn((double)y, -__dmul_rn(dh, __dadd_rn(x3, lin)));
+  }
+}
+
+template <typename Acc>
+struct RowAcc {
+  Acc v[kMaxRB];
+};
+
+// Shared machinery: stream the CTA's J rows through shared memory and form dot products with the
+// CTA's replica vectors. MODE 0: v = x; MODE 1: v = sign(x).
+template <int MODE, typename Acc>
+__device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, int n, int row0,
+                                           int rows, const float *__restrict__ xv, int xp, int r0,
+                                           int rb, float *sJ, float *sV, uint64_t *full,
+                                           Acc (&acc)[kMaxRB]) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nchunks = (jp + kChunk - 1) / kChunk;
+#pragma unroll
+  for (int q = 0; q < kMaxRB; ++q) acc[q] = Acc(0);
+  auto issue = [&](int c) {
+    const int k0 = c * kChunk;
+    const int len = min(kChunk, jp - k0);
+    const uint32_t bytes = (uint32_t)len * 4u;
+    uint64_t *bar = &full[c & 1];
+    ptx::mbar_arrive_expect_tx(bar, bytes * (uint32_t)rows);
+    for (int w = 0; w < rows; ++w)
+      ptx::bulk_g2s(sJ + ((c & 1) * kRows + w) * kChunk, J + (size_t)(row0 + w) * jp + k0, bytes,
+                    bar);
+  };
+  if (tid == 0) {
+    issue(0);
+    if (nchunks > 1) issue(1);
+  }
+  bool ok = true;
+  for (int c = 0; c < nchunks; ++c) {
+    const int k0 = c * kChunk;
+    const int len = min(kChunk, jp - k0);
+    // stage the vector chunk (len is a multiple of 4)
+    for (int rr = 0; rr < rb; ++rr) {
+      const float *src = xv + (size_t)(r0 + rr) * xp + k0;
+      float *dst = sV + rr * kChunk;
+      for (int q = tid * 4; q < len; q += kThreads * 4) {
+        float4 t = *reinterpret_cast<const float4 *>(src + q);
+        if (MODE == 1) {
+          t.x = sgn(t.x);
+          t.y = sgn(t.y);
+          t.z = sgn(t.z);
+          t.w = sgn(t.w);
+        }
+        *reinterpret_cast<float4 *>(dst + q) = t;
+      }
+    }
+    if (!ptx::mbar_wait(&full[c & 1], (uint32_t)((c >> 1) & 1))) ok = false;
+    __syncthreads();
+    if (warp < rows && ok) {
+      const float4 *jr = reinterpret_cast<const float4 *>(sJ + ((c & 1) * kRows + warp) * kChunk);
+      for (int q = lane; q < (len >> 2); q += 32) {
+        const float4 jv = jr[q];
+#pragma unroll
+        for (int rr = 0; rr < kMaxRB; ++rr) {
+          if (rr < rb) {
+            const float4 vv = reinterpret_cast<const float4 *>(sV + rr * kChunk)[q];
+            if constexpr (sizeof(Acc) == 8) {
+              acc[rr] += (double)jv.x * (double)vv.x + (double)jv.y * (double)vv.y +
+                         (double)jv.z * (double)vv.z + (double)jv.w * (double)vv.w;
+            } else {
+              acc[rr] = __fmaf_rn(jv.x, vv.x, acc[rr]);
+              acc[rr] = __fmaf_rn(jv.y, vv.y, acc[rr]);
+              acc[rr] = __fmaf_rn(jv.z, vv.z, acc[rr]);
+              acc[rr] = __fmaf_rn(jv.w, vv.w, acc[rr]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && c + 2 < nchunks && ok) issue(c + 2);
+  }
+  // every thread leaves with the same verdict, so no thread skips a later barrier
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+#pragma unroll
+  for (int rr = 0; rr < kMaxRB; ++rr) {
+    Acc v = acc[rr];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    acc[rr] = v;
+  }
+  return ok;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float *sJ = reinterpret_cast<float *>(smem);
+  float *sV = sJ + 2 * kRows * kChunk;
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ double red[kRows][kMaxRB];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * kRows;
+  const int r0 = blockIdx.y * a.rb;
+  const int rb = min(a.rb, a.R - r0);
+  const int rows = min(kRows, a.n - row0);
+  if (rows <= 0 || rb <= 0 || rb > kMaxRB) {
+    if (tid == 0) atomicOr(a.status, kErrBadShape);
+    return;
+  }
+  if (tid == 0) {
+    ptx::mbar_init(&full[0], 1);
+    ptx::mbar_init(&full[1], 1);
+    ptx::fence_mbar_init();
+  }
+  if (tid < kRows * kMaxRB) red[tid / kMaxRB][tid % kMaxRB] = 0.0;
+  __syncthreads();
+  float acc[kMaxRB];
+  const bool ok = field_rows<VARIANT == 2 ? 1 : 0, float>(a.J, a.jp, a.n, row0, rows, a.x_in,
+                                                          a.xp, r0, rb, sJ, sV, full, acc);
+  if (!ok) {
+    if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
+    return;
+  }
+  if (warp < rows && lane < rb) {
+    float f = 0.0f;
+#pragma unroll
+    for (int rr = 0; rr < kMaxRB; ++rr)
+      if (rr == lane) f = acc[rr];
+    const int i = row0 + warp, r = r0 + lane;
+    const size_t k = (size_t)r * a.xp + i;
+    float x = a.x_in[k], y = a.y[k];
+    const float hv = a.h ? a.h[i] : 0.0f;
+    if (VARIANT == 0) {
+      y = __fmaf_rn(a.coeff, f, y);
+      if (a.do_local) asb_local(x, y, a.amp_next, a.m, a.mts_dt, a.detune, a.kerr);
+    } else {
+      const float s = sgn(x);
+      if (VARIANT == 2) red[warp][lane] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
+      sb_update(f, hv, a.pump, a.c0, a.dt, a.dta0, x, y);
+    }
+    a.x_out[k] = x;
+    a.y[k] = y;
+  }
+  if (VARIANT == 2 && a.energy) {
+    __syncthreads();
+    if (tid < rb) {
+      double e = 0.0;
+      for (int w = 0; w < rows; ++w) e += red[w][tid];
+      atomicAdd(a.energy + r0 + tid, e);
+    }
+  }
+}
+
+template <typename Acc>
+__global__ void __launch_bounds__(kThreads) plain_energy_kernel(PlainEnergy a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float *sJ = reinterpret_cast<float *>(smem);
+  float *sV = sJ + 2 * kRows * kChunk;
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ double red[kRows][kMaxRB];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * kRows;
+  const int r0 = blockIdx.y * a.rb;
+  const int rb = min(a.rb, a.R - r0);
+  const int rows = min(kRows, a.n - row0);
+  if (rows <= 0 || rb <= 0 || rb > kMaxRB) {
+    if (tid == 0) atomicOr(a.status, kErrBadShape);
+    return;
+  }
+  if (tid == 0) {
+    ptx::mbar_init(&full[0], 1);
+    ptx::mbar_init(&full[1], 1);
+    ptx::fence_mbar_init();
+  }
+  if (tid < kRows * kMaxRB) red[tid / kMaxRB][tid % kMaxRB] = 0.0;
+  __syncthreads();
+  Acc acc[kMaxRB];
+  const bool ok =
+      field_rows<1, Acc>(a.J, a.jp, a.n, row0, rows, a.x, a.xp, r0, rb, sJ, sV, full, acc);
+  if (!ok) {
+    if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
+    return;
+  }
+  if (warp < rows && lane < rb) {
+    Acc f = Acc(0);
+#pragma unroll
+    for (int rr = 0; rr < kMaxRB; ++rr)
+      if (rr == lane) f = acc[rr];
+    const int i = row0 + warp, r = r0 + lane;
+    const double s = sgn(a.x[(size_t)r * a.xp + i]);
+    const double hv = a.h ? (double)a.h[i] : 0.0;
+    red[warp][lane] = -0.5 * s * (double)f - hv * s;
+  }
+  __syncthreads();
+  if (tid < rb) {
+    double e = 0.0;
+    for (int w = 0; w < rows; ++w) e += red[w][tid];
+    atomicAdd(a.energy + r0 + tid, e);
+  }
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ULL;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return z;
+}
+
+__device__ __forceinline__ float uniform_value(uint64_t seed, uint64_t e) {
+  const uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ULL * (e + 1));
+  const uint32_t u = (uint32_t)(z >> 40);
+  const float f = __fmul_rn((float)u, 5.9604644775390625e-08f);
+  const float t = __fadd_rn(__fmul_rn(f, 2.0f), -1.0f);
+  return __fmul_rn(t, 0.1f);
+}
+
+__global__ void init_uniform_kernel(float *x, float *y, int n, int R, int xp, uint64_t seed) {
+  const size_t total = (size_t)n * R;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / n, i = k % n;
+    const uint64_t e = 2 * (uint64_t)k;
+    x[r * xp + i] = uniform_value(seed, e);
+    y[r * xp + i] = uniform_value(seed, e + 1);
+  }
+}
+
+// prepare_points (SB/CUDA_GPU/m2_opt.cu:48-56) with per-spin state i (m2_opt.cu:136-137);
+// replica r gets trial r's draws. The float division by (float)MAX = 2^32 is an exact scaling.
+__global__ void init_reference_kernel(float *x, float *y, int n, int R, int xp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t st = (uint32_t)i;
+  for (int r = 0; r < R; ++r) {
+    uint32_t u[2];
+    for (int d = 0; d < 2; ++d) {
+      st ^= st << 13;
+      st ^= st >> 17;
+      st ^= st << 5;
+      u[d] = st;
+    }
+    const float qx = __fmul_rn(__uint2float_rn(u[0]), 2.3283064365386963e-10f);
+    const float qy = __fmul_rn(__uint2float_rn(u[1]), 2.3283064365386963e-10f);
+    x[(size_t)r * xp + i] = __double2float_rn(__ddiv_rn((double)qx, 10.0));
+    y[(size_t)r * xp + i] = __double2float_rn(__ddiv_rn((double)qy, 10.0));
+  }
+}
+
+__global__ void asb_local_kernel(float *x, float *y, int n, int R, int xp, float amp, int m,
+                                 float mts_dt, float detune, float kerr) {
+  const size_t total = (size_t)n * R;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / n, i = k % n, idx = r * xp + i;
+    float lx = x[idx], ly = y[idx];
+    asb_local(lx, ly, amp, m, mts_dt, detune, kerr);
+    x[idx] = lx;
+    y[idx] = ly;
+  }
+}
+
+__global__ void pad_rows_f32_kernel(const float *src, float *dst, int n, int jp) {
+  const size_t total = (size_t)n * jp;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = k / jp, j = k % jp;
+    dst[k] = j < (size_t)n ? src[i * n + j] : 0.0f;
+  }
+}
+
+int grid_for(size_t total) {
+  size_t g = (total + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  return (int)(g > 0 ? g : 1);
+}
+
+}  // namespace
+
+template <typename K>
+void set_smem_once(K kernel) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+}
+
+struct PlainAttrInit {
+  PlainAttrInit() {
+    set_smem_once(plain_step_kernel<0>);
+    set_smem_once(plain_step_kernel<1>);
+    set_smem_once(plain_step_kernel<2>);
+    set_smem_once(plain_energy_kernel<float>);
+    set_smem_once(plain_energy_kernel<double>);
+  }
+};
+
+void plain_attrs() { static PlainAttrInit once; }
+
+void init_kernel_attributes() { plain_attrs(); }
+
+cudaError_t launch_plain_step(const PlainStep &a, cudaStream_t st) {
+  plain_attrs();
+  if (a.rb < 1 || a.rb > kMaxRB || a.jp % 4 || a.xp % 4 || a.jp > a.xp) return cudaErrorInvalidValue;
+  dim3 grid((a.n + kRows - 1) / kRows, (a.R + a.rb - 1) / a.rb);
+  switch (a.variant) {
+    case 0:
+      plain_step_kernel<0><<<grid, kThreads, kSmemBytes, st>>>(a);
+      break;
+    case 1:
+      plain_step_kernel<1><<<grid, kThreads, kSmemBytes, st>>>(a);
+      break;
+    case 2:
+      plain_step_kernel<2><<<grid, kThreads, kSmemBytes, st>>>(a);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain_energy(const PlainEnergy &a, bool fp64, cudaStream_t st) {
+  plain_attrs();
+  if (a.rb < 1 || a.rb > kMaxRB || a.jp % 4 || a.xp % 4 || a.jp > a.xp) return cudaErrorInvalidValue;
+  dim3 grid((a.n + kRows - 1) / kRows, (a.R + a.rb - 1) / a.rb);
+  if (fp64) {
+    plain_energy_kernel<double><<<grid, kThreads, kSmemBytes, st>>>(a);
+  } else {
+    plain_energy_kernel<float><<<grid, kThreads, kSmemBytes, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_uniform(float *x, float *y, int n, int R, int xp, uint64_t seed,
+                                cudaStream_t st) {
+  init_uniform_kernel<<<grid_for((size_t)n * R), 256, 0, st>>>(x, y, n, R, xp, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_reference(float *x, float *y, int n, int R, int xp, cudaStream_t st) {
+  init_reference_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, n, R, xp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_asb_local(float *x, float *y, int n, int R, int xp, float amp, int m,
+                             float mts_dt, float detune, float kerr, cudaStream_t st) {
+  asb_local_kernel<<<grid_for((size_t)n * R), 256, 0, st>>>(x, y, n, R, xp, amp, m, mts_dt,
+                                                            detune, kerr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pad_rows_f32(const float *src, float *dst, int n, int jp, cudaStream_t st) {
+  pad_rows_f32_kernel<<<grid_for((size_t)n * jp), 256, 0, st>>>(src, dst, n, jp);
+  return cudaGetLastError();
+}
+
+}  // namespace sbk

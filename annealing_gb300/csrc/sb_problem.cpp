@@ -1,0 +1,424 @@
+// Host-side problem handling: graph reader, coefficients, schedule, exact energy evaluators.
+// No CUDA here; everything in this file works without a GPU.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "sb.h"
+#include "sb_host.h"
+
+extern "C" {
+
+const char *sb_status_string(sb_status s) {
+  switch (s) {
+    case SB_OK: return "ok";
+    case SB_ERR_INVALID_ARG: return "invalid argument";
+    case SB_ERR_IO: return "i/o error";
+    case SB_ERR_PARSE: return "parse error";
+    case SB_ERR_CUDA: return "cuda error";
+    case SB_ERR_OOM: return "out of memory";
+    case SB_ERR_UNSUPPORTED: return "unsupported";
+    case SB_ERR_TIMEOUT: return "device wait timed out";
+    case SB_ERR_BUSY: return "busy";
+    case SB_ERR_NOT_FOUND: return "not found";
+    case SB_ERR_CANCELLED: return "cancelled";
+    case SB_ERR_NO_DEVICE: return "no usable device";
+    case SB_ERR_PENDING: return "pending";
+  }
+  return "unknown status";
+}
+
+int32_t sb_abi_version(void) { return SB_ABI_VERSION; }
+
+void sb_params_default(sb_params *p, int32_t variant) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->variant = variant;
+  p->field_mode = SB_FIELD_AUTO;
+  p->init_mode = variant == SB_ASB ? SB_INIT_REFERENCE : SB_INIT_UNIFORM;
+  p->steps = variant == SB_ASB ? 100 : 1000;  // aSB: STEP of m2_opt.cu:22
+  p->replicas = 1;
+  p->seed = 1234;
+  p->dt = 1.25f;
+  p->a0 = 1.0f;
+  p->c0 = 0.0f;
+  p->mts_m = 2;          // m2_opt.cu:21
+  p->mts_dt = 0.5f;      // m2_opt.cu:19
+  p->coupling_dt = 1.0f; // m2_opt.cu:20
+  p->xi = 0.01565f;      // m2_opt.cu:18 (<= 0 selects 0.7 * detune / sqrt(N))
+  p->detune = 1.0f;      // m2_opt.cu:17
+  p->kerr = 1.0f;        // m2_opt.cu:16
+}
+
+void sb_graph_opts_default(sb_graph_opts *o) {
+  if (!o) return;
+  o->index_base = -1;
+  o->n_override = 0;
+  o->strict = 0;
+}
+
+float sb_pump(float a0, int32_t t, int32_t steps) {
+  float a = (float)((double)a0 * (double)t / (double)steps);
+  return a0 - a;
+}
+
+double sb_coupling_std(const sb_problem *p) {
+  if (!p || !p->J || p->n < 2) return 0.0;
+  const int n = p->n;
+  double s = 0.0, s2 = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const float *Ji = p->J + (size_t)i * n;
+    for (int j = 0; j < n; ++j) {
+      if (i == j) continue;
+      double v = (double)Ji[j];
+      s += v;
+      s2 += v * v;
+    }
+  }
+  double cnt = (double)n * (double)(n - 1);
+  double mean = s / cnt;
+  double var = s2 / cnt - mean * mean;
+  return var > 0.0 ? sqrt(var) : 0.0;
+}
+
+float sb_default_c0(const sb_problem *p) {
+  double sd = sb_coupling_std(p);
+  if (!(sd > 0.0)) sd = 1.0;
+  return (float)(0.5 / (sqrt((double)(p ? p->n : 1)) * sd));
+}
+
+sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out) {
+  if (!p || !p->J || !spins || !out || p->n <= 0) return SB_ERR_INVALID_ARG;
+  const int n = p->n;
+  int64_t e = 0;
+  for (int i = 0; i < n; ++i) {
+    const float *Ji = p->J + (size_t)i * n;
+    int64_t row = 0;
+    for (int j = i + 1; j < n; ++j) {
+      const float w = Ji[j];
+      if (w != floorf(w)) return SB_ERR_UNSUPPORTED;
+      row += (int64_t)w * (int64_t)spins[j];
+    }
+    e -= row * (int64_t)spins[i];
+    if (p->h) {
+      if (p->h[i] != floorf(p->h[i])) return SB_ERR_UNSUPPORTED;
+      e -= (int64_t)p->h[i] * (int64_t)spins[i];
+    }
+  }
+  *out = e;
+  return SB_OK;
+}
+
+double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
+  if (!p || !p->J || !spins || p->n <= 0) return 0.0;
+  const int n = p->n;
+  double e = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const float *Ji = p->J + (size_t)i * n;
+    double row = 0.0;
+    for (int j = i + 1; j < n; ++j) row += (double)Ji[j] * (double)spins[j];
+    e -= row * (double)spins[i];
+    if (p->h) e -= (double)p->h[i] * (double)spins[i];
+  }
+  return e;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Problem bookkeeping.
+
+void sbh::problem_scan(sb_problem *p) {
+  const int n = p->n;
+  bool integral = true;
+  double maxabs = 0.0;
+  int64_t edges = 0;
+  for (int i = 0; i < n; ++i) {
+    const float *Ji = p->J + (size_t)i * n;
+    for (int j = 0; j < n; ++j) {
+      const float w = Ji[j];
+      if (w == 0.0f) continue;
+      if (j > i) ++edges;
+      if (w != floorf(w)) integral = false;
+      const double a = fabs((double)w);
+      if (a > maxabs) maxabs = a;
+    }
+  }
+  if (p->h)
+    for (int i = 0; i < n; ++i)
+      if (p->h[i] != floorf(p->h[i])) integral = false;
+  p->integer_valued = integral ? 1 : 0;
+  p->max_abs_j = (int32_t)ceil(maxabs > 2e9 ? 2e9 : maxabs);
+  p->n_edges = edges;
+}
+
+extern "C" sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, const float *h) {
+  if (!p || !J || n <= 0) return SB_ERR_INVALID_ARG;
+  memset(p, 0, sizeof(*p));
+  const size_t nn = (size_t)n * (size_t)n;
+  p->J = (float *)malloc(nn * sizeof(float));
+  if (!p->J) return SB_ERR_OOM;
+  memcpy(p->J, J, nn * sizeof(float));
+  for (int i = 0; i < n; ++i) p->J[(size_t)i * n + i] = 0.0f;
+  if (h) {
+    p->h = (float *)malloc((size_t)n * sizeof(float));
+    if (!p->h) {
+      free(p->J);
+      p->J = nullptr;
+      return SB_ERR_OOM;
+    }
+    memcpy(p->h, h, (size_t)n * sizeof(float));
+  }
+  p->n = n;
+  p->lib_owned = 1;
+  sbh::problem_scan(p);
+  return SB_OK;
+}
+
+extern "C" void sb_problem_free(sb_problem *p) {
+  if (!p) return;
+  if (p->lib_owned) {
+    free(p->J);
+    free(p->h);
+  }
+  memset(p, 0, sizeof(*p));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Graph reader. The reference reads "N" then "%d%d%d" triples until EOF (SB/CUDA_GPU/m2_opt.cu:
+// 111-123) into a dense symmetric float matrix; a later line for the same pair wins. This reader
+// keeps that, and adds: real weights, "i i h" field lines, an optional edge count in the header,
+// 1-based indices, '#' comments, and errors instead of undefined behaviour for bad input.
+
+namespace {
+
+struct Cursor {
+  const char *p, *end;
+  int line = 1;
+};
+
+void skip_space(Cursor &c, bool stop_at_newline) {
+  while (c.p < c.end) {
+    const char ch = *c.p;
+    if (ch == '#') {
+      while (c.p < c.end && *c.p != '\n') ++c.p;
+      continue;
+    }
+    if (ch == '\n') {
+      if (stop_at_newline) return;
+      ++c.line;
+      ++c.p;
+      continue;
+    }
+    if (ch == ' ' || ch == '\t' || ch == '\r' || ch == ',') {
+      ++c.p;
+      continue;
+    }
+    return;
+  }
+}
+
+bool is_delim(char ch) {
+  return ch == ' ' || ch == '\t' || ch == '\r' || ch == '\n' || ch == ',' || ch == '#';
+}
+
+bool parse_int(Cursor &c, long long &v) {
+  const char *q = c.p;
+  bool neg = false;
+  if (q < c.end && (*q == '-' || *q == '+')) neg = (*q++ == '-');
+  if (q >= c.end || *q < '0' || *q > '9') return false;
+  long long acc = 0;
+  while (q < c.end && *q >= '0' && *q <= '9') {
+    acc = acc * 10 + (*q - '0');
+    if (acc > (1LL << 40)) return false;
+    ++q;
+  }
+  if (q < c.end && !is_delim(*q)) return false;
+  v = neg ? -acc : acc;
+  c.p = q;
+  return true;
+}
+
+bool parse_num(Cursor &c, double &v) {
+  long long iv;
+  Cursor save = c;
+  if (parse_int(c, iv)) {
+    v = (double)iv;
+    return true;
+  }
+  c = save;
+  char buf[64];
+  size_t len = 0;
+  while (c.p + len < c.end && !is_delim(c.p[len]) && len < sizeof(buf) - 1) {
+    buf[len] = c.p[len];
+    ++len;
+  }
+  if (len == 0) return false;
+  buf[len] = 0;
+  char *e = nullptr;
+  v = strtod(buf, &e);
+  if (e != buf + len || !isfinite(v)) return false;
+  c.p += len;
+  return true;
+}
+
+struct Triple {
+  long long i, j;
+  double w;
+  int line;
+};
+
+}  // namespace
+
+sb_status sbh::load_graph(const char *path, const sb_graph_opts *opts_in, sb_problem *out,
+                          std::string &err) {
+  if (!path || !out) return SB_ERR_INVALID_ARG;
+  sb_graph_opts opts;
+  sb_graph_opts_default(&opts);
+  if (opts_in) opts = *opts_in;
+  memset(out, 0, sizeof(*out));
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    err = std::string("cannot open ") + path;
+    return SB_ERR_IO;
+  }
+  std::vector<char> buf;
+  {
+    char tmp[1 << 16];
+    size_t got;
+    while ((got = fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
+    const bool bad = ferror(f) != 0;
+    fclose(f);
+    if (bad) {
+      err = std::string("read error on ") + path;
+      return SB_ERR_IO;
+    }
+  }
+  Cursor c{buf.data(), buf.data() + buf.size()};
+  skip_space(c, false);
+  long long header[2] = {0, -1};
+  int nh = 0;
+  while (c.p < c.end && *c.p != '\n') {
+    long long v;
+    if (!parse_int(c, v)) {
+      err = "line " + std::to_string(c.line) + ": header must be N or N E";
+      return SB_ERR_PARSE;
+    }
+    if (nh < 2) header[nh] = v;
+    ++nh;
+    skip_space(c, true);
+  }
+  if (nh < 1 || nh > 2) {
+    err = "header must be N or N E";
+    return SB_ERR_PARSE;
+  }
+  long long n = opts.n_override > 0 ? opts.n_override : header[0];
+  if (n <= 0 || n > 65536) {
+    err = "N out of range (1..65536): " + std::to_string(n);
+    return SB_ERR_PARSE;
+  }
+  std::vector<Triple> tr;
+  long long min_idx = (1LL << 40), max_idx = -1;
+  for (;;) {
+    skip_space(c, false);
+    if (c.p >= c.end) break;
+    Triple t;
+    t.line = c.line;
+    double wi, wj;
+    if (!parse_num(c, wi)) {
+      err = "line " + std::to_string(c.line) + ": expected an index";
+      return SB_ERR_PARSE;
+    }
+    skip_space(c, true);
+    if (c.p >= c.end || *c.p == '\n' || !parse_num(c, wj)) {
+      err = "line " + std::to_string(t.line) + ": expected 'i j w'";
+      return SB_ERR_PARSE;
+    }
+    skip_space(c, true);
+    if (c.p >= c.end || *c.p == '\n' || !parse_num(c, t.w)) {
+      err = "line " + std::to_string(t.line) + ": expected 'i j w'";
+      return SB_ERR_PARSE;
+    }
+    if (wi != floor(wi) || wj != floor(wj)) {
+      err = "line " + std::to_string(t.line) + ": indices must be integers";
+      return SB_ERR_PARSE;
+    }
+    t.i = (long long)wi;
+    t.j = (long long)wj;
+    if (t.i < min_idx) min_idx = t.i;
+    if (t.j < min_idx) min_idx = t.j;
+    if (t.i > max_idx) max_idx = t.i;
+    if (t.j > max_idx) max_idx = t.j;
+    tr.push_back(t);
+  }
+  int base = opts.index_base;
+  if (base < 0) base = (!tr.empty() && max_idx == n && min_idx >= 1) ? 1 : 0;
+  const size_t nn = (size_t)n * (size_t)n;
+  float *J = (float *)calloc(nn, sizeof(float));
+  if (!J) {
+    err = "host allocation of J failed";
+    return SB_ERR_OOM;
+  }
+  float *h = nullptr;
+  for (const Triple &t : tr) {
+    const long long i = t.i - base, j = t.j - base;
+    if (i < 0 || j < 0 || i >= n || j >= n) {
+      free(J);
+      free(h);
+      err = "line " + std::to_string(t.line) + ": index out of range for N=" + std::to_string(n);
+      return SB_ERR_PARSE;
+    }
+    const float w = (float)t.w;
+    if (i == j) {
+      if (!h) {
+        h = (float *)calloc((size_t)n, sizeof(float));
+        if (!h) {
+          free(J);
+          err = "host allocation of h failed";
+          return SB_ERR_OOM;
+        }
+      }
+      if (opts.strict && h[i] != 0.0f && h[i] != w) {
+        free(J);
+        free(h);
+        err = "line " + std::to_string(t.line) + ": conflicting field for spin " +
+              std::to_string(i);
+        return SB_ERR_PARSE;
+      }
+      h[i] = w;
+      continue;
+    }
+    float &a = J[(size_t)i * n + j];
+    if (opts.strict && a != 0.0f && a != w) {
+      free(J);
+      free(h);
+      err = "line " + std::to_string(t.line) + ": conflicting weight for edge " +
+            std::to_string(i) + "-" + std::to_string(j);
+      return SB_ERR_PARSE;
+    }
+    a = w;
+    J[(size_t)j * n + i] = w;
+  }
+  out->n = (int32_t)n;
+  out->J = J;
+  out->h = h;
+  out->lib_owned = 1;
+  problem_scan(out);
+  return SB_OK;
+}
+
+extern "C" sb_status sb_load_graph_ex(const char *path, const sb_graph_opts *opts,
+                                      sb_problem *out) {
+  std::string err;
+  sb_status s = sbh::load_graph(path, opts, out, err);
+  if (s != SB_OK) sbh::set_thread_error(err);
+  return s;
+}
+
+extern "C" sb_status sb_load_graph(const char *path, sb_problem *out) {
+  return sb_load_graph_ex(path, nullptr, out);
+}

@@ -1,0 +1,388 @@
+"""ctypes binding of the solver's C ABI (include/sb.h).
+
+This mirrors the reference program's contract (SB/CUDA_GPU/m2_opt.cu): read a graph, run SB
+trials, report one energy per trial and the best spin vector. There is no CPU fallback: if
+libsbsolve.so is missing this module raises on import of the library, and every solve runs the
+CUDA kernels in that library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsbsolve.so")
+
+# enums (sb.h)
+SB_OK, SB_ERR_PENDING = 0, 12
+ASB, BSB, DSB = 0, 1, 2
+FIELD_AUTO, FIELD_FP32, FIELD_TC = 0, 1, 2
+INIT_UNIFORM, INIT_REFERENCE = 0, 1
+DTYPE_NAMES = {0: "f32", 1: "fp8e4m3", 2: "bf16", 3: "bf16x2"}
+VARIANTS = {"asb": ASB, "bsb": BSB, "dsb": DSB}
+
+
+class GraphOpts(C.Structure):
+    _fields_ = [("index_base", C.c_int32), ("n_override", C.c_int32), ("strict", C.c_int32)]
+
+
+class ProblemStruct(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("J", C.POINTER(C.c_float)),
+        ("h", C.POINTER(C.c_float)),
+        ("integer_valued", C.c_int32),
+        ("max_abs_j", C.c_int32),
+        ("n_edges", C.c_int64),
+        ("lib_owned", C.c_int32),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("variant", C.c_int32),
+        ("field_mode", C.c_int32),
+        ("init_mode", C.c_int32),
+        ("steps", C.c_int32),
+        ("replicas", C.c_int32),
+        ("seed", C.c_uint64),
+        ("dt", C.c_float),
+        ("a0", C.c_float),
+        ("c0", C.c_float),
+        ("mts_m", C.c_int32),
+        ("mts_dt", C.c_float),
+        ("coupling_dt", C.c_float),
+        ("xi", C.c_float),
+        ("detune", C.c_float),
+        ("kerr", C.c_float),
+        ("trace", C.c_int32),
+        ("trace_all", C.c_int32),
+        ("profile", C.c_int32),
+    ]
+
+    @classmethod
+    def default(cls, variant: int = DSB, **kw) -> "Params":
+        p = cls()
+        lib().sb_params_default(C.byref(p), variant)
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+
+class ResultStruct(C.Structure):
+    _fields_ = [
+        ("best_spins", C.POINTER(C.c_int8)),
+        ("replica_energies", C.POINTER(C.c_double)),
+        ("energy_trace", C.POINTER(C.c_double)),
+        ("energy_trace_all", C.POINTER(C.c_double)),
+        ("final_x", C.POINTER(C.c_float)),
+        ("final_y", C.POINTER(C.c_float)),
+        ("best_energy", C.c_double),
+        ("best_energy_i64", C.c_int64),
+        ("best_replica", C.c_int32),
+        ("field_mode_used", C.c_int32),
+        ("field_dtype_used", C.c_int32),
+        ("energy_check_ok", C.c_int32),
+        ("device_ms", C.c_double),
+        ("kernel_ms_avg", C.c_double),
+        ("kernel_launches", C.c_int64),
+        ("total_ms", C.c_double),
+        ("spin_updates_per_s", C.c_double),
+    ]
+
+
+class DeviceOpts(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("stream", C.c_void_p),
+        ("hbm_budget_bytes", C.c_int64),
+        ("max_inflight", C.c_int32),
+    ]
+
+
+class ServingStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64),
+        ("finished", C.c_int64),
+        ("cancelled", C.c_int64),
+        ("inflight", C.c_int64),
+        ("queued", C.c_int64),
+        ("grouped_launches", C.c_int64),
+        ("busy_ms", C.c_double),
+        ("peak_inflight", C.c_int64),
+    ]
+
+
+# Every symbol include/sb.h declares, with its ctypes signature.
+_SIGS = {
+    "sb_status_string": (C.c_char_p, [C.c_int]),
+    "sb_abi_version": (C.c_int32, []),
+    "sb_params_default": (None, [C.POINTER(Params), C.c_int32]),
+    "sb_graph_opts_default": (None, [C.POINTER(GraphOpts)]),
+    "sb_load_graph": (C.c_int, [C.c_char_p, C.POINTER(ProblemStruct)]),
+    "sb_load_graph_ex": (C.c_int, [C.c_char_p, C.POINTER(GraphOpts), C.POINTER(ProblemStruct)]),
+    "sb_problem_init": (C.c_int, [C.POINTER(ProblemStruct), C.c_int32, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+    "sb_problem_free": (None, [C.POINTER(ProblemStruct)]),
+    "sb_coupling_std": (C.c_double, [C.POINTER(ProblemStruct)]),
+    "sb_default_c0": (C.c_float, [C.POINTER(ProblemStruct)]),
+    "sb_pump": (C.c_float, [C.c_float, C.c_int32, C.c_int32]),
+    "sb_energy_i64": (C.c_int, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8),
+                                C.POINTER(C.c_int64)]),
+    "sb_energy_f64": (C.c_double, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8)]),
+    "sb_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(DeviceOpts)]),
+    "sb_destroy": (C.c_int, [C.c_void_p]),
+    "sb_last_error": (C.c_char_p, [C.c_void_p]),
+    "sb_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(Params),
+                           C.POINTER(ResultStruct)]),
+    "sb_plan_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(Params),
+                                 C.POINTER(C.c_void_p)]),
+    "sb_plan_run": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(ResultStruct)]),
+    "sb_plan_destroy": (C.c_int, [C.c_void_p]),
+    "sb_plan_footprint": (C.c_int64, [C.POINTER(ProblemStruct), C.POINTER(Params)]),
+    "sb_submit": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(Params),
+                            C.POINTER(C.c_uint64)]),
+    "sb_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(ResultStruct), C.c_int32]),
+    "sb_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "sb_serving_stats_get": (C.c_int, [C.c_void_p, C.POINTER(ServingStats)]),
+}
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib() -> C.CDLL:
+    """Load libsbsolve.so (built in-tree by __graft_entry__.build()). Raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class SBError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        self.status = status
+        name = lib().sb_status_string(status).decode()
+        super().__init__(f"{name} ({status}): {msg}")
+
+
+def _check(status: int, ctx=None) -> None:
+    if status != SB_OK:
+        raise SBError(status, (lib().sb_last_error(ctx) or b"").decode())
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Problem:
+    """A dense symmetric Ising instance: H(s) = -sum_{i<j} J_ij s_i s_j - sum_i h_i s_i."""
+
+    def __init__(self, struct: ProblemStruct, owner=None):
+        self.s = struct
+        self._owner = owner
+
+    @classmethod
+    def from_dense(cls, J: np.ndarray, h: Optional[np.ndarray] = None) -> "Problem":
+        J = np.ascontiguousarray(J, dtype=np.float32)
+        n = J.shape[0]
+        if J.shape != (n, n):
+            raise ValueError("J must be square")
+        hh = None if h is None else np.ascontiguousarray(h, dtype=np.float32)
+        st = ProblemStruct()
+        _check(lib().sb_problem_init(C.byref(st), n, _fp(J), _fp(hh) if hh is not None else None))
+        return cls(st)
+
+    @classmethod
+    def load(cls, path: str, index_base: int = -1, n: int = 0, strict: bool = False) -> "Problem":
+        o = GraphOpts(index_base, n, 1 if strict else 0)
+        st = ProblemStruct()
+        _check(lib().sb_load_graph_ex(path.encode(), C.byref(o), C.byref(st)))
+        return cls(st)
+
+    @property
+    def n(self) -> int:
+        return self.s.n
+
+    @property
+    def J(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.s.J, shape=(self.n, self.n))
+
+    @property
+    def h(self) -> Optional[np.ndarray]:
+        return np.ctypeslib.as_array(self.s.h, shape=(self.n,)) if self.s.h else None
+
+    @property
+    def integer_valued(self) -> bool:
+        return bool(self.s.integer_valued)
+
+    def default_c0(self) -> float:
+        return lib().sb_default_c0(C.byref(self.s))
+
+    def energy(self, spins: np.ndarray) -> float:
+        sp = np.ascontiguousarray(spins, dtype=np.int8)
+        if self.integer_valued:
+            out = C.c_int64()
+            _check(lib().sb_energy_i64(C.byref(self.s), sp.ctypes.data_as(C.POINTER(C.c_int8)),
+                                       C.byref(out)))
+            return int(out.value)
+        return lib().sb_energy_f64(C.byref(self.s), sp.ctypes.data_as(C.POINTER(C.c_int8)))
+
+    def close(self) -> None:
+        if self.s.J:
+            lib().sb_problem_free(C.byref(self.s))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Result:
+    best_spins: np.ndarray
+    replica_energies: np.ndarray
+    best_energy: float
+    best_energy_i64: int
+    best_replica: int
+    field_mode: int
+    field_dtype: str
+    energy_check_ok: bool
+    device_ms: float
+    kernel_ms_avg: float
+    kernel_launches: int
+    total_ms: float
+    spin_updates_per_s: float
+    energy_trace: Optional[np.ndarray] = None
+    energy_trace_all: Optional[np.ndarray] = None
+    final_x: Optional[np.ndarray] = None
+    final_y: Optional[np.ndarray] = None
+
+
+class _ResultBuffers:
+    def __init__(self, n: int, params: Params, want_state: bool):
+        R, T = params.replicas, params.steps
+        self.spins = np.zeros(n, np.int8)
+        self.energies = np.zeros(R, np.float64)
+        self.trace = np.zeros(T + 1, np.float64) if params.trace else None
+        self.trace_all = np.zeros((T + 1, R), np.float64) if params.trace_all else None
+        self.x = np.zeros((R, n), np.float32) if want_state else None
+        self.y = np.zeros((R, n), np.float32) if want_state else None
+        r = ResultStruct()
+        r.best_spins = self.spins.ctypes.data_as(C.POINTER(C.c_int8))
+        r.replica_energies = self.energies.ctypes.data_as(C.POINTER(C.c_double))
+        if self.trace is not None:
+            r.energy_trace = self.trace.ctypes.data_as(C.POINTER(C.c_double))
+        if self.trace_all is not None:
+            r.energy_trace_all = self.trace_all.ctypes.data_as(C.POINTER(C.c_double))
+        if want_state:
+            r.final_x = _fp(self.x)
+            r.final_y = _fp(self.y)
+        self.r = r
+
+    def result(self) -> Result:
+        r = self.r
+        return Result(
+            best_spins=self.spins, replica_energies=self.energies, best_energy=r.best_energy,
+            best_energy_i64=r.best_energy_i64, best_replica=r.best_replica,
+            field_mode=r.field_mode_used, field_dtype=DTYPE_NAMES.get(r.field_dtype_used, "?"),
+            energy_check_ok=bool(r.energy_check_ok), device_ms=r.device_ms,
+            kernel_ms_avg=r.kernel_ms_avg, kernel_launches=r.kernel_launches, total_ms=r.total_ms,
+            spin_updates_per_s=r.spin_updates_per_s, energy_trace=self.trace,
+            energy_trace_all=self.trace_all, final_x=self.x, final_y=self.y)
+
+
+class Plan:
+    """J resident on the device; each run() is one solve (init, steps, final energy)."""
+
+    def __init__(self, ctx: "Context", problem: Problem, params: Params, want_state: bool):
+        self.ctx, self.problem, self.params, self.want_state = ctx, problem, params, want_state
+        h = C.c_void_p()
+        _check(lib().sb_plan_create(ctx.h, C.byref(problem.s), C.byref(params), C.byref(h)), ctx.h)
+        self.h = h
+
+    def run(self, seed: Optional[int] = None) -> Result:
+        buf = _ResultBuffers(self.problem.n, self.params, self.want_state)
+        sd = self.params.seed if seed is None else seed
+        _check(lib().sb_plan_run(self.h, sd, C.byref(buf.r)), self.ctx.h)
+        return buf.result()
+
+    def close(self) -> None:
+        if self.h:
+            lib().sb_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device, one stream (cudaStream_t as an integer handle, or None for an owned one)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None, hbm_budget: int = 0,
+                 max_inflight: int = 0):
+        o = DeviceOpts(device, stream or None, hbm_budget, max_inflight)
+        h = C.c_void_p()
+        _check(lib().sb_create(C.byref(h), C.byref(o)))
+        self.h = h
+
+    def solve(self, problem: Problem, params: Params, want_state: bool = False) -> Result:
+        buf = _ResultBuffers(problem.n, params, want_state)
+        _check(lib().sb_solve(self.h, C.byref(problem.s), C.byref(params), C.byref(buf.r)), self.h)
+        return buf.result()
+
+    def plan(self, problem: Problem, params: Params, want_state: bool = False) -> Plan:
+        return Plan(self, problem, params, want_state)
+
+    def submit(self, problem: Problem, params: Params) -> int:
+        t = C.c_uint64()
+        _check(lib().sb_submit(self.h, C.byref(problem.s), C.byref(params), C.byref(t)), self.h)
+        return t.value
+
+    def poll(self, ticket: int, n: int, params: Params, wait_ms: int = 0,
+             want_state: bool = False) -> Optional[Result]:
+        buf = _ResultBuffers(n, params, want_state)
+        st = lib().sb_poll(self.h, ticket, C.byref(buf.r), wait_ms)
+        if st == SB_ERR_PENDING:
+            return None
+        _check(st, self.h)
+        return buf.result()
+
+    def cancel(self, ticket: int) -> None:
+        _check(lib().sb_cancel(self.h, ticket), self.h)
+
+    def serving_stats(self) -> dict:
+        s = ServingStats()
+        _check(lib().sb_serving_stats_get(self.h, C.byref(s)), self.h)
+        return {k: getattr(s, k) for k, _ in ServingStats._fields_}
+
+    def close(self) -> None:
+        if self.h:
+            lib().sb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pump(a0: float, t: int, steps: int) -> float:
+    return lib().sb_pump(a0, t, steps)

@@ -1,0 +1,227 @@
+/*
+ * sb.h — C ABI of the GB300 simulated-bifurcation (SB) Ising solver.
+ *
+ * The reference program (strongshih/Annealing, SB/CUDA_GPU/m2_opt.cu) has no library
+ * interface: its contract is `./opt <graph>` -> output.txt (one energy per trial).
+ * Every entry point below names the piece of that program it replaces:
+ *
+ *   sb_load_graph   <- the graph reader in main()           SB/CUDA_GPU/m2_opt.cu:111-123
+ *   sb_solve        <- the trial loop + step loop + energy   SB/CUDA_GPU/m2_opt.cu:152-203
+ *                      (prepare_points :48-56, UpdateTwice :58-75, cublasSgemv :169,
+ *                       host energy :192-202)
+ *   sb_energy_i64 / sb_energy_f64
+ *                   <- the host energy loop                  SB/CUDA_GPU/m2_opt.cu:192-202
+ *   sb_params.trace <- print_energy (per-step energy trace)  SB/CUDA_GPU/m2_opt.cu:77-91
+ *                      (filled into sb_result.energy_trace)
+ *   sb_create / sb_destroy
+ *                   <- cublasCreate + the cudaMalloc block   SB/CUDA_GPU/m2_opt.cu:106-145
+ *
+ * The one library-style precedent in the reference repository is
+ *   float gpu_nmfa(int N, float* J, std::vector<float> betas, ...)   NMFA/CUDA_GPU/src/cuda_nmfa.h:10-14
+ * (caller-owned J, returns elapsed ms). This ABI keeps that shape — caller-owned host buffers,
+ * plain pointers and sizes — but reports errors as status codes instead of exit()/assert
+ * (SB/CUDA_GPU/m2_opt.cu:24-36, :113). Nothing here throws or exits.
+ *
+ * Threading: one CUDA stream per context; every call on a context is serialised by the context's
+ * own mutex, so a context may be shared by threads. Different contexts run concurrently.
+ *
+ * Energy convention (README.md:9-13): H(s) = -sum_{i<j} J_ij s_i s_j - sum_i h_i s_i, with
+ * s_i = (x_i > 0) ? +1 : -1 (SB/CUDA_GPU/m2_opt.cu:197-198). With h = 0 this is exactly the value
+ * the reference writes to output.txt (it stores -E, m2_opt.cu:202).
+ */
+#ifndef SB_H
+#define SB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SB_ABI_VERSION 1
+
+typedef enum sb_status {
+  SB_OK = 0,
+  SB_ERR_INVALID_ARG = 1,   /* a NULL pointer, a size out of range, an unknown enum value */
+  SB_ERR_IO = 2,            /* the graph file cannot be opened or read */
+  SB_ERR_PARSE = 3,         /* malformed line, index out of range, non-numeric weight */
+  SB_ERR_CUDA = 4,          /* a CUDA runtime call failed; sb_last_error() has the text */
+  SB_ERR_OOM = 5,           /* device or host allocation failed / over the context's HBM budget */
+  SB_ERR_UNSUPPORTED = 6,   /* the requested field mode cannot represent this problem exactly */
+  SB_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up (kernel returned a status) */
+  SB_ERR_BUSY = 8,          /* serving queue is full */
+  SB_ERR_NOT_FOUND = 9,     /* unknown ticket */
+  SB_ERR_CANCELLED = 10,    /* the request was cancelled before it finished */
+  SB_ERR_NO_DEVICE = 11,    /* no CUDA device, or the device is not sm_103 */
+  SB_ERR_PENDING = 12       /* sb_poll: request not finished yet */
+} sb_status;
+
+/* SB variants.
+ *  SB_ASB: the reference's adiabatic SB with multiple-time-step (MTS) integration:
+ *          M local sub-steps  x += detune*y*deltaT; y -= deltaT*(K x^3 + (detune - p) x)
+ *          then the coupling kick  y += DeltaT*xi * J x   (m2_opt.cu:58-75, :169), p = s/steps.
+ *  SB_BSB: ballistic SB (Goto et al., Sci. Adv. 7, eabe7953, 2021):
+ *          y += dt*(-(a0 - a(t)) x + c0 (J x + h)); x += dt*a0*y; |x|>1 -> x = sign x, y = 0.
+ *  SB_DSB: discrete SB: the same with J*sign(x) in place of J*x. */
+typedef enum sb_variant { SB_ASB = 0, SB_BSB = 1, SB_DSB = 2 } sb_variant;
+
+/* How the field J*v is computed.
+ *  SB_FIELD_AUTO: tensor cores when replicas >= 32 and the problem allows an exact/declared
+ *                 precision, otherwise the plain FP32 kernel.
+ *  SB_FIELD_FP32: the plain fused FP32 kernel, one launch per step (the drop-in form).
+ *  SB_FIELD_TC:   tcgen05 tensor cores. dSB with integer |J| <= 16: FP8 E4M3 operands, FP32
+ *                 accumulation (bit-exact). dSB with integer |J| <= 256: BF16 operands (bit-exact).
+ *                 dSB with real J: BF16 hi+lo split of J. bSB: BF16 hi+lo split of J and of x
+ *                 (three products), FP32 accumulation. aSB is not offered on tensor cores. */
+typedef enum sb_field_mode { SB_FIELD_AUTO = 0, SB_FIELD_FP32 = 1, SB_FIELD_TC = 2 } sb_field_mode;
+
+/* Initial x, y.
+ *  SB_INIT_UNIFORM:   x, y iid uniform in [-0.1, 0.1) from a counter-based hash of (seed, replica,
+ *                     spin); identical on the device and in the CPU oracle.
+ *  SB_INIT_REFERENCE: the reference's prepare_points (m2_opt.cu:48-56): per-spin xorshift32 state
+ *                     seeded with the spin index (m2_opt.cu:136-137), values in [0, 0.1);
+ *                     replica r takes the values trial r would get. */
+typedef enum sb_init_mode { SB_INIT_UNIFORM = 0, SB_INIT_REFERENCE = 1 } sb_init_mode;
+
+/* Graph-file options (sb_load_graph_ex). The reference format is: first integer N, then
+ * "i j w" lines with 0-based i != j (m2_opt.cu:115-121). Extensions accepted here:
+ * "i i h" lines give the field h_i (the SA_king/CUDA_GPU/tests/king.py:27-28 convention),
+ * a header "N E" (rudy / Gset), real-valued weights, and '#' comment lines. */
+typedef struct sb_graph_opts {
+  int32_t index_base;      /* 0 (reference) or 1 (rudy / Gset); -1 = autodetect: 1 if any index == N
+                              and none == 0 */
+  int32_t n_override;      /* > 0: use this N instead of the header (the reference ignores the header
+                              and uses its compile-time N, m2_opt.cu:10,115) */
+  int32_t strict;          /* 1: a repeated edge with a different weight is an error; 0: the last line
+                              wins, as in the reference */
+} sb_graph_opts;
+
+/* A dense problem instance. J is N*N row-major, symmetric, zero diagonal. */
+typedef struct sb_problem {
+  int32_t n;
+  float *J;                /* n*n */
+  float *h;                /* n, or NULL for h = 0 */
+  int32_t integer_valued;  /* 1 if every J_ij and h_i is an integer */
+  int32_t max_abs_j;       /* max |J_ij| rounded up (valid when integer_valued) */
+  int64_t n_edges;         /* number of nonzero J_ij with i < j */
+  int32_t lib_owned;       /* 1 when J/h were allocated by sb_load_graph (free with sb_problem_free) */
+} sb_problem;
+
+typedef struct sb_params {
+  int32_t variant;         /* sb_variant */
+  int32_t field_mode;      /* sb_field_mode */
+  int32_t init_mode;       /* sb_init_mode */
+  int32_t steps;           /* SB time steps (reference STEP, m2_opt.cu:22) */
+  int32_t replicas;        /* independent trajectories run together (reference TIMES runs them
+                              one after another, m2_opt.cu:12,152) */
+  uint64_t seed;
+  /* bSB / dSB */
+  float dt;                /* 1.25 */
+  float a0;                /* 1.0; a(t) = a0 * t / steps, t = 0 .. steps-1 (m2_opt.cu:158 form) */
+  float c0;                /* <= 0: 0.5 / (sqrt(N) * std(J_offdiag)) */
+  /* aSB (reference constants, m2_opt.cu:15-22) */
+  int32_t mts_m;           /* M = 2 */
+  float mts_dt;            /* deltaT = 0.5 */
+  float coupling_dt;       /* DeltaT = 1.0 */
+  float xi;                /* 0.01565 (m2_opt.cu:18); <= 0: 0.7 * detune / sqrt(N) (its comment, rho = 1) */
+  float detune;            /* 1.0 */
+  float kerr;              /* K = 1.0 */
+  int32_t trace;           /* 1: record the per-step energy trace (min over replicas) */
+  int32_t trace_all;       /* 1: record every replica's energy at every step */
+  int32_t profile;         /* 1: run the step loop launch by launch (no CUDA graph) with a CUDA
+                              event pair around every step kernel; fills kernel_ms_avg */
+} sb_params;
+
+/* Results. The caller owns every array; any of them may be NULL. */
+typedef struct sb_result {
+  int8_t *best_spins;          /* [n]  +1 / -1 of the lowest-energy replica (final state) */
+  double *replica_energies;    /* [replicas] final-state energy of each replica */
+  double *energy_trace;        /* [steps + 1] min-over-replicas energy of s(t), t = 0..steps (trace) */
+  double *energy_trace_all;    /* [(steps + 1) * replicas] (trace_all) */
+  float *final_x;              /* [replicas * n] final positions, replica-major */
+  float *final_y;              /* [replicas * n] final momenta */
+  /* scalar outputs */
+  double best_energy;          /* energy of best_spins */
+  int64_t best_energy_i64;     /* exact host re-check (integer problems); 0 otherwise */
+  int32_t best_replica;
+  int32_t field_mode_used;     /* SB_FIELD_FP32 or SB_FIELD_TC */
+  int32_t field_dtype_used;    /* 0 fp32, 1 fp8 e4m3, 2 bf16, 3 bf16 hi+lo */
+  int32_t energy_check_ok;     /* 1 when the host re-check agrees with the device energy */
+  double device_ms;            /* CUDA-event time of init + step loop + final energy */
+  double kernel_ms_avg;        /* average device time of one step-kernel launch (profile == 1), else 0 */
+  int64_t kernel_launches;     /* kernels this call launched on the device */
+  double total_ms;             /* host wall time of the call, copies included */
+  double spin_updates_per_s;   /* n * replicas * steps / (device_ms / 1e3) */
+} sb_result;
+
+typedef struct sb_device_opts {
+  int32_t device;              /* CUDA ordinal */
+  void *stream;                /* cudaStream_t to run on, or NULL for a stream the context owns */
+  int64_t hbm_budget_bytes;    /* serving admission budget; <= 0: 80% of free memory at create */
+  int32_t max_inflight;        /* serving: most requests resident at once (<= 0: 64) */
+} sb_device_opts;
+
+typedef struct sb_ctx sb_ctx;
+typedef struct sb_plan sb_plan;
+
+/* ---- library ---- */
+const char *sb_status_string(sb_status s);
+int32_t sb_abi_version(void);
+void sb_params_default(sb_params *p, int32_t variant);
+void sb_graph_opts_default(sb_graph_opts *o);
+
+/* ---- problems (host only, no GPU needed) ---- */
+sb_status sb_load_graph(const char *path, sb_problem *out);
+sb_status sb_load_graph_ex(const char *path, const sb_graph_opts *opts, sb_problem *out);
+sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, const float *h);
+void sb_problem_free(sb_problem *p);
+/* std of the off-diagonal couplings and the default c0 for that problem */
+double sb_coupling_std(const sb_problem *p);
+float sb_default_c0(const sb_problem *p);
+/* pump term a0 - a(t) for step t (shared by every kernel and the host) */
+float sb_pump(float a0, int32_t t, int32_t steps);
+/* exact energies: int64 when every J, h is integral (else SB_ERR_UNSUPPORTED), double otherwise */
+sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out);
+double sb_energy_f64(const sb_problem *p, const int8_t *spins);
+
+/* ---- contexts ---- */
+sb_status sb_create(sb_ctx **out, const sb_device_opts *opts);
+sb_status sb_destroy(sb_ctx *ctx);
+const char *sb_last_error(sb_ctx *ctx);
+
+/* One blocking solve from host buffers: upload J, run, copy results back. */
+sb_status sb_solve(sb_ctx *ctx, const sb_problem *p, const sb_params *params, sb_result *res);
+
+/* Device-resident form: sb_plan_create uploads J once (converted to the field dtype) and allocates
+ * the state; sb_plan_run runs one solve on it (init + steps + final energy) and copies the results
+ * out. Used for repeated solves and for timing with inputs resident in HBM. */
+sb_status sb_plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *params, sb_plan **out);
+sb_status sb_plan_run(sb_plan *plan, uint64_t seed, sb_result *res);
+sb_status sb_plan_destroy(sb_plan *plan);
+/* bytes of HBM a plan for (p, params) would hold */
+int64_t sb_plan_footprint(const sb_problem *p, const sb_params *params);
+
+/* ---- serving: continuous batching ----
+ * sb_submit copies the problem, queues it and returns a ticket at once. A worker thread admits
+ * queued requests while the context's HBM budget and in-flight limit allow, runs all admitted
+ * requests' steps together (one grouped launch per step over every resident request), retires
+ * each request at its own step budget and frees its memory for the next. */
+sb_status sb_submit(sb_ctx *ctx, const sb_problem *p, const sb_params *params, uint64_t *ticket);
+/* SB_OK when finished (res filled; the ticket is released), SB_ERR_PENDING otherwise.
+ * res->best_spins etc. must hold n / replicas entries. wait_ms < 0 blocks until done. */
+sb_status sb_poll(sb_ctx *ctx, uint64_t ticket, sb_result *res, int32_t wait_ms);
+sb_status sb_cancel(sb_ctx *ctx, uint64_t ticket);
+/* latency of every finished request in submission order: arrival->result ms, and queue stats */
+typedef struct sb_serving_stats {
+  int64_t submitted, finished, cancelled, inflight, queued;
+  int64_t grouped_launches;     /* device steps run by the serving loop */
+  double busy_ms;               /* time the worker had work resident */
+  int64_t peak_inflight;
+} sb_serving_stats;
+sb_status sb_serving_stats_get(sb_ctx *ctx, sb_serving_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SB_H */

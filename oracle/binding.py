@@ -1,0 +1,184 @@
+"""ctypes binding of oracle/libsboracle.so (the CPU oracle and the multithreaded CPU baseline).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline, never by the solver.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsboracle.so")
+_lib = None
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} missing: run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        sig = {
+            "oracle_xorshift32": (C.c_uint32, [C.POINTER(C.c_uint32)]),
+            "oracle_init_reference": (None, [C.c_int, C.c_int, f32p, f32p]),
+            "oracle_uniform_value": (C.c_float, [C.c_uint64, C.c_uint64]),
+            "oracle_init_uniform": (None, [C.c_int, C.c_int, C.c_uint64, f32p, f32p]),
+            "oracle_pump": (C.c_float, [C.c_float, C.c_int, C.c_int]),
+            "oracle_coupling_std": (C.c_double, [C.c_int, f32p]),
+            "oracle_default_c0": (C.c_float, [C.c_int, f32p]),
+            "oracle_field_f32": (None, [C.c_int, C.c_int, f32p, f32p, f32p]),
+            "oracle_field_f64": (None, [C.c_int, C.c_int, f32p, f64p, f64p]),
+            "oracle_sb_update_f32": (None, [C.c_int, C.c_int, f32p, C.c_void_p, f32p, f32p,
+                                            C.c_float, C.c_float, C.c_float, C.c_float]),
+            "oracle_sb_run_f32": (None, [C.c_int, C.c_int, C.c_int, f32p, C.c_void_p, f32p, f32p,
+                                         C.c_int, C.c_float, C.c_float, C.c_float, C.c_void_p,
+                                         C.c_void_p]),
+            "oracle_sb_run_f64": (None, [C.c_int, C.c_int, C.c_int, f32p, C.c_void_p, f32p, f32p,
+                                         f64p, f64p, C.c_int, C.c_double, C.c_double,
+                                         C.c_double]),
+            "oracle_asb_local": (None, [C.c_size_t, f32p, f32p, C.c_float, C.c_int, C.c_float,
+                                        C.c_float, C.c_float]),
+            "oracle_asb_coeff": (C.c_float, [C.c_float, C.c_float]),
+            "oracle_asb_run": (None, [C.c_int, C.c_int, f32p, f32p, f32p, C.c_int, C.c_int,
+                                      C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                      C.c_void_p, C.c_void_p]),
+            "oracle_energy_i64": (C.c_int, [C.c_int, f32p, C.c_void_p, i8p,
+                                            C.POINTER(C.c_int64)]),
+            "oracle_energy_f64": (C.c_double, [C.c_int, f32p, C.c_void_p, i8p]),
+            "oracle_energies_of_x": (None, [C.c_int, C.c_int, f32p, C.c_void_p, f32p, f64p]),
+            "oracle_cpu_run": (C.c_int, [C.c_int, C.c_int, C.c_int, f32p, C.c_void_p, f32p, f32p,
+                                         C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                                         C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.c_int]),
+        }
+        for k, (r, a) in sig.items():
+            fn = getattr(L, k)
+            fn.restype = r
+            fn.argtypes = a
+        _lib = L
+    return _lib
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def init_reference(n, R):
+    x = np.zeros((R, n), np.float32)
+    y = np.zeros((R, n), np.float32)
+    lib().oracle_init_reference(n, R, x, y)
+    return x, y
+
+
+def init_uniform(n, R, seed):
+    x = np.zeros((R, n), np.float32)
+    y = np.zeros((R, n), np.float32)
+    lib().oracle_init_uniform(n, R, seed, x, y)
+    return x, y
+
+
+def pump(a0, t, steps):
+    return lib().oracle_pump(a0, t, steps)
+
+
+def default_c0(J):
+    J = np.ascontiguousarray(J, np.float32)
+    return lib().oracle_default_c0(J.shape[0], J)
+
+
+def coupling_std(J):
+    J = np.ascontiguousarray(J, np.float32)
+    return lib().oracle_coupling_std(J.shape[0], J)
+
+
+def field_f32(J, v):
+    J = np.ascontiguousarray(J, np.float32)
+    v = np.ascontiguousarray(v, np.float32)
+    f = np.zeros_like(v)
+    lib().oracle_field_f32(J.shape[0], v.shape[0], J, v, f)
+    return f
+
+
+def sb_run_f32(variant, J, h, x, y, steps, a0, c0, dt, trace=False, trace_all=False):
+    """bSB (1) / dSB (2) in FP32 with the device's operation order. x, y updated in place."""
+    J = np.ascontiguousarray(J, np.float32)
+    R = x.shape[0]
+    tr = np.zeros(steps + 1) if trace else None
+    tra = np.zeros((steps + 1, R)) if trace_all else None
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    lib().oracle_sb_run_f32(variant, J.shape[0], R, J, _vp(hh), x, y, steps, a0, c0, dt,
+                            _vp(tr), _vp(tra))
+    return tr, tra
+
+
+def sb_run_f64(variant, J, h, x0, y0, steps, a0, c0, dt):
+    J = np.ascontiguousarray(J, np.float32)
+    R, n = x0.shape
+    xd = np.zeros((R, n))
+    yd = np.zeros((R, n))
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    lib().oracle_sb_run_f64(variant, n, R, J, _vp(hh), np.ascontiguousarray(x0),
+                            np.ascontiguousarray(y0), xd, yd, steps, a0, c0, dt)
+    return xd, yd
+
+
+def asb_run(J, x, y, steps, m=2, mts_dt=0.5, coupling_dt=1.0, xi=0.01565, detune=1.0, kerr=1.0,
+            want_trace=False):
+    J = np.ascontiguousarray(J, np.float32)
+    R, n = x.shape
+    xt = np.zeros((steps, R, n), np.float32) if want_trace else None
+    yt = np.zeros((steps, R, n), np.float32) if want_trace else None
+    lib().oracle_asb_run(n, R, J, x, y, steps, m, mts_dt, coupling_dt, xi, detune, kerr, _vp(xt),
+                         _vp(yt))
+    return xt, yt
+
+
+def asb_local(x, y, amp, m=2, mts_dt=0.5, detune=1.0, kerr=1.0):
+    lib().oracle_asb_local(x.size, x, y, amp, m, mts_dt, detune, kerr)
+
+
+def energy_i64(J, h, s):
+    J = np.ascontiguousarray(J, np.float32)
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    out = C.c_int64()
+    rc = lib().oracle_energy_i64(J.shape[0], J, _vp(hh), np.ascontiguousarray(s, np.int8),
+                                 C.byref(out))
+    if rc != 0:
+        raise ValueError("non-integer couplings")
+    return int(out.value)
+
+
+def energy_f64(J, h, s):
+    J = np.ascontiguousarray(J, np.float32)
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    return lib().oracle_energy_f64(J.shape[0], J, _vp(hh), np.ascontiguousarray(s, np.int8))
+
+
+def energies_of_x(J, h, x):
+    J = np.ascontiguousarray(J, np.float32)
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    e = np.zeros(x.shape[0])
+    lib().oracle_energies_of_x(J.shape[0], x.shape[0], J, _vp(hh), x, e)
+    return e
+
+
+def cpu_run(variant, J, h, x, y, steps, a0=1.0, c0=0.0, dt=1.25, m=2, mts_dt=0.5,
+            coupling_dt=1.0, xi=0.01565, detune=1.0, kerr=1.0, threads=None):
+    """Multithreaded FP32 port (the timed CPU baseline). x, y (R, n) updated in place."""
+    J = np.ascontiguousarray(J, np.float32)
+    R, n = x.shape
+    hh = None if h is None else np.ascontiguousarray(h, np.float32)
+    threads = threads or (os.cpu_count() or 1)
+    rc = lib().oracle_cpu_run(variant, n, R, J, _vp(hh), x, y, steps, a0, c0, dt, m, mts_dt,
+                              coupling_dt, xi, detune, kerr, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle_cpu_run failed: {rc}")
+    return threads

@@ -1,0 +1,140 @@
+"""C-ABI library: loads, exports what include/sb.h declares, host-side entry points (CPU only)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import annealing_gb300 as sb
+from annealing_gb300 import instances
+from annealing_gb300.sb import lib
+from oracle import binding as orc
+from oracle.reader import read_reference_format
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sb.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared_functions()
+    assert len(names) >= 20
+    L = lib()
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_status_strings():
+    assert lib().sb_abi_version() == 1
+    assert lib().sb_status_string(0) == b"ok"
+    assert lib().sb_status_string(3) == b"parse error"
+
+
+def test_defaults_follow_reference_constants():
+    p = sb.Params.default(sb.ASB)
+    # m2_opt.cu:15-22
+    assert (p.mts_m, p.mts_dt, p.coupling_dt, p.detune, p.kerr) == (2, 0.5, 1.0, 1.0, 1.0)
+    assert abs(p.xi - 0.01565) < 1e-9 and p.steps == 100 and p.replicas == 1
+    assert p.init_mode == sb.INIT_REFERENCE
+    q = sb.Params.default(sb.DSB)
+    assert (q.dt, q.a0, q.c0, q.init_mode) == (1.25, 1.0, 0.0, sb.INIT_UNIFORM)
+
+
+def test_pump_and_c0_match_oracle():
+    for steps in (1, 7, 1000, 3000):
+        for t in range(0, steps, max(1, steps // 13)):
+            assert sb.pump(1.0, t, steps) == orc.pump(1.0, t, steps)
+    for J in (instances.complete_pm1(100, 1), instances.gaussian(90, 2)[0],
+              instances.erdos_renyi(70, 0.1, 3, jmax=8, allow_zero=True)):
+        p = sb.Problem.from_dense(J)
+        assert p.default_c0() == orc.default_c0(J)
+
+
+def test_energy_evaluators_match_oracle():
+    rng = np.random.default_rng(1)
+    J = instances.erdos_renyi(120, 0.4, 11, jmax=8, allow_zero=True)
+    h = rng.integers(-5, 6, 120).astype(np.float32)
+    s = (rng.integers(0, 2, 120) * 2 - 1).astype(np.int8)
+    p = sb.Problem.from_dense(J, h)
+    assert p.integer_valued
+    assert p.energy(s) == orc.energy_i64(J, h, s)
+    Jg, hg = instances.gaussian(80, 5)
+    pg = sb.Problem.from_dense(Jg, hg)
+    assert not pg.integer_valued
+    assert pg.energy(s[:80]) == orc.energy_f64(Jg, hg, s[:80])
+
+
+def test_graph_reader_reference_format(tmp_path):
+    J = instances.erdos_renyi(60, 0.3, 2, jmax=3)
+    path = str(tmp_path / "g.txt")
+    instances.write_graph(path, J)
+    p = sb.Problem.load(path)
+    hdr, Jr = read_reference_format(path)
+    assert hdr == 60 and p.n == 60
+    assert np.array_equal(p.J, Jr) and np.array_equal(p.J, J)
+    assert p.h is None and p.integer_valued
+    assert p.s.n_edges == int(np.count_nonzero(np.triu(J, 1)))
+
+
+def test_graph_reader_fields_realweights_onebased(tmp_path):
+    Jg, hg = instances.gaussian(40, 3)
+    path = str(tmp_path / "g.txt")
+    instances.write_graph(path, Jg, hg, header_edges=True)
+    p = sb.Problem.load(path)
+    assert np.allclose(p.J, Jg, rtol=1e-7, atol=0) and np.allclose(p.h, hg, rtol=1e-7, atol=0)
+    assert not p.integer_valued
+    one = str(tmp_path / "one.txt")
+    with open(one, "w") as f:
+        f.write("# rudy style, 1-based\n3 2\n1 2 1\n2 3 -1\n")
+    q = sb.Problem.load(one)
+    assert q.n == 3 and q.J[0, 1] == 1 and q.J[1, 2] == -1 and q.J[2, 1] == -1
+    z = sb.Problem.load(one, index_base=0, n=4)  # explicit base and an N override
+    assert z.n == 4 and z.J[1, 2] == 1 and z.J[2, 3] == -1
+
+
+def test_graph_reader_errors(tmp_path):
+    def write(txt):
+        p = str(tmp_path / "bad.txt")
+        open(p, "w").write(txt)
+        return p
+
+    with pytest.raises(sb.SBError) as e:
+        sb.Problem.load(str(tmp_path / "missing.txt"))
+    assert e.value.status == 2
+    for txt in ("3\n0 1\n", "3\n0 1 x\n", "3\n0 5 1\n", "abc\n", "3\n0 1 1 2\n"):
+        with pytest.raises(sb.SBError) as e:
+            sb.Problem.load(write(txt))
+        assert e.value.status == 3, txt
+    # a later line for the same pair wins (m2_opt.cu:120-121), unless strict
+    p = sb.Problem.load(write("3\n0 1 1\n0 1 -2\n"))
+    assert p.J[0, 1] == -2 and p.J[1, 0] == -2
+    with pytest.raises(sb.SBError):
+        sb.Problem.load(write("3\n0 1 1\n0 1 -2\n"), strict=True)
+
+
+def test_footprint_is_positive_and_grows_with_replicas():
+    J = instances.complete_pm1(256, 1)
+    p = sb.Problem.from_dense(J)
+    f1 = lib().sb_plan_footprint(p.s, sb.Params.default(sb.DSB, replicas=1, field_mode=1))
+    f2 = lib().sb_plan_footprint(p.s, sb.Params.default(sb.DSB, replicas=64, field_mode=1))
+    assert 0 < f1 < f2
+
+
+def test_cli_prints_usage():
+    out = subprocess.run([os.path.join(ROOT, "annealing_gb300", "sb")], capture_output=True, text=True)
+    assert out.returncode == 0 and "Usage" in out.stdout
+
+
+def test_create_without_gpu_fails_cleanly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(sb.SBError) as e:
+        sb.Context(0)
+    assert e.value.status == 11

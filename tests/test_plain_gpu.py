@@ -1,0 +1,113 @@
+"""Plain fused FP32 kernel (one launch per step) against the CPU oracle, through the C ABI."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import annealing_gb300 as sb
+from annealing_gb300 import instances
+from oracle import binding as orc
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_dsb(ctx, J, h, R, steps, seed, **kw):
+    prob = sb.Problem.from_dense(J, h)
+    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_FP32, **kw)
+    res = ctx.solve(prob, prm, want_state=True)
+    n = J.shape[0]
+    x, y = orc.init_uniform(n, R, seed)
+    tr = orc.sb_run_f32(2, J, h, x, y, steps, 1.0, prob.default_c0(), 1.25,
+                        trace=bool(kw.get("trace")), trace_all=bool(kw.get("trace_all")))
+    return prob, res, x, y, tr
+
+
+@pytest.mark.parametrize("n,R,steps,h", [(200, 3, 60, False), (37, 9, 25, True), (2000, 1, 100, False),
+                                         (1, 1, 5, False), (130, 16, 0, True)])
+def test_dsb_fp32_bit_exact(ctx, n, R, steps, h):
+    J = instances.erdos_renyi(n, 0.5, seed=n, jmax=4, allow_zero=True) if n > 1 else np.zeros((1, 1), np.float32)
+    hv = np.random.default_rng(n).integers(-3, 4, n).astype(np.float32) if h else None
+    prob, res, x, y, _ = run_dsb(ctx, J, hv, R, steps, seed=17)
+    assert res.field_mode == sb.FIELD_FP32
+    np.testing.assert_array_equal(res.final_x, x)
+    np.testing.assert_array_equal(res.final_y, y)
+    e = orc.energies_of_x(J, hv, x)
+    np.testing.assert_array_equal(res.replica_energies, e)
+    assert res.energy_check_ok and res.best_energy_i64 == res.best_energy == e.min()
+    s = np.where(x[res.best_replica] > 0, 1, -1).astype(np.int8)
+    np.testing.assert_array_equal(res.best_spins, s)
+
+
+def test_dsb_trace_matches_oracle(ctx):
+    J = instances.complete_pm1(300, seed=3)
+    prob, res, x, y, (tr, tra) = run_dsb(ctx, J, None, 5, 40, seed=2, trace=1, trace_all=1)
+    np.testing.assert_array_equal(res.energy_trace_all, tra)
+    np.testing.assert_array_equal(res.energy_trace, tr)
+
+
+def test_bsb_fp32_tracks_fp64_oracle(ctx):
+    Jg, hg = instances.gaussian(512, seed=4)
+    prob = sb.Problem.from_dense(Jg, hg)
+    R, K = 4, 30
+    prm = sb.Params.default(sb.BSB, steps=K, replicas=R, seed=8, field_mode=sb.FIELD_FP32)
+    res = ctx.solve(prob, prm, want_state=True)
+    x0, y0 = orc.init_uniform(512, R, 8)
+    xd, yd = orc.sb_run_f64(1, Jg, hg, x0, y0, K, 1.0, float(prob.default_c0()), 1.25)
+    # FP32 field, first 30 steps: within 1e-4 absolute of the FP64 trajectory
+    assert np.max(np.abs(res.final_x - xd)) < 1e-4
+    assert np.max(np.abs(res.final_y - yd)) < 1e-4
+    assert res.energy_check_ok  # FP64 device energy of the returned spins == host FP64
+
+
+def test_asb_reference_init_and_trajectory(ctx):
+    n, R = 256, 3
+    J = instances.complete_pm1(n, seed=5)
+    prob = sb.Problem.from_dense(J)
+    p0 = sb.Params.default(sb.ASB, steps=0, replicas=R, field_mode=sb.FIELD_FP32)
+    r0 = ctx.solve(prob, p0, want_state=True)
+    xr, yr = orc.init_reference(n, R)
+    np.testing.assert_array_equal(r0.final_x, xr)
+    np.testing.assert_array_equal(r0.final_y, yr)
+    steps = 20
+    p = sb.Params.default(sb.ASB, steps=steps, replicas=R, field_mode=sb.FIELD_FP32)
+    r = ctx.solve(prob, p, want_state=True)
+    x, y = xr.copy(), yr.copy()
+    orc.asb_run(J, x, y, steps)
+    assert np.max(np.abs(r.final_x - x)) < 1e-4
+    assert r.energy_check_ok
+
+
+def test_plan_reuse_and_seeds(ctx):
+    J = instances.complete_pm1(128, seed=6)
+    prob = sb.Problem.from_dense(J)
+    prm = sb.Params.default(sb.DSB, steps=50, replicas=8, field_mode=sb.FIELD_FP32)
+    plan = ctx.plan(prob, prm, want_state=True)
+    a = plan.run(seed=1)
+    b = plan.run(seed=1)
+    c = plan.run(seed=2)
+    np.testing.assert_array_equal(a.final_x, b.final_x)
+    assert not np.array_equal(a.final_x, c.final_x)
+    plan.close()
+
+
+def test_profile_mode_reports_kernel_time(ctx):
+    J = instances.complete_pm1(512, seed=7)
+    prob = sb.Problem.from_dense(J)
+    prm = sb.Params.default(sb.DSB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1)
+    r = ctx.solve(prob, prm)
+    assert r.kernel_ms_avg > 0 and r.kernel_launches >= 22
+
+
+def test_cli_drop_in(tmp_path):
+    J = instances.complete_pm1(64, seed=8)
+    g = str(tmp_path / "k64.txt")
+    instances.write_graph(g, J)
+    out = subprocess.run([os.path.join(ROOT, "annealing_gb300", "sb"), g, "--trials", "3", "--steps", "20"],
+                         cwd=tmp_path, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    lines = open(tmp_path / "output.txt").read().split()
+    assert len(lines) == 3
+    spins = np.array(open(tmp_path / "best_spins.txt").read().split(), dtype=np.int8)
+    assert spins.shape == (64,) and int(min(map(int, lines))) == orc.energy_i64(J, None, spins)
