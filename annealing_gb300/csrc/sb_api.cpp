@@ -126,6 +126,10 @@ sb_status resolve_mode(const sb_problem *p, const sb_params *prm, int &mode, int
       dtype = sbk::kTcBf16Split;
   } else {
     dtype = sbk::kTcBf16Split;
+    if (prm->trace || prm->trace_all) {
+      err = "per-step energy traces of bSB are produced by the plain FP32 path only";
+      return SB_ERR_UNSUPPORTED;
+    }
   }
   return SB_OK;
 }
@@ -279,57 +283,64 @@ cudaError_t enqueue_energy(sb_plan *pl, const float *x, double *slot, cudaStream
   return sbk::launch_plain_energy(a, !pl->integral, st);
 }
 
-// Everything between the initial state and the final energy: steps x (step kernel [+ trace
-// energy pass]). With `evs`, an event pair brackets each step kernel (profiling).
+// Everything between the initial state and the final energy. Plain path: steps x (step kernel
+// [+ trace energy pass]), captured into a graph. Tensor-core path: one persistent launch.
+// With `evs`, an event pair brackets each step-kernel launch (profiling).
 cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> *evs,
                          int64_t *launches) {
   const sb_params &p = pl->prm;
   const bool tr = needs_trace(p);
   const int R = pl->R;
   int64_t nl = 0;
+  if (pl->mode == SB_FIELD_TC) {
+    if (p.steps > 0) {
+      if (evs) cudaEventRecord((*evs)[0], st);
+      cudaError_t e = sbk::tc_run(pl->tc, p.steps, p.steps, pl->dx[0], pl->dy, pl->dh, p.a0, pl->c0, p.dt,
+                                  pl->dta0, tr ? pl->denergy : nullptr, pl->dstatus, st);
+      if (e != cudaSuccess) return e;
+      if (evs) cudaEventRecord((*evs)[1], st);
+      nl = 1;
+    }
+    if (launches) *launches = nl;
+    return cudaSuccess;
+  }
   for (int t = 0; t < p.steps; ++t) {
     cudaError_t e;
     if (tr && p.variant != SB_DSB) {
       const int slot = p.variant == SB_ASB ? t + 1 : t;
-      const float *xin = pl->mode == SB_FIELD_TC ? pl->dx[0] : pl->dx[t & 1];
-      e = enqueue_energy(pl, xin, pl->denergy + (size_t)slot * R, st, -1);
+      e = enqueue_energy(pl, pl->dx[t & 1], pl->denergy + (size_t)slot * R, st, -1);
       if (e != cudaSuccess) return e;
       ++nl;
     }
     double *eslot = (tr && p.variant == SB_DSB) ? pl->denergy + (size_t)t * R : nullptr;
     if (evs) cudaEventRecord((*evs)[2 * t], st);
-    if (pl->mode == SB_FIELD_TC) {
-      e = sbk::tc_step(pl->tc, t, pl->dx[0], pl->dy, pl->dh, sb_pump(p.a0, t, p.steps), pl->c0,
-                       p.dt, pl->dta0, eslot, pl->dstatus, st);
-    } else {
-      sbk::PlainStep a;
-      memset(&a, 0, sizeof(a));
-      a.variant = p.variant;
-      a.n = pl->n;
-      a.R = R;
-      a.jp = pl->jp;
-      a.xp = pl->xp;
-      a.rb = R < 8 ? R : 8;
-      a.J = pl->dJ;
-      a.h = pl->dh;
-      a.x_in = pl->dx[t & 1];
-      a.x_out = pl->dx[(t + 1) & 1];
-      a.y = pl->dy;
-      a.pump = sb_pump(p.a0, t, p.steps);
-      a.c0 = pl->c0;
-      a.dt = p.dt;
-      a.dta0 = pl->dta0;
-      a.coeff = pl->coeff;
-      a.amp_next = (float)(t + 1) / (float)p.steps;
-      a.mts_dt = p.mts_dt;
-      a.detune = p.detune;
-      a.kerr = p.kerr;
-      a.m = p.mts_m;
-      a.do_local = (t + 1 < p.steps) ? 1 : 0;
-      a.energy = eslot;
-      a.status = pl->dstatus;
-      e = sbk::launch_plain_step(a, st);
-    }
+    sbk::PlainStep a;
+    memset(&a, 0, sizeof(a));
+    a.variant = p.variant;
+    a.n = pl->n;
+    a.R = R;
+    a.jp = pl->jp;
+    a.xp = pl->xp;
+    a.rb = R < 8 ? R : 8;
+    a.J = pl->dJ;
+    a.h = pl->dh;
+    a.x_in = pl->dx[t & 1];
+    a.x_out = pl->dx[(t + 1) & 1];
+    a.y = pl->dy;
+    a.pump = sb_pump(p.a0, t, p.steps);
+    a.c0 = pl->c0;
+    a.dt = p.dt;
+    a.dta0 = pl->dta0;
+    a.coeff = pl->coeff;
+    a.amp_next = (float)(t + 1) / (float)p.steps;
+    a.mts_dt = p.mts_dt;
+    a.detune = p.detune;
+    a.kerr = p.kerr;
+    a.m = p.mts_m;
+    a.do_local = (t + 1 < p.steps) ? 1 : 0;
+    a.energy = eslot;
+    a.status = pl->dstatus;
+    e = sbk::launch_plain_step(a, st);
     if (e != cudaSuccess) return e;
     if (evs) cudaEventRecord((*evs)[2 * t + 1], st);
     ++nl;
@@ -376,12 +387,13 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   }
   double kernel_ms = 0.0;
   if (p.profile) {
-    std::vector<cudaEvent_t> evs((size_t)2 * p.steps);
+    const int nmeas = pl->mode == SB_FIELD_TC ? (p.steps > 0 ? 1 : 0) : p.steps;
+    std::vector<cudaEvent_t> evs((size_t)2 * (nmeas > 0 ? nmeas : 1));
     for (auto &ev : evs) SB_CUDA(cudaEventCreate(&ev));
     int64_t nl = 0;
     cudaError_t e = enqueue_loop(pl, st, &evs, &nl);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (int t = 0; t < p.steps && e == cudaSuccess; ++t) {
+    for (int t = 0; t < nmeas && e == cudaSuccess; ++t) {
       float ms = 0.0f;
       e = cudaEventElapsedTime(&ms, evs[2 * t], evs[2 * t + 1]);
       kernel_ms += ms;
@@ -391,7 +403,11 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
       err = std::string("profiled step loop: ") + cudaGetErrorString(e);
       return SB_ERR_CUDA;
     }
-    if (p.steps > 0) kernel_ms /= p.steps;
+    if (nmeas > 0) kernel_ms /= nmeas;
+    launches += nl;
+  } else if (p.steps > 0 && pl->mode == SB_FIELD_TC) {
+    int64_t nl = 0;
+    SB_CUDA(enqueue_loop(pl, st, nullptr, &nl));
     launches += nl;
   } else if (p.steps > 0) {
     if (!pl->graph) {
@@ -489,6 +505,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   }
   res->device_ms = dev_ms;
   res->kernel_ms_avg = kernel_ms;
+  res->steps_per_launch = pl->mode == SB_FIELD_TC ? p.steps : 1;
   res->kernel_launches = launches;
   res->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   res->spin_updates_per_s =

@@ -91,6 +91,7 @@ class ResultStruct(C.Structure):
         ("energy_check_ok", C.c_int32),
         ("device_ms", C.c_double),
         ("kernel_ms_avg", C.c_double),
+        ("steps_per_launch", C.c_int32),
         ("kernel_launches", C.c_int64),
         ("total_ms", C.c_double),
         ("spin_updates_per_s", C.c_double),
@@ -263,6 +264,7 @@ class Result:
     energy_check_ok: bool
     device_ms: float
     kernel_ms_avg: float
+    steps_per_launch: int
     kernel_launches: int
     total_ms: float
     spin_updates_per_s: float
@@ -300,7 +302,8 @@ class _ResultBuffers:
             best_energy_i64=r.best_energy_i64, best_replica=r.best_replica,
             field_mode=r.field_mode_used, field_dtype=DTYPE_NAMES.get(r.field_dtype_used, "?"),
             energy_check_ok=bool(r.energy_check_ok), device_ms=r.device_ms,
-            kernel_ms_avg=r.kernel_ms_avg, kernel_launches=r.kernel_launches, total_ms=r.total_ms,
+            kernel_ms_avg=r.kernel_ms_avg, steps_per_launch=r.steps_per_launch,
+            kernel_launches=r.kernel_launches, total_ms=r.total_ms,
             spin_updates_per_s=r.spin_updates_per_s, energy_trace=self.trace,
             energy_trace_all=self.trace_all, final_x=self.x, final_y=self.y)
 

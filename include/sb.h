@@ -149,7 +149,9 @@ typedef struct sb_result {
   int32_t field_dtype_used;    /* 0 fp32, 1 fp8 e4m3, 2 bf16, 3 bf16 hi+lo */
   int32_t energy_check_ok;     /* 1 when the host re-check agrees with the device energy */
   double device_ms;            /* CUDA-event time of init + step loop + final energy */
-  double kernel_ms_avg;        /* average device time of one step-kernel launch (profile == 1), else 0 */
+  double kernel_ms_avg;        /* profile == 1: average device time of one launch of the step kernel
+                                  (the tensor-core kernel runs every step in one launch), else 0 */
+  int32_t steps_per_launch;    /* SB steps one step-kernel launch advances (1 plain, steps TC) */
   int64_t kernel_launches;     /* kernels this call launched on the device */
   double total_ms;             /* host wall time of the call, copies included */
   double spin_updates_per_s;   /* n * replicas * steps / (device_ms / 1e3) */

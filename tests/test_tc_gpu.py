@@ -1,0 +1,101 @@
+"""Tensor-core (tcgen05) path against the CPU oracle, through the C ABI.
+
+dSB with integer couplings runs on FP8 E4M3 (|J| <= 16) or BF16 (|J| <= 256) operands with FP32
+accumulation: the field is exact, the update uses the oracle's operation order, so trajectories
+and energies are bit-exact. Real couplings use BF16 hi + lo splits and are compared with the FP64
+oracle for the first steps.
+"""
+import numpy as np
+import pytest
+
+import annealing_gb300 as sb
+from annealing_gb300 import instances
+from oracle import binding as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def solve_tc(ctx, J, h, variant, R, steps, seed, **kw):
+    prob = sb.Problem.from_dense(J, h)
+    prm = sb.Params.default(variant, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC, **kw)
+    return prob, ctx.solve(prob, prm, want_state=True)
+
+
+def oracle_dsb(J, h, R, steps, seed, c0, trace=False):
+    n = J.shape[0]
+    x, y = orc.init_uniform(n, R, seed)
+    if trace or n * n * R * steps < 4e8:
+        tr, tra = orc.sb_run_f32(2, J, h, x, y, steps, 1.0, c0, 1.25, trace=trace, trace_all=trace)
+        return x, y, tra
+    orc.cpu_run(2, J, h, x, y, steps, 1.0, c0, 1.25)  # same operation order, multithreaded
+    return x, y, None
+
+
+@pytest.mark.parametrize("n,R,steps,jmax,dtype", [
+    (96, 40, 30, 1, "fp8e4m3"),
+    (300, 130, 40, 1, "fp8e4m3"),
+    (129, 33, 25, 16, "fp8e4m3"),
+    (257, 64, 25, 100, "bf16"),
+])
+def test_dsb_integer_bit_exact(ctx, n, R, steps, jmax, dtype):
+    J = instances.erdos_renyi(n, 0.6, seed=n + R, jmax=jmax, allow_zero=jmax > 1)
+    prob, res = solve_tc(ctx, J, None, sb.DSB, R, steps, seed=21)
+    assert res.field_mode == sb.FIELD_TC and res.field_dtype == dtype
+    x, y, _ = oracle_dsb(J, None, R, steps, 21, prob.default_c0())
+    np.testing.assert_array_equal(res.final_x, x)
+    np.testing.assert_array_equal(res.final_y, y)
+    np.testing.assert_array_equal(res.replica_energies, orc.energies_of_x(J, None, x))
+    assert res.energy_check_ok and res.best_energy_i64 == res.best_energy
+
+
+def test_dsb_with_field_and_trace(ctx):
+    n, R, steps = 200, 48, 30
+    J = instances.complete_pm1(n, seed=12)
+    h = np.random.default_rng(3).integers(-2, 3, n).astype(np.float32)
+    prob, res = solve_tc(ctx, J, h, sb.DSB, R, steps, seed=5, trace=1, trace_all=1)
+    x, y, tra = oracle_dsb(J, h, R, steps, 5, prob.default_c0(), trace=True)
+    np.testing.assert_array_equal(res.final_x, x)
+    np.testing.assert_array_equal(res.energy_trace_all, tra)
+    np.testing.assert_array_equal(res.energy_trace, tra.min(axis=1))
+
+
+def test_dsb_batched_2000_by_1024(ctx):
+    """The batched workload's shape (N = 2000 complete +-1, R = 1024) for 20 steps."""
+    J = instances.complete_pm1(2000, seed=1234)
+    prob, res = solve_tc(ctx, J, None, sb.DSB, 1024, 20, seed=1234)
+    x, y, _ = oracle_dsb(J, None, 1024, 20, 1234, prob.default_c0())
+    np.testing.assert_array_equal(res.final_x, x)
+    np.testing.assert_array_equal(res.final_y, y)
+    assert res.energy_check_ok
+
+
+def _fp64_errors(J, h, variant, R, steps, seed, c0, xg):
+    n = J.shape[0]
+    x0, y0 = orc.init_uniform(n, R, seed)
+    xd, _ = orc.sb_run_f64(variant, J, h, x0, y0, steps, 1.0, float(c0), 1.25)
+    xf, yf = x0.copy(), y0.copy()
+    orc.sb_run_f32(variant, J, h, xf, yf, steps, 1.0, c0, 1.25)
+    return np.max(np.abs(xg - xd)), np.max(np.abs(xf - xd))
+
+
+@pytest.mark.parametrize("variant", [sb.BSB, sb.DSB])
+def test_real_couplings_split_bf16_vs_fp64(ctx, variant):
+    """BF16 hi + lo operands: over the first 10 steps the trajectory stays within 2e-3 of the FP64
+    oracle (and within 50x the FP32 field's own distance to FP64 plus 1e-4)."""
+    J, h = instances.gaussian(384, seed=7)
+    R, K = 64, 10
+    prob, res = solve_tc(ctx, J, h, variant, R, K, seed=9)
+    assert res.field_dtype == "bf16x2"
+    err_tc, err_32 = _fp64_errors(J, h, variant, R, K, 9, prob.default_c0(), res.final_x)
+    print("split-bf16 err", err_tc, "fp32 err", err_32)
+    assert err_tc <= 2e-3
+    assert err_tc <= 50 * err_32 + 1e-4
+    assert res.energy_check_ok
+
+
+def test_profile_reports_persistent_launch(ctx):
+    J = instances.complete_pm1(512, seed=1)
+    prob = sb.Problem.from_dense(J)
+    prm = sb.Params.default(sb.DSB, steps=50, replicas=256, field_mode=sb.FIELD_TC, profile=1)
+    r = ctx.solve(prob, prm)
+    assert r.steps_per_launch == 50 and r.kernel_ms_avg > 0
