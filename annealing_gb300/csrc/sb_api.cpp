@@ -58,6 +58,7 @@ struct sb_plan {
   float *dJ = nullptr, *dh = nullptr, *dx[2] = {nullptr, nullptr}, *dy = nullptr;
   double *denergy = nullptr;
   uint32_t *dstatus = nullptr;
+  float *dpump = nullptr;  // [steps] a0 - a(t), the schedule every kernel reads
   sbk::TcEngine *tc = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -169,6 +170,8 @@ void plan_free_device(sb_plan *pl) {
   cudaFree(pl->dy);
   cudaFree(pl->denergy);
   cudaFree(pl->dstatus);
+  cudaFree(pl->dpump);
+  pl->dpump = nullptr;
   if (pl->ev0) cudaEventDestroy(pl->ev0);
   if (pl->ev1) cudaEventDestroy(pl->ev1);
   pl->graph = nullptr;
@@ -191,14 +194,15 @@ sb_status upload_problem(sb_plan *pl, const sb_problem *p, std::string &err) {
   SB_CUDA(cudaMemcpy2DAsync(pl->dJ, (size_t)pl->jp * sizeof(float), p->J, (size_t)n * sizeof(float),
                             (size_t)n * sizeof(float), (size_t)n, cudaMemcpyHostToDevice, st));
   if (p->h) SB_CUDA(cudaMemcpyAsync(pl->dh, p->h, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
-  if (pl->tc) {
-    sbk::tc_destroy(pl->tc);
-    pl->tc = nullptr;
-  }
   if (pl->mode == SB_FIELD_TC) {
-    sbk::TcSetup s{pl->prm.variant, pl->dtype, n, pl->R, pl->xp};
-    sb_status ts = sbk::tc_create(&pl->tc, s, pl->dJ, pl->jp, err, st);
-    if (ts != SB_OK) return ts;
+    if (pl->tc) {
+      // same shapes: re-convert the new couplings into the engine's operand buffers
+      SB_CUDA(sbk::tc_reload(pl->tc, pl->dJ, pl->jp, st));
+    } else {
+      sbk::TcSetup s{pl->prm.variant, pl->dtype, n, pl->R, pl->xp};
+      sb_status ts = sbk::tc_create(&pl->tc, s, pl->dJ, pl->jp, err, st);
+      if (ts != SB_OK) return ts;
+    }
   }
   pl->prob = p;
   return SB_OK;
@@ -250,7 +254,16 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->dy, xs);
   PLAN_ALLOC(pl->denergy, energy_slots(*prm) * (size_t)pl->R * sizeof(double));
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
+  PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
 #undef PLAN_ALLOC
+  {
+    std::vector<float> pumps((size_t)(prm->steps > 0 ? prm->steps : 1), 0.0f);
+    for (int t = 0; t < prm->steps; ++t) pumps[t] = sb_pump(prm->a0, t, prm->steps);
+    if (cudaMemcpy(pl->dpump, pumps.data(), pumps.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+      err = "uploading the pump schedule failed";
+      return fail(SB_ERR_CUDA);
+    }
+  }
   // padding columns of the state stay zero for the life of the plan
   if (cudaMemsetAsync(pl->dx[0], 0, xs, ctx->stream) != cudaSuccess ||
       (pl->dx[1] && cudaMemsetAsync(pl->dx[1], 0, xs, ctx->stream) != cudaSuccess) ||
@@ -295,7 +308,7 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
   if (pl->mode == SB_FIELD_TC) {
     if (p.steps > 0) {
       if (evs) cudaEventRecord((*evs)[0], st);
-      cudaError_t e = sbk::tc_run(pl->tc, p.steps, p.steps, pl->dx[0], pl->dy, pl->dh, p.a0, pl->c0, p.dt,
+      cudaError_t e = sbk::tc_run(pl->tc, p.steps, pl->dpump, pl->dx[0], pl->dy, pl->dh, pl->c0, p.dt,
                                   pl->dta0, tr ? pl->denergy : nullptr, pl->dstatus, st);
       if (e != cudaSuccess) return e;
       if (evs) cudaEventRecord((*evs)[1], st);
@@ -306,7 +319,9 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
   }
   for (int t = 0; t < p.steps; ++t) {
     cudaError_t e;
-    if (tr && p.variant != SB_DSB) {
+    // aSB: the pass before step t records the state after reference step t (slot t + 1); the
+    // final pass records slot `steps`, so the last step needs none here.
+    if (tr && p.variant != SB_DSB && !(p.variant == SB_ASB && t + 1 == p.steps)) {
       const int slot = p.variant == SB_ASB ? t + 1 : t;
       e = enqueue_energy(pl, pl->dx[t & 1], pl->denergy + (size_t)slot * R, st, -1);
       if (e != cudaSuccess) return e;

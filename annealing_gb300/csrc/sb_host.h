@@ -31,15 +31,18 @@ struct TcSetup {
 sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, std::string &err,
                     cudaStream_t st);
 void tc_destroy(TcEngine *e);
+// Re-converts new couplings (same n) into an existing engine's J operand.
+cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st);
 int64_t tc_footprint(const TcSetup &s);
 // Builds the step-0 operand (sign(x) or x hi/lo) from the initial state.
 cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st);
 // The whole step loop in one persistent cooperative launch: x / y live in TMEM between steps,
 // the operand ping-pongs between buffers 0 and 1 (step t reads t & 1). energy_trace (may be
 // null, dSB only): slot t (R doubles) += energy of s(t), t = 0 .. steps-1.
-cudaError_t tc_run(TcEngine *e, int steps, int total_steps, float *x, float *y, const float *h,
-                   float a0, float c0, float dt, float dta0, double *energy_trace,
-                   uint32_t *status, cudaStream_t st);
+// pumps: device array, pumps[t] = a0 - a(t) for t = 0 .. steps-1.
+cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *y, const float *h,
+                   float c0, float dt, float dta0, double *energy_trace, uint32_t *status,
+                   cudaStream_t st);
 int tc_units(const TcEngine *e);
 int tc_replica_tile(const TcEngine *e);
 // Field-only pass on operand buffer (t & 1): energy of s(t) per replica (dSB, integer J).

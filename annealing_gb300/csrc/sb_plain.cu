@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
       if (a.do_local) asb_local(x, y, a.amp_next, a.m, a.mts_dt, a.detune, a.kerr);
     } else {
       const float s = sgn(x);
-      if (VARIANT == 2) red[warp][lane] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
+      if (VARIANT == 2 && a.energy)
+        red[warp][lane] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
       sb_update(f, hv, a.pump, a.c0, a.dt, a.dta0, x, y);
     }
     a.x_out[k] = x;

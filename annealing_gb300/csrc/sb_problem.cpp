@@ -179,6 +179,17 @@ extern "C" sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, c
   return SB_OK;
 }
 
+extern "C" sb_status sb_problem_wrap(sb_problem *p, int32_t n, float *J, float *h) {
+  if (!p || !J || n <= 0) return SB_ERR_INVALID_ARG;
+  memset(p, 0, sizeof(*p));
+  p->n = n;
+  p->J = J;
+  p->h = h;
+  p->lib_owned = 0;
+  sbh::problem_scan(p);
+  return SB_OK;
+}
+
 extern "C" void sb_problem_free(sb_problem *p) {
   if (!p) return;
   if (p->lib_owned) {

@@ -56,10 +56,10 @@ struct alignas(64) TcArgs {
   uint32_t *barrier;       // grid barrier counter (zeroed before the launch)
   int n, R, xp, Kp, Rp, n_mtiles, n_rtiles, k_chunks;
   int steps, t0;           // steps to run; schedule offset
-  int total_steps;         // the schedule length (pump uses t / total_steps)
   int energy_only;         // 1: one contraction on V[buf0], energy of sign(x) into energy[R]
   int buf0;                // V buffer holding V(t0)
-  float a0, c0, dt, dta0;
+  const float *pumps;      // pumps[t] = a0 - a(t), computed on the host
+  float c0, dt, dta0;
 };
 
 template <int DT>
@@ -107,11 +107,6 @@ __device__ __forceinline__ void sb_update(float f, float hv, float pump, float c
     x = copysignf(1.0f, x);
     y = 0.0f;
   }
-}
-
-__device__ __forceinline__ float pump_at(float a0, int t, int steps) {
-  const double a = __ddiv_rn(__dmul_rn((double)a0, (double)t), (double)steps);
-  return __fsub_rn(a0, __double2float_rn(a));
 }
 
 // Write element (r, i) of the next operand.
@@ -181,7 +176,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accum_bar;
   __shared__ uint32_t tmem_base_sh;
-  __shared__ double ered[4][NR];
+  __shared__ float ered[4][NR];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.x % p.n_mtiles, rt = blockIdx.x / p.n_mtiles;
@@ -236,7 +231,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   }
 
   const int nsteps = p.energy_only ? 1 : p.steps;
+  const bool want_e = p.energy != nullptr && (p.energy_only || VARIANT == 2);
   uint32_t gchunk = 0;  // chunks issued so far (producer and MMA count identically)
+  int pre = 0;          // producer: chunks of the coming step whose J part is already in flight
   for (int ls = 0; ls < nsteps; ++ls) {
     const int t = p.t0 + ls;
     const int buf = (p.buf0 + ls) & 1;
@@ -245,18 +242,40 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++gchunk) {
         const int s = gchunk % STAGES;
         const uint32_t use = gchunk / STAGES;
-        if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
-          ok = false;
-          break;
-        }
         uint8_t *st = smem + s * kStage;
-        ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
         const int kx = kc * (kChunkBytes / C::kElem);
-        for (int a = 0; a < C::kAParts; ++a)
-          ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+        if (kc >= pre) {
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+          for (int a = 0; a < C::kAParts; ++a)
+            ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+        }
         for (int b = 0; b < C::kBParts; ++b)
           ptx::tma_load_2d(st + C::kAParts * kATile + b * kBTile, &p.tmB[buf][b], kx, r0,
                            &full_bar[s]);
+      }
+      // J does not change between steps: start the next step's first J tiles now, so they land
+      // while the epilogue and the grid barrier run.
+      pre = 0;
+      if (ok && ls + 1 < nsteps) {
+        const int npre = p.k_chunks < STAGES ? p.k_chunks : STAGES;
+        for (int kc = 0; kc < npre; ++kc) {
+          const uint32_t g = gchunk + kc;
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+          for (int a = 0; a < C::kAParts; ++a)
+            ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
+                             &full_bar[s]);
+          ++pre;
+        }
       }
     } else if (warp == 1 && lane == 0) {
       // ---- MMA issuer ----
@@ -296,8 +315,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       // ---- epilogue ----
       if (!ptx::mbar_wait(&accum_bar, (uint32_t)(ls & 1))) ok = false;
       ptx::tc_fence_after();
-      const bool want_e = p.energy != nullptr && (p.energy_only || VARIANT == 2);
-      const float pump = pump_at(p.a0, t, p.total_steps);
+      const float pump = p.energy_only ? 0.0f : p.pumps[t];
       uint8_t *const vnext[2] = {p.v[buf ^ 1][0], p.v[buf ^ 1][1]};
       for (int c = 0; c < NR; c += 16) {
         uint32_t va[16], vx[16], vy[16];
@@ -307,7 +325,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           ptx::tmem_ld16(t_y + lane_off + c, vy);
         }
         ptx::tmem_ld_wait();
-        double e[16];
+        float e2[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int r = r0 + c + j;
@@ -321,8 +339,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             x = __uint_as_float(vx[j]);
             y = __uint_as_float(vy[j]);
           }
-          const float s = sgnf(x);
-          e[j] = in ? (-0.5 * (double)s * (double)f - (double)hv * (double)s) : 0.0;
+          // 2 x (energy contribution) of s(t): -s f - 2 h s, an integer for integer J and h
+          if (want_e) {
+            const float s = sgnf(x);
+            e2[j] = in ? __fsub_rn(-__fmul_rn(s, f), __fmul_rn(2.0f * hv, s)) : 0.0f;
+          }
           if (!p.energy_only && in) {
             sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
             store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
@@ -337,7 +358,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         if (want_e) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            double v = e[j];
+            float v = e2[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0) ered[q][c + j] = v;
@@ -348,14 +369,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
     }
     ptx::tc_fence_before();
     // energy of s(t): one atomic per replica per CTA
-    const bool want_e = p.energy != nullptr && (p.energy_only || VARIANT == 2);
     if (want_e) {
       __syncthreads();
       for (int c = threadIdx.x; c < NR; c += kTcThreads) {
         const int r = r0 + c;
         if (r < p.R) {
-          double* slot = p.energy_only ? p.energy : p.energy + (size_t)t * p.R;
-          atomicAdd(slot + r, ered[0][c] + ered[1][c] + ered[2][c] + ered[3][c]);
+          double *slot = p.energy_only ? p.energy : p.energy + (size_t)t * p.R;
+          const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
+          atomicAdd(slot + r, 0.5 * sum);
         }
       }
     }
@@ -636,6 +657,12 @@ void tc_destroy(TcEngine *e) {
   delete e;
 }
 
+cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st) {
+  convert_j_kernel<<<grid_1d((size_t)e->Np * e->Kp), 256, 0, st>>>(dJ, e->s.n, jp, e->a[0], e->a[1], e->Np, e->Kp,
+                                                                   e->s.dtype);
+  return cudaGetLastError();
+}
+
 int tc_dtype(const TcEngine *e) { return e ? e->s.dtype : 0; }
 int tc_units(const TcEngine *e) { return e ? e->units : 0; }
 int tc_replica_tile(const TcEngine *e) { return e ? e->nr : 0; }
@@ -662,8 +689,8 @@ static cudaError_t launch(TcEngine *e, const TcArgs &a, cudaStream_t st) {
   return cudaLaunchKernelExC(&cfg, e->kernel, params);
 }
 
-cudaError_t tc_run(TcEngine *e, int steps, int total_steps, float *x, float *y, const float *h, float a0,
-                   float c0, float dt, float dta0, double *energy_trace, uint32_t *status, cudaStream_t st) {
+cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *y, const float *h, float c0,
+                   float dt, float dta0, double *energy_trace, uint32_t *status, cudaStream_t st) {
   if (steps <= 0) return cudaSuccess;
   TcArgs a = e->args;
   a.x = x;
@@ -673,10 +700,9 @@ cudaError_t tc_run(TcEngine *e, int steps, int total_steps, float *x, float *y, 
   a.status = status;
   a.steps = steps;
   a.t0 = 0;
-  a.total_steps = total_steps;
   a.energy_only = 0;
   a.buf0 = 0;
-  a.a0 = a0;
+  a.pumps = pumps;
   a.c0 = c0;
   a.dt = dt;
   a.dta0 = dta0;
@@ -700,7 +726,6 @@ cudaError_t tc_energy(TcEngine *e, int t, const float *x, const float *h, double
   a.status = status;
   a.steps = 1;
   a.t0 = 0;
-  a.total_steps = 1;
   a.energy_only = 1;
   a.buf0 = t & 1;
   return launch(e, a, st);

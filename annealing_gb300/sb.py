@@ -130,6 +130,7 @@ _SIGS = {
     "sb_load_graph_ex": (C.c_int, [C.c_char_p, C.POINTER(GraphOpts), C.POINTER(ProblemStruct)]),
     "sb_problem_init": (C.c_int, [C.POINTER(ProblemStruct), C.c_int32, C.POINTER(C.c_float),
                                   C.POINTER(C.c_float)]),
+    "sb_problem_wrap": (C.c_int, [C.POINTER(ProblemStruct), C.c_int32, C.c_void_p, C.c_void_p]),
     "sb_problem_free": (None, [C.POINTER(ProblemStruct)]),
     "sb_coupling_std": (C.c_double, [C.POINTER(ProblemStruct)]),
     "sb_default_c0": (C.c_float, [C.POINTER(ProblemStruct)]),
@@ -205,6 +206,13 @@ class Problem:
         st = ProblemStruct()
         _check(lib().sb_problem_init(C.byref(st), n, _fp(J), _fp(hh) if hh is not None else None))
         return cls(st)
+
+    @classmethod
+    def wrap(cls, n: int, J_ptr: int, h_ptr: int = 0, keepalive=None) -> "Problem":
+        """Refer to caller-owned host memory (e.g. pinned buffers) without copying."""
+        st = ProblemStruct()
+        _check(lib().sb_problem_wrap(C.byref(st), n, J_ptr, h_ptr or None))
+        return cls(st, owner=keepalive)
 
     @classmethod
     def load(cls, path: str, index_base: int = -1, n: int = 0, strict: bool = False) -> "Problem":

@@ -1,0 +1,343 @@
+"""Benchmark: SB spin-updates/s on the batched dSB workload (and the other workloads on request).
+
+Default workload (one GB300): complete graph N = 2000 with J_ij iid in {-1, +1}, R = 1024
+replicas, 2000 SB steps, dSB with the field J*sign(x) on the tensor cores (FP8 E4M3 operands,
+FP32 accumulation, bit-exact), x and y in FP32. One bench "step" is one full solve (init, 2000 SB
+steps, final energies, best spins back to the host).
+
+  value  spin-updates/s = N * R * sb_steps / solve time, J resident in HBM (sb_plan_run), device
+         time from CUDA events on the solver's stream; L2 is flushed (256 MB write) between solves
+  e2e    the same metric through sb_solve from pinned host memory: H2D of J and D2H of the
+         results inside the timed region
+  roofline  the persistent tensor-core kernel: algorithmic FLOPs (2 N^2 R per SB step) per launch
+         over its event-timed launch duration, against 2x the measured dense BF16 peak (FP8 rate)
+  cpu_baseline  the multithreaded FP32 CPU port of the same step loop (oracle/sb_cpu_baseline.c)
+         on this host's cores, on a bounded sample of the workload
+
+Multi-GPU: the path shards by replicas / instances only; each rank runs its own solve (weak
+scaling) and the value is the total over ranks divided by the slowest rank's time.
+`--impl reference` times the CPU port of the reference step loop (the reference has no CPU
+implementation of its own) on the same workload and prints its line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (variant, n, replicas, sb_steps, field, description)
+    "batched-dsb": ("dsb", 2000, 1024, 2000, "tc",
+                    "batched dSB: complete N=2000, J iid +-1, R=1024, 2000 steps, FP8 tensor-core field"),
+    "plain-dsb": ("dsb", 2000, 1, 1000, "fp32",
+                  "plain dSB: complete N=2000, J iid +-1, R=1, 1000 steps, fused FP32 kernel"),
+    "batched-bsb": ("bsb", 8192, 256, 3000, "tc",
+                    "batched bSB: complete N=8192, J ~ N(0,1/N), h ~ N(0,0.1), R=256, 3000 steps, "
+                    "BF16 hi+lo tensor-core field"),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_problem(name):
+    from annealing_gb300 import instances
+
+    variant, n, R, steps, field, desc = WORKLOADS[name]
+    if variant == "bsb":
+        J, h = instances.gaussian(n, seed=1234)
+    else:
+        J, h = instances.complete_pm1(n, seed=1234), None
+    return J, h
+
+
+def cpu_sample(name, J, h, budget_s=12.0, threads=None, max_steps=None):
+    """Time the CPU port on a bounded sample: all replicas, as many SB steps as fit ~budget_s."""
+    from oracle import binding as orc
+
+    variant, n, R, steps, field, desc = WORKLOADS[name]
+    vcode = {"asb": 0, "bsb": 1, "dsb": 2}[variant]
+    c0 = orc.default_c0(J)
+    x, y = orc.init_uniform(n, R, 1234)
+    t0 = time.perf_counter()
+    nthreads = orc.cpu_run(vcode, J, h, x, y, 1, 1.0, c0, 1.25, threads=threads)
+    t1 = time.perf_counter() - t0
+    k = max(1, int(budget_s / max(t1, 1e-6)))
+    k = min(k, steps if max_steps is None else max_steps)
+    t0 = time.perf_counter()
+    orc.cpu_run(vcode, J, h, x, y, k, 1.0, c0, 1.25, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n * R * k / dt, "unit": "spin-updates/s", "cores": nthreads, "kind": "port",
+            "sample": f"{k} SB steps x {R} replicas of the workload (N={n}), FP32, {nthreads} threads",
+            "seconds": dt, "steps": k}
+
+
+def run_reference(args, rank, world):
+    """The CPU port of the reference step loop, timed per bench step on a bounded sample."""
+    if rank != 0:
+        return
+    J, h = make_problem(args.workload)
+    variant, n, R, steps, field, desc = WORKLOADS[args.workload]
+    budget = max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample(args.workload, J, h, budget_s=budget / 4)
+    vals, samples = [], []
+    for _ in range(args.steps):
+        s = cpu_sample(args.workload, J, h, budget_s=budget)
+        vals.append(s["value"])
+        samples.append(s)
+    value = float(statistics.median(vals))
+    ms_per_step = 1e3 * n * R * steps / value  # time for one full solve at this rate
+    line = {
+        "impl": "reference", "metric": "SB spin-updates/s", "value": value, "unit": "spin-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": desc, "n": n, "replicas": R, "sb_steps": steps},
+        "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": samples[0]["cores"],
+                         "kind": "port", "sample": samples[0]["sample"]},
+        "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference ships no CPU implementation of the SB step loop; this is the C port "
+                "of its loop (UpdateTwice + dense matrix-vector field, and the bSB/dSB update) with "
+                "POSIX threads, each bench step a bounded sample of the workload",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import annealing_gb300 as sb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    variant, n, R, sb_steps, field, desc = WORKLOADS[args.workload]
+    vcode = {"asb": sb.ASB, "bsb": sb.BSB, "dsb": sb.DSB}[variant]
+    fmode = sb.FIELD_TC if field == "tc" else sb.FIELD_FP32
+    J, h = make_problem(args.workload)
+    stream = torch.cuda.current_stream(dev)
+    ctx = sb.Context(local_rank, stream=stream.cuda_stream)
+    prob = sb.Problem.from_dense(J, h)
+    prm = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=fmode, seed=1234 + rank)
+    plan = ctx.plan(prob, prm)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- value: J resident ----
+    for k in range(args.warmup):
+        plan.run(seed=1000 + k)
+    barrier()
+    times, launches, results = [], 0, []
+    with ClockSampler(local_rank) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = plan.run(seed=2000 + k)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            launches += r.kernel_launches
+            results.append(r)
+        barrier()
+        wall = time.perf_counter() - wall0
+    total_ms = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * R * sb_steps * args.steps / (total_ms * 1e-3)
+
+    # ---- roofline of the dominant kernel: one profiled solve (event pair around each launch) ----
+    prm_p = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=fmode, seed=77, profile=1)
+    plan_p = ctx.plan(prob, prm_p)
+    plan_p.run()
+    rp = plan_p.run(seed=78)
+    plan_p.close()
+    hbm, bf16, src = peaks()
+    flops_per_launch = 2.0 * n * n * R * rp.steps_per_launch
+    if field == "tc":
+        tc_peak = 2.0 * bf16 if results[0].field_dtype == "fp8e4m3" else bf16
+        achieved = flops_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                "frac": achieved / tc_peak, "traffic": None,
+                "kernel": "tc_sb_kernel (persistent, one launch per solve)",
+                "launch_ms": rp.kernel_ms_avg, "sb_steps_per_launch": rp.steps_per_launch,
+                "flops_per_launch": flops_per_launch,
+                "peak_source": (f"2 x {src} dense BF16 burst (FP8 E4M3 rate)" if results[0].field_dtype == "fp8e4m3"
+                                else f"{src} dense BF16 burst")}
+        if results[0].field_dtype == "bf16x2":
+            roof["note"] = "split operands run 3 products per field; achieved counts the algorithmic 2N^2R"
+    else:
+        bytes_per_launch = 4.0 * n * n + 16.0 * n * R
+        achieved = bytes_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "kernel": "plain_step_kernel",
+                "launch_ms": rp.kernel_ms_avg, "peak_source": f"{src} HBM copy",
+                "note": "J (16 MB) is L2-resident between steps; the fraction is of HBM bandwidth"}
+
+    # ---- e2e: host buffers through sb_solve ----
+    Jp = torch.from_numpy(J).pin_memory()
+    hp = torch.from_numpy(h).pin_memory() if h is not None else None
+    pw = sb.Problem.wrap(n, Jp.data_ptr(), hp.data_ptr() if hp is not None else 0, keepalive=(Jp, hp))
+    for k in range(max(1, args.warmup)):
+        ctx.solve(pw, prm)
+    barrier()
+    e2e_ms = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r = ctx.solve(pw, prm)  # H2D of J, solve, D2H of spins / energies; returns when done
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_total = float(sum(e2e_ms))
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = world * n * R * sb_steps * args.steps / (e2e_total * 1e-3)
+    h2d = J.nbytes + (h.nbytes if h is not None else 0)
+    d2h = n + 8 * R + 4  # best spins (int8), replica energies (f64), status word
+
+    if rank != 0:
+        plan.close()
+        ctx.close()
+        return
+    line = {
+        "metric": "SB spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp8e4m3": "fp8e4m3 field (f32 accumulate), f32 state",
+                  "bf16x2": "bf16 hi+lo field (f32 accumulate), f32 state",
+                  "bf16": "bf16 field (f32 accumulate), f32 state",
+                  "f32": "f32"}[results[0].field_dtype],
+        "data": "synthetic (seeded; the reference's WK2000_1.rud is not shipped)",
+        "config": {"workload": desc, "n": n, "replicas": R, "sb_steps": sb_steps,
+                   "variant": variant, "field": results[0].field_dtype,
+                   "parallelism": f"replicas-only x{world}",
+                   "l2": "flushed between timed solves (256 MB write outside the timed events)"},
+        "e2e": {"value": e2e_value, "unit": "spin-updates/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_total / args.steps},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "quality": {"best_energy": min(r.best_energy for r in results),
+                    "mean_best_energy": float(np.mean([r.best_energy for r in results])),
+                    "mean_replica_energy": float(np.mean(results[0].replica_energies)),
+                    "energy_check_ok": all(r.energy_check_ok for r in results)},
+        "wall_s": wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample(args.workload, J, h).items()
+                                if k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched-dsb")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -177,6 +177,9 @@ void sb_graph_opts_default(sb_graph_opts *o);
 sb_status sb_load_graph(const char *path, sb_problem *out);
 sb_status sb_load_graph_ex(const char *path, const sb_graph_opts *opts, sb_problem *out);
 sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, const float *h);
+/* Zero-copy form of sb_problem_init: p refers to the caller's J / h (which must stay alive and
+ * unchanged while p is used; J must already be symmetric with a zero diagonal). */
+sb_status sb_problem_wrap(sb_problem *p, int32_t n, float *J, float *h);
 void sb_problem_free(sb_problem *p);
 /* std of the off-diagonal couplings and the default c0 for that problem */
 double sb_coupling_std(const sb_problem *p);
