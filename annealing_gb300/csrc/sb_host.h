@@ -50,4 +50,22 @@ cudaError_t tc_energy(TcEngine *e, int t, const float *x, const float *h, double
                       uint32_t *status, cudaStream_t st);
 int tc_dtype(const TcEngine *e);
 
+// dSB on FP8 operands over buffers the caller provides; allocates nothing.
+struct TcExternal {
+  const float *J;   // device couplings, row pitch jp floats
+  int jp;
+  const float *h;   // device fields or null
+  int n, R, xp;
+  float *x, *y;     // device state [R][xp]: initial in, final out
+  uint8_t *a;       // FP8 J operand, tc_external_sizes() a_bytes
+  uint8_t *v0, *v1; // operand buffers, v_bytes each, zero on entry
+  uint32_t *barrier, *status;  // 64 bytes of barrier, one status word
+  const float *pumps;          // [steps]
+  int steps;
+  float c0, dt, dta0;
+  double *energy;   // [R] final energies, zero on entry
+};
+void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes);
+cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st);
+
 }  // namespace sbk

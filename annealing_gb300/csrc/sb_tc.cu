@@ -716,6 +716,59 @@ cudaError_t tc_step(TcEngine *, int, float *, float *, const float *, float, flo
   return cudaErrorNotSupported;  // the persistent kernel runs every step in one launch (tc_run)
 }
 
+void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes) {
+  const int r = choose_nr(n, R, sm_count());
+  const size_t Np = (size_t)(n + kBM - 1) / kBM * kBM, Kp = (size_t)(n + 127) / 128 * 128;
+  const size_t Rp = r > 0 ? (size_t)(R + r - 1) / r * r : 0;
+  *nr = r;
+  *a_bytes = Np * Kp;
+  *v_bytes = Rp * Kp;
+}
+
+cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
+  TcEngine e;  // on the stack: every buffer below belongs to the caller
+  e.s = TcSetup{2, kTcFp8, ext.n, ext.R, ext.xp};
+  e.nr = choose_nr(ext.n, ext.R, sm_count());
+  if (e.nr == 0 || !pick(&e, kTcFp8, 2, e.nr)) return cudaErrorInvalidValue;
+  e.Np = (ext.n + kBM - 1) / kBM * kBM;
+  e.Kp = (ext.n + 127) / 128 * 128;
+  e.Rp = (ext.R + e.nr - 1) / e.nr * e.nr;
+  e.n_mtiles = e.Np / kBM;
+  e.n_rtiles = e.Rp / e.nr;
+  e.units = e.n_mtiles * e.n_rtiles;
+  e.a[0] = ext.a;
+  e.v[0][0] = ext.v0;
+  e.v[1][0] = ext.v1;
+  e.barrier = ext.barrier;
+  TcArgs &g = e.args;
+  memset(&g, 0, sizeof(g));
+  if (!encode_2d(&g.tmA[0], e.a[0], 1, (uint64_t)e.Kp, (uint64_t)e.Np, kBM) ||
+      !encode_2d(&g.tmB[0][0], e.v[0][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr) ||
+      !encode_2d(&g.tmB[1][0], e.v[1][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr))
+    return cudaErrorInvalidValue;
+  g.v[0][0] = e.v[0][0];
+  g.v[1][0] = e.v[1][0];
+  g.barrier = e.barrier;
+  g.n = ext.n;
+  g.R = ext.R;
+  g.xp = ext.xp;
+  g.Kp = e.Kp;
+  g.Rp = e.Rp;
+  g.n_mtiles = e.n_mtiles;
+  g.n_rtiles = e.n_rtiles;
+  g.k_chunks = e.Kp / kChunkBytes;
+  cudaError_t ce = cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem);
+  if (ce != cudaSuccess) return ce;
+  convert_j_kernel<<<grid_1d((size_t)e.Np * e.Kp), 256, 0, st>>>(ext.J, ext.n, ext.jp, e.a[0], nullptr, e.Np, e.Kp,
+                                                                 kTcFp8);
+  if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+  if ((ce = tc_prepare(&e, ext.x, st)) != cudaSuccess) return ce;
+  if ((ce = tc_run(&e, ext.steps, ext.pumps, ext.x, ext.y, ext.h, ext.c0, ext.dt, ext.dta0, nullptr, ext.status,
+                   st)) != cudaSuccess)
+    return ce;
+  return tc_energy(&e, ext.steps, ext.x, ext.h, ext.energy, ext.status, st);
+}
+
 cudaError_t tc_energy(TcEngine *e, int t, const float *x, const float *h, double *energy, uint32_t *status,
                       cudaStream_t st) {
   TcArgs a = e->args;

@@ -153,6 +153,9 @@ _SIGS = {
     "sb_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(ResultStruct), C.c_int32]),
     "sb_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sb_serving_stats_get": (C.c_int, [C.c_void_p, C.POINTER(ServingStats)]),
+    "sb_dsb_solve_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib: Optional[C.CDLL] = None

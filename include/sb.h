@@ -226,6 +226,27 @@ typedef struct sb_serving_stats {
 } sb_serving_stats;
 sb_status sb_serving_stats_get(sb_ctx *ctx, sb_serving_stats *out);
 
+/* ---- dSB without any device allocation ----
+ * No counterpart in the reference (its program allocates everything itself, m2_opt.cu:106-145).
+ * For callers that cannot call cudaMalloc: code that lives inside a host process which owns the
+ * device memory budget (and hands out buffers from its own pool), or that must not pay the
+ * implicit synchronisation, latency or out-of-memory risk of cudaMalloc / cudaFree in the middle
+ * of its work. It runs the same solve as sb_solve with variant SB_DSB on the tensor-core path
+ * with FP8 operands (uniform initial state from `seed`, schedule a(t) = a0 t / steps), on device
+ * buffers the caller owns: d_J [n*n] row-major (symmetric, zero diagonal, integers |J| <= 16),
+ * d_h [n] or NULL, outputs d_x, d_y [replicas*n] (final state, replica-major) and
+ * d_energies [replicas] (final energies), all on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) of the current device. c0 must be given (> 0; sb_default_c0 on the host problem gives
+ * the usual value). The call returns when the work has finished.
+ * Scratch is one fixed array of 8,454,400 bytes in the library's device memory, held by every GPU
+ * that loads the library until the process exits; hence the limits n <= 2048, replicas <= 1024,
+ * steps <= 16384 (larger sizes return SB_ERR_INVALID_ARG). The first call on a device looks up
+ * the array's device address; make that first call before any stream capture. All calls share the
+ * array: calls that overlap on the GPU (other streams or threads at the same time) race. */
+sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, int32_t n, int32_t replicas,
+                               int32_t steps, uint64_t seed, float dt, float a0, float c0,
+                               float *d_x, float *d_y, double *d_energies, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
