@@ -59,7 +59,7 @@ struct TcExternal {
   float *x, *y;     // device state [R][xp]: initial in, final out
   uint8_t *a;       // FP8 J operand, tc_external_sizes() a_bytes
   uint8_t *v0, *v1; // operand buffers, v_bytes each, zero on entry
-  uint32_t *barrier, *status;  // 64 bytes of barrier, one status word
+  uint32_t *flags, *status;    // one flag word per unit (<= 512 bytes), one status word
   const float *pumps;          // [steps]
   int steps;
   float c0, dt, dta0;

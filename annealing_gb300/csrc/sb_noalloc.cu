@@ -38,7 +38,7 @@ constexpr size_t kOffV0 = kOffA + (size_t)kMaxN * kMaxN;
 constexpr size_t kOffV1 = kOffV0 + (size_t)kMaxReplicas * kMaxN;
 constexpr size_t kOffPump = kOffV1 + (size_t)kMaxReplicas * kMaxN;
 constexpr size_t kOffCtl = kOffPump + (size_t)kMaxSteps * sizeof(float);
-constexpr size_t kNoAllocScratchBytes = kOffCtl + 256;
+constexpr size_t kNoAllocScratchBytes = kOffCtl + 1024;
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -113,8 +113,8 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
   sbk::tc_external_sizes(n, replicas, &nr, &a_bytes, &v_bytes);
   if (nr == 0 || a_bytes > kOffV0 - kOffA || v_bytes > kOffV1 - kOffV0)
     return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: shape does not fit the scratch tiling");
-  uint32_t *ctl = (uint32_t *)(sc + kOffCtl);  // [0, 16): grid barrier (64 B), [16]: status
-  uint32_t *status = ctl + 16;
+  uint32_t *ctl = (uint32_t *)(sc + kOffCtl);  // [0, 128): per-unit step flags, [192]: status
+  uint32_t *status = ctl + 192;
   float *pumps = (float *)(sc + kOffPump);
   cudaError_t e;
   std::string where;
@@ -125,7 +125,7 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
   }
   // what must start at zero: control words, both operand buffers (their padding is never
   // written), the caller's energy accumulators
-  NA_CUDA(cudaMemsetAsync(ctl, 0, 256, st));
+  NA_CUDA(cudaMemsetAsync(ctl, 0, 1024, st));
   NA_CUDA(cudaMemsetAsync(sc + kOffV0, 0, v_bytes, st));
   NA_CUDA(cudaMemsetAsync(sc + kOffV1, 0, v_bytes, st));
   NA_CUDA(cudaMemsetAsync(d_energies, 0, (size_t)replicas * sizeof(double), st));
@@ -149,7 +149,7 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
     ext.a = sc + kOffA;
     ext.v0 = sc + kOffV0;
     ext.v1 = sc + kOffV1;
-    ext.barrier = ctl;
+    ext.flags = ctl;
     ext.status = status;
     ext.pumps = pumps;
     ext.steps = steps;

@@ -14,404 +14,41 @@
 //     memory through a STAGES-deep mbarrier ring; warp 1 (one lane) issues tcgen05.mma
 //     (kind::f8f6f4 for FP8 E4M3 operands, kind::f16 for BF16), committing each stage back to the
 //     producer and the finished accumulator to the epilogue;
-//   * warps 2..5 (one per TMEM lane quadrant) read the accumulator, x and y with tcgen05.ld, apply
-//     the SB update with the exact operation order of the CPU oracle, write x and y back to TMEM
-//     and the next step's operand V (sign as FP8/BF16, or x as BF16 hi + lo) to global memory;
-//   * a grid-wide barrier (release/acquire counter, bounded spin) separates the steps, because
-//     every unit needs all of V(t) before step t's contraction.
+//   * warps 2..9 (two per TMEM lane quadrant, each half of the replica columns) read the
+//     accumulator, x and y with tcgen05.ld, apply the SB update with the exact operation order of
+//     the CPU oracle, write x and y back to TMEM and the next step's operand V (sign as FP8/BF16,
+//     or x as BF16 hi + lo) to global memory; the accumulator is double-buffered in TMEM so the
+//     next contraction can start while the epilogue drains;
+//   * steps are ordered by per-unit release/acquire flags instead of a grid barrier: a unit
+//     publishes its V(t+1) chunk and the units of its replica column wait only for the chunks they
+//     load (bounded spins).
 // Operand dtypes: FP8 E4M3 holds +-1 and integers |J| <= 16 exactly; BF16 holds integers up to 256;
 // BF16 hi + lo (J = Jh + Jl, x = xh + xl) gives ~16 bits for real values, with the three products
 // Jh*xh + Jh*xl + Jl*xh accumulated in FP32. Integer fields are exact whenever every partial sum
 // stays below 2^24 in magnitude, which holds for n * max|J| < 2^24.
 // Every wait is bounded; a timeout sets a status bit, the kernel still frees its TMEM and returns.
 #include <cuda.h>
-#include <cuda_bf16.h>
-#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <mutex>
 #include <string>
 
 #include "sb_host.h"
-#include "sb_internal.h"
-#include "sb_ptx.cuh"
+#include "sb_tc_kernel.cuh"
 
 namespace sbk {
+
+// Kernel lookup by (variant, replica tile, epilogue mode); one definition per operand dtype, each
+// in its own translation unit (sb_tc_fp8.cu, sb_tc_bf16.cu, sb_tc_split.cu).
+bool tc_kernel_fp8(int variant, int nr, int emode, const void **k, size_t *smem);
+bool tc_kernel_bf16(int variant, int nr, int emode, const void **k, size_t *smem);
+bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem);
+
 namespace {
-
-constexpr int kTcThreads = 192;  // 6 warps: producer, MMA, 4 epilogue
-constexpr int kBM = 128;         // spins per unit (MMA M, TMEM lanes)
-constexpr int kChunkBytes = 128; // K bytes per stage (one 128-byte swizzle atom row)
-
-struct alignas(64) TcArgs {
-  CUtensorMap tmA[2];      // J operand parts: [Np rows][Kp] K-major
-  CUtensorMap tmB[2][2];   // V operand [buffer][part]: [Rp rows][Kp] K-major
-  float *x, *y;            // [R][xp] state (read at start, written at the end)
-  const float *h;          // [n] or null
-  uint8_t *v[2][2];        // V operand [buffer][part] base pointers (bytes)
-  double *energy;          // trace: [(steps + 1) * R] (step t -> slot t) or energy pass: [R]
-  uint32_t *status;
-  uint32_t *barrier;       // grid barrier counter (zeroed before the launch)
-  int n, R, xp, Kp, Rp, n_mtiles, n_rtiles, k_chunks;
-  int steps, t0;           // steps to run; schedule offset
-  int energy_only;         // 1: one contraction on V[buf0], energy of sign(x) into energy[R]
-  int buf0;                // V buffer holding V(t0)
-  const float *pumps;      // pumps[t] = a0 - a(t), computed on the host
-  float c0, dt, dta0;
-};
-
-template <int DT>
-struct DtTraits;
-template <>
-struct DtTraits<kTcFp8> {
-  static constexpr int kElem = 1, kParts = 1;
-};
-template <>
-struct DtTraits<kTcBf16> {
-  static constexpr int kElem = 2, kParts = 1;
-};
-template <>
-struct DtTraits<kTcBf16Split> {
-  static constexpr int kElem = 2, kParts = 2;
-};
-
-template <int DT, int VARIANT>
-struct Cfg {
-  static constexpr int kElem = DtTraits<DT>::kElem;
-  static constexpr int kAParts = DtTraits<DT>::kParts;
-  // V = sign(x) needs one part even when J is split; bSB's x is split with J.
-  static constexpr int kBParts = (DT == kTcBf16Split && VARIANT == 1) ? 2 : 1;
-  static constexpr int kKPerMma = 32 / kElem;  // 32 bytes of K per instruction
-  static constexpr int kMmaPerChunk = kChunkBytes / 32;
-};
-
-__host__ __device__ constexpr uint32_t make_idesc(int dt, int m, int n) {
-  // D = F32 (bits 4-5 = 1); A/B format: E4M3 = 0 (kind::f8f6f4) or BF16 = 1 (kind::f16);
-  // both K-major; N >> 3 at bits 17-22; M >> 4 at bits 24-28.
-  return (1u << 4) | ((dt == kTcFp8 ? 0u : 1u) << 7) | ((dt == kTcFp8 ? 0u : 1u) << 10) |
-         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : -1.0f; }
-
-__device__ __forceinline__ void sb_update(float f, float hv, float pump, float c0, float dt,
-                                          float dta0, float &x, float &y) {
-  const float fv = __fadd_rn(f, hv);
-  const float g = __fmul_rn(c0, fv);
-  const float force = __fmaf_rn(-pump, x, g);
-  y = __fmaf_rn(dt, force, y);
-  x = __fmaf_rn(dta0, y, x);
-  if (fabsf(x) > 1.0f) {
-    x = copysignf(1.0f, x);
-    y = 0.0f;
-  }
-}
-
-// Write element (r, i) of the next operand.
-template <int DT, int VARIANT>
-__device__ __forceinline__ void store_operand(uint8_t *const (&vb)[2], size_t idx, float x) {
-  if constexpr (DT == kTcFp8) {
-    vb[0][idx] = x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;  // E4M3 +1 / -1
-  } else if constexpr (Cfg<DT, VARIANT>::kBParts == 1) {
-    reinterpret_cast<uint16_t *>(vb[0])[idx] = x > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80;
-  } else {
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(x, __bfloat162float(hi)));
-    reinterpret_cast<__nv_bfloat16 *>(vb[0])[idx] = hi;
-    reinterpret_cast<__nv_bfloat16 *>(vb[1])[idx] = lo;
-  }
-}
-
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
-  uint32_t v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void red_release_add(uint32_t *p, uint32_t v) {
-  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Grid-wide barrier for a cooperative launch: every CTA adds 1, then waits (bounded) until the
-// counter reaches `target`. Returns false everywhere in the CTA if the wait gave up.
-__device__ __forceinline__ bool grid_barrier(uint32_t *counter, uint32_t target) {
-  __shared__ int ok_sh;
-  ptx::fence_proxy_async_global();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    __threadfence();
-    red_release_add(counter, 1u);
-    if (ld_acquire(counter) < target) {
-      const long long t0 = clock64();
-      while (ld_acquire(counter) < target) {
-        if (clock64() - t0 > ptx::kWaitCycles) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    ptx::fence_proxy_async_global();
-    ok_sh = ok;
-  }
-  __syncthreads();
-  return ok_sh != 0;
-}
-
-template <int DT, int VARIANT, int NR, int STAGES>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_constant__ TcArgs p) {
-  using C = Cfg<DT, VARIANT>;
-  constexpr int kATile = kBM * kChunkBytes;  // bytes per A part per stage
-  constexpr int kBTile = NR * kChunkBytes;   // bytes per B part per stage
-  constexpr int kStage = C::kAParts * kATile + C::kBParts * kBTile;
-  constexpr uint32_t kTx = (uint32_t)kStage;
-  constexpr uint32_t kCols = 4 * NR <= 32 ? 32 : (4 * NR <= 64 ? 64 : (4 * NR <= 128 ? 128 : (4 * NR <= 256 ? 256 : 512)));
-  constexpr uint32_t kIdesc = make_idesc(DT, kBM, NR);
-  static_assert(NR % 16 == 0 && NR >= 16 && NR <= 128, "replica tile");
-  static_assert(3 * NR <= 512, "accumulator + x + y must fit TMEM");
-
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accum_bar;
-  __shared__ uint32_t tmem_base_sh;
-  __shared__ float ered[4][NR];
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int mt = blockIdx.x % p.n_mtiles, rt = blockIdx.x / p.n_mtiles;
-  const int m0 = mt * kBM, r0 = rt * NR;
-  bool ok = true;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      ptx::mbar_init(&full_bar[s], 1);
-      ptx::mbar_init(&empty_bar[s], 1);
-    }
-    ptx::mbar_init(&accum_bar, 1);
-    ptx::fence_mbar_init();
-    for (int a = 0; a < C::kAParts; ++a) ptx::prefetch_tmap(&p.tmA[a]);
-    for (int b = 0; b < C::kBParts; ++b) {
-      ptx::prefetch_tmap(&p.tmB[0][b]);
-      ptx::prefetch_tmap(&p.tmB[1][b]);
-    }
-  }
-  if (warp == 1) {
-    ptx::tmem_alloc(&tmem_base_sh, kCols);
-    ptx::tmem_relinquish();
-  }
-  ptx::tc_fence_before();
-  __syncthreads();
-  ptx::tc_fence_after();
-  const uint32_t tmem = tmem_base_sh;
-  const uint32_t t_acc = tmem, t_x = tmem + NR, t_y = tmem + 2 * NR;
-
-  // epilogue geometry
-  const int q = warp & 3;                // TMEM lane quadrant of this warp
-  const int row = m0 + 32 * q + lane;    // spin index of this thread
-  const uint32_t lane_off = (uint32_t)(32 * q) << 16;
-  const bool is_epi = warp >= 2;
-  const float hv = (is_epi && p.h && row < p.n) ? p.h[row] : 0.0f;
-
-  // load x, y into TMEM
-  if (is_epi && !p.energy_only) {
-    for (int c = 0; c < NR; c += 16) {
-      uint32_t vx[16], vy[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int r = r0 + c + j;
-        const bool in = row < p.n && r < p.R;
-        vx[j] = __float_as_uint(in ? p.x[(size_t)r * p.xp + row] : 0.0f);
-        vy[j] = __float_as_uint(in ? p.y[(size_t)r * p.xp + row] : 0.0f);
-      }
-      ptx::tmem_st16(t_x + lane_off + c, vx);
-      ptx::tmem_st16(t_y + lane_off + c, vy);
-    }
-    ptx::tmem_st_wait();
-  }
-
-  const int nsteps = p.energy_only ? 1 : p.steps;
-  const bool want_e = p.energy != nullptr && (p.energy_only || VARIANT == 2);
-  uint32_t gchunk = 0;  // chunks issued so far (producer and MMA count identically)
-  int pre = 0;          // producer: chunks of the coming step whose J part is already in flight
-  for (int ls = 0; ls < nsteps; ++ls) {
-    const int t = p.t0 + ls;
-    const int buf = (p.buf0 + ls) & 1;
-    if (warp == 0 && lane == 0) {
-      // ---- TMA producer ----
-      for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++gchunk) {
-        const int s = gchunk % STAGES;
-        const uint32_t use = gchunk / STAGES;
-        uint8_t *st = smem + s * kStage;
-        const int kx = kc * (kChunkBytes / C::kElem);
-        if (kc >= pre) {
-          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
-            ok = false;
-            break;
-          }
-          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
-          for (int a = 0; a < C::kAParts; ++a)
-            ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
-        }
-        for (int b = 0; b < C::kBParts; ++b)
-          ptx::tma_load_2d(st + C::kAParts * kATile + b * kBTile, &p.tmB[buf][b], kx, r0,
-                           &full_bar[s]);
-      }
-      // J does not change between steps: start the next step's first J tiles now, so they land
-      // while the epilogue and the grid barrier run.
-      pre = 0;
-      if (ok && ls + 1 < nsteps) {
-        const int npre = p.k_chunks < STAGES ? p.k_chunks : STAGES;
-        for (int kc = 0; kc < npre; ++kc) {
-          const uint32_t g = gchunk + kc;
-          const int s = g % STAGES;
-          const uint32_t use = g / STAGES;
-          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
-            ok = false;
-            break;
-          }
-          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
-          for (int a = 0; a < C::kAParts; ++a)
-            ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
-                             &full_bar[s]);
-          ++pre;
-        }
-      }
-    } else if (warp == 1 && lane == 0) {
-      // ---- MMA issuer ----
-      for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++gchunk) {
-        const int s = gchunk % STAGES;
-        const uint32_t use = gchunk / STAGES;
-        if (!ptx::mbar_wait(&full_bar[s], use & 1)) {
-          ok = false;
-          break;
-        }
-        ptx::tc_fence_after();
-        const uint32_t sa = ptx::smem_u32(smem + s * kStage);
-        const uint32_t sb = sa + C::kAParts * kATile;
-        int prod = 0;
-#pragma unroll
-        for (int a = 0; a < C::kAParts; ++a) {
-#pragma unroll
-          for (int b = 0; b < C::kBParts; ++b) {
-            if (a + b > 1) continue;  // lo * lo is below the FP32 accumulator's resolution
-#pragma unroll
-            for (int k = 0; k < C::kMmaPerChunk; ++k) {
-              const uint64_t ad = ptx::smem_desc_sw128(sa + a * kATile + k * 32);
-              const uint64_t bd = ptx::smem_desc_sw128(sb + b * kBTile + k * 32);
-              const uint32_t acc = (kc > 0 || prod > 0 || k > 0) ? 1u : 0u;
-              if constexpr (DT == kTcFp8)
-                ptx::mma_f8(t_acc, ad, bd, kIdesc, acc);
-              else
-                ptx::mma_f16(t_acc, ad, bd, kIdesc, acc);
-            }
-            ++prod;
-          }
-        }
-        ptx::mma_commit(&empty_bar[s]);
-      }
-      ptx::mma_commit(&accum_bar);
-    } else if (is_epi) {
-      // ---- epilogue ----
-      if (!ptx::mbar_wait(&accum_bar, (uint32_t)(ls & 1))) ok = false;
-      ptx::tc_fence_after();
-      const float pump = p.energy_only ? 0.0f : p.pumps[t];
-      uint8_t *const vnext[2] = {p.v[buf ^ 1][0], p.v[buf ^ 1][1]};
-      for (int c = 0; c < NR; c += 16) {
-        uint32_t va[16], vx[16], vy[16];
-        ptx::tmem_ld16(t_acc + lane_off + c, va);
-        if (!p.energy_only) {
-          ptx::tmem_ld16(t_x + lane_off + c, vx);
-          ptx::tmem_ld16(t_y + lane_off + c, vy);
-        }
-        ptx::tmem_ld_wait();
-        float e2[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = r0 + c + j;
-          const bool in = ok && row < p.n && r < p.R;
-          const float f = __uint_as_float(va[j]);
-          float x, y;
-          if (p.energy_only) {
-            x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
-            y = 0.0f;
-          } else {
-            x = __uint_as_float(vx[j]);
-            y = __uint_as_float(vy[j]);
-          }
-          // 2 x (energy contribution) of s(t): -s f - 2 h s, an integer for integer J and h
-          if (want_e) {
-            const float s = sgnf(x);
-            e2[j] = in ? __fsub_rn(-__fmul_rn(s, f), __fmul_rn(2.0f * hv, s)) : 0.0f;
-          }
-          if (!p.energy_only && in) {
-            sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
-            store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
-          }
-          vx[j] = __float_as_uint(x);
-          vy[j] = __float_as_uint(y);
-        }
-        if (!p.energy_only) {
-          ptx::tmem_st16(t_x + lane_off + c, vx);
-          ptx::tmem_st16(t_y + lane_off + c, vy);
-        }
-        if (want_e) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float v = e2[j];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) ered[q][c + j] = v;
-          }
-        }
-      }
-      if (!p.energy_only) ptx::tmem_st_wait();
-    }
-    ptx::tc_fence_before();
-    // energy of s(t): one atomic per replica per CTA
-    if (want_e) {
-      __syncthreads();
-      for (int c = threadIdx.x; c < NR; c += kTcThreads) {
-        const int r = r0 + c;
-        if (r < p.R) {
-          double *slot = p.energy_only ? p.energy : p.energy + (size_t)t * p.R;
-          const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
-          atomicAdd(slot + r, 0.5 * sum);
-        }
-      }
-    }
-    if (p.energy_only) break;
-    // every unit needs all of V(t+1) before the next contraction
-    if (!grid_barrier(p.barrier, (uint32_t)(ls + 1) * gridDim.x)) ok = false;
-    ptx::tc_fence_after();
-    if (!ok) break;
-  }
-
-  // write the state back
-  if (is_epi && !p.energy_only && ok) {
-    for (int c = 0; c < NR; c += 16) {
-      uint32_t vx[16], vy[16];
-      ptx::tmem_ld16(t_x + lane_off + c, vx);
-      ptx::tmem_ld16(t_y + lane_off + c, vy);
-      ptx::tmem_ld_wait();
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int r = r0 + c + j;
-        if (row < p.n && r < p.R) {
-          p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
-          p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
-        }
-      }
-    }
-  }
-  if (!ok) atomicOr(p.status, kErrWaitTimeout);
-  ptx::tc_fence_before();
-  __syncthreads();
-  if (warp == 1) {
-    ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, kCols);
-  }
-}
+using namespace tck;
 
 // ---- operand preparation ----
 
@@ -489,12 +126,6 @@ bool encode_2d(CUtensorMap *m, void *base, int elem, uint64_t inner, uint64_t ou
   return r == CUDA_SUCCESS;
 }
 
-template <int DT, int VARIANT, int NR, int STAGES>
-constexpr size_t smem_bytes() {
-  using C = Cfg<DT, VARIANT>;
-  return (size_t)STAGES * (C::kAParts * kBM * kChunkBytes + C::kBParts * NR * kChunkBytes) + 1024;
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -504,40 +135,26 @@ struct TcEngine {
   int nr = 128, Np = 0, Kp = 0, Rp = 0, n_mtiles = 0, n_rtiles = 0, units = 0;
   uint8_t *a[2] = {nullptr, nullptr};
   uint8_t *v[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  uint32_t *barrier = nullptr;
+  uint32_t *flags = nullptr;
   TcArgs args{};
-  const void *kernel = nullptr;
+  const void *kernel[3] = {nullptr, nullptr, nullptr};  // by epilogue mode
   size_t smem = 0;
 };
 
 namespace {
 
-template <int DT, int VARIANT, int NR>
-void pick_kernel(TcEngine *e) {
-  constexpr int kStageBytes = Cfg<DT, VARIANT>::kAParts * kBM * kChunkBytes + Cfg<DT, VARIANT>::kBParts * NR * kChunkBytes;
-  constexpr int STAGES = (200 * 1024) / kStageBytes > 8 ? 8 : (200 * 1024) / kStageBytes;
-  e->kernel = reinterpret_cast<const void *>(&tc_sb_kernel<DT, VARIANT, NR, STAGES>);
-  e->smem = smem_bytes<DT, VARIANT, NR, STAGES>();
-}
-
-template <int DT, int VARIANT>
-bool pick_nr(TcEngine *e, int nr) {
-  switch (nr) {
-    case 32: pick_kernel<DT, VARIANT, 32>(e); return true;
-    case 64: pick_kernel<DT, VARIANT, 64>(e); return true;
-    case 128: pick_kernel<DT, VARIANT, 128>(e); return true;
-    default: return false;
-  }
-}
-
 bool pick(TcEngine *e, int dt, int variant, int nr) {
-  if (variant == 2) {
-    if (dt == kTcFp8) return pick_nr<kTcFp8, 2>(e, nr);
-    if (dt == kTcBf16) return pick_nr<kTcBf16, 2>(e, nr);
-    return pick_nr<kTcBf16Split, 2>(e, nr);
+  size_t smem = 0;
+  for (int m = 0; m < 3; ++m) {
+    const void *k = nullptr;
+    bool ok;
+    if (dt == kTcFp8) ok = tc_kernel_fp8(variant, nr, m, &k, &smem);
+    else if (dt == kTcBf16) ok = tc_kernel_bf16(variant, nr, m, &k, &smem);
+    else ok = tc_kernel_split(variant, nr, m, &k, &smem);
+    e->kernel[m] = ok ? k : nullptr;
   }
-  if (dt == kTcBf16Split) return pick_nr<kTcBf16Split, 1>(e, nr);
-  return false;
+  e->smem = smem;
+  return e->kernel[kEmodeStep] != nullptr;
 }
 
 int sm_count() {
@@ -547,20 +164,18 @@ int sm_count() {
   return n > 0 ? n : 1;
 }
 
-// Replica tile: the largest of {128, 64, 32} that keeps every unit co-resident (one CTA per SM).
+// Replica tile (MMA N): the smallest of {32, 64, 128} covering R when R <= 128 (no padded replicas
+// to compute), else 128; every unit needs its own SM for the whole solve (cooperative launch), so
+// 0 when the units outnumber the SMs.
 int choose_nr(int n, int R, int sms) {
   const int mt = (n + kBM - 1) / kBM;
-  for (int nr : {128, 64, 32}) {
-    const int rt = (R + nr - 1) / nr;
-    if (mt * rt <= sms) {
-      // prefer the smaller tile when it does not need more units than SMs and wastes less padding
-      return nr;
-    }
-  }
-  return 0;
+  const int nr = R <= 32 ? 32 : (R <= 64 ? 64 : 128);
+  return mt * ((R + nr - 1) / nr) <= sms ? nr : 0;
 }
 
 }  // namespace
+
+size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * sizeof(uint32_t) + 255) / 256 * 256; }
 
 int64_t tc_footprint(const TcSetup &s) {
   const int elem = s.dtype == kTcFp8 ? 1 : 2;
@@ -568,7 +183,7 @@ int64_t tc_footprint(const TcSetup &s) {
   const int64_t Rp = (s.R + 127) / 128 * 128;
   const int ap = s.dtype == kTcBf16Split ? 2 : 1;
   const int bp = (s.dtype == kTcBf16Split && s.variant == 1) ? 2 : 1;
-  return Np * Kp * elem * ap + 2 * Rp * Kp * elem * bp + 64;
+  return Np * Kp * elem * ap + 2 * Rp * Kp * elem * bp + 4096;
 }
 
 sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, std::string &err,
@@ -619,7 +234,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
       if ((ce = cudaMalloc(&e->v[b][pp], vbytes)) != cudaSuccess) return fail("cudaMalloc(V operand)", ce);
       if ((ce = cudaMemsetAsync(e->v[b][pp], 0, vbytes, st)) != cudaSuccess) return fail("memset", ce);
     }
-  if ((ce = cudaMalloc(&e->barrier, 64)) != cudaSuccess) return fail("cudaMalloc(barrier)", ce);
+  if ((ce = cudaMalloc(&e->flags, flag_bytes(e))) != cudaSuccess) return fail("cudaMalloc(flags)", ce);
   convert_j_kernel<<<grid_1d((size_t)e->Np * e->Kp), 256, 0, st>>>(dJ, s.n, jp, e->a[0], e->a[1], e->Np, e->Kp, s.dtype);
   if ((ce = cudaGetLastError()) != cudaSuccess) return fail("convert_j_kernel", ce);
   TcArgs &g = e->args;
@@ -632,7 +247,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
         return fail("cuTensorMapEncodeTiled(V)", cudaSuccess);
       g.v[b][pp] = e->v[b][pp];
     }
-  g.barrier = e->barrier;
+  g.flags = e->flags;
   g.n = s.n;
   g.R = s.R;
   g.xp = s.xp;
@@ -641,8 +256,10 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
   g.n_mtiles = e->n_mtiles;
   g.n_rtiles = e->n_rtiles;
   g.k_chunks = e->Kp * elem / kChunkBytes;
-  if ((ce = cudaFuncSetAttribute(e->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem)) != cudaSuccess)
-    return fail("cudaFuncSetAttribute", ce);
+  for (int m = 0; m < 3; ++m)
+    if (e->kernel[m] &&
+        (ce = cudaFuncSetAttribute(e->kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem)) != cudaSuccess)
+      return fail("cudaFuncSetAttribute", ce);
   *out = e;
   return SB_OK;
 }
@@ -653,7 +270,7 @@ void tc_destroy(TcEngine *e) {
   cudaFree(e->a[1]);
   for (int b = 0; b < 2; ++b)
     for (int pp = 0; pp < 2; ++pp) cudaFree(e->v[b][pp]);
-  cudaFree(e->barrier);
+  cudaFree(e->flags);
   delete e;
 }
 
@@ -673,7 +290,8 @@ cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-static cudaError_t launch(TcEngine *e, const TcArgs &a, cudaStream_t st) {
+static cudaError_t launch(TcEngine *e, int emode, const TcArgs &a, cudaStream_t st) {
+  if (!e->kernel[emode]) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3((unsigned)e->units);
@@ -686,7 +304,7 @@ static cudaError_t launch(TcEngine *e, const TcArgs &a, cudaStream_t st) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   void *params[1] = {const_cast<TcArgs *>(&a)};
-  return cudaLaunchKernelExC(&cfg, e->kernel, params);
+  return cudaLaunchKernelExC(&cfg, e->kernel[emode], params);
 }
 
 cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *y, const float *h, float c0,
@@ -700,20 +318,14 @@ cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *
   a.status = status;
   a.steps = steps;
   a.t0 = 0;
-  a.energy_only = 0;
   a.buf0 = 0;
   a.pumps = pumps;
   a.c0 = c0;
   a.dt = dt;
   a.dta0 = dta0;
-  cudaError_t ce = cudaMemsetAsync(e->barrier, 0, 64, st);
+  cudaError_t ce = cudaMemsetAsync(e->flags, 0, flag_bytes(e), st);
   if (ce != cudaSuccess) return ce;
-  return launch(e, a, st);
-}
-
-cudaError_t tc_step(TcEngine *, int, float *, float *, const float *, float, float, float, float, double *,
-                    uint32_t *, cudaStream_t) {
-  return cudaErrorNotSupported;  // the persistent kernel runs every step in one launch (tc_run)
+  return launch(e, energy_trace ? kEmodeStepTrace : kEmodeStep, a, st);
 }
 
 void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes) {
@@ -739,7 +351,7 @@ cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
   e.a[0] = ext.a;
   e.v[0][0] = ext.v0;
   e.v[1][0] = ext.v1;
-  e.barrier = ext.barrier;
+  e.flags = ext.flags;
   TcArgs &g = e.args;
   memset(&g, 0, sizeof(g));
   if (!encode_2d(&g.tmA[0], e.a[0], 1, (uint64_t)e.Kp, (uint64_t)e.Np, kBM) ||
@@ -748,7 +360,7 @@ cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
     return cudaErrorInvalidValue;
   g.v[0][0] = e.v[0][0];
   g.v[1][0] = e.v[1][0];
-  g.barrier = e.barrier;
+  g.flags = e.flags;
   g.n = ext.n;
   g.R = ext.R;
   g.xp = ext.xp;
@@ -779,9 +391,8 @@ cudaError_t tc_energy(TcEngine *e, int t, const float *x, const float *h, double
   a.status = status;
   a.steps = 1;
   a.t0 = 0;
-  a.energy_only = 1;
   a.buf0 = t & 1;
-  return launch(e, a, st);
+  return launch(e, kEmodeEnergy, a, st);
 }
 
 }  // namespace sbk

@@ -1,0 +1,502 @@
+// Tensor-core (tcgen05) SB kernel: the field J*V for R replicas as a GEMM on the 5th-generation
+// tensor cores, with the SB update fused into the epilogue.
+//
+// Replaces the reference's per-step field call (cublasSgemv, SB/CUDA_GPU/m2_opt.cu:169; the
+// tensor-op GEMM form cublasSgemm(N,1,N) of SB/CUDA_GPU/m2_opt2.cu:155-163; the FP16 form
+// cublasHgemm of SB/CUDA_GPU/m2_opt3.cu:161-162) by a contraction over all replicas at once:
+//     F[i][r] = sum_k J[i][k] * V[r][k],   V = sign(x) (dSB) or x (bSB).
+//
+// Kernel structure (one persistent cooperative launch for the whole solve):
+//   * the work is tiled into units of 128 spins (TMEM lanes, MMA M) x NR replicas (MMA N); each
+//     CTA owns one unit for every step, so its x and y live in TMEM for the whole solve
+//     (columns [NR, 2NR) and [2NR, 3NR); the FP32 accumulator is columns [0, NR));
+//   * warp 0 (one lane) streams J tiles and V tiles with 2-D TMA into 128-byte-swizzled shared
+//     memory through a STAGES-deep mbarrier ring; warp 1 (one lane) issues tcgen05.mma
+//     (kind::f8f6f4 for FP8 E4M3 operands, kind::f16 for BF16), committing each stage back to the
+//     producer and the finished accumulator to the epilogue;
+//   * warps 2..9 (two per TMEM lane quadrant, each half of the replica columns) read the
+//     accumulator, x and y with tcgen05.ld, apply the SB update with the exact operation order of
+//     the CPU oracle, write x and y back to TMEM and the next step's operand V (sign as FP8/BF16,
+//     or x as BF16 hi + lo) to global memory; the accumulator is double-buffered in TMEM so the
+//     next contraction can start while the epilogue drains;
+//   * steps are ordered by per-unit release/acquire flags instead of a grid barrier: a unit
+//     publishes its V(t+1) chunk and the units of its replica column wait only for the chunks they
+//     load (bounded spins).
+// Operand dtypes: FP8 E4M3 holds +-1 and integers |J| <= 16 exactly; BF16 holds integers up to 256;
+// BF16 hi + lo (J = Jh + Jl, x = xh + xl) gives ~16 bits for real values, with the three products
+// Jh*xh + Jh*xl + Jl*xh accumulated in FP32. Integer fields are exact whenever every partial sum
+// stays below 2^24 in magnitude, which holds for n * max|J| < 2^24.
+// Every wait is bounded; a timeout sets a status bit, the kernel still frees its TMEM and returns.
+// tcgen05 SB kernel template (shared by the per-dtype instantiation files and the host engine).
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sb_internal.h"
+#include "sb_ptx.cuh"
+
+namespace sbk {
+namespace tck {
+
+constexpr int kEmodeStep = 0, kEmodeStepTrace = 1, kEmodeEnergy = 2;
+constexpr int kEpiWarps = 8;     // two per TMEM lane quadrant
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kEpiFirstThread = 64;
+constexpr int kTcThreads = 64 + kEpiThreads;  // producer warp, MMA warp, epilogue warps
+constexpr int kBM = 128;         // spins per unit (MMA M, TMEM lanes)
+constexpr int kChunkBytes = 128; // K bytes per stage (one 128-byte swizzle atom row)
+
+struct alignas(64) TcArgs {
+  CUtensorMap tmA[2];      // J operand parts: [Np rows][Kp] K-major
+  CUtensorMap tmB[2][2];   // V operand [buffer][part]: [Rp rows][Kp] K-major
+  float *x, *y;            // [R][xp] state (read at start, written at the end)
+  const float *h;          // [n] or null
+  uint8_t *v[2][2];        // V operand [buffer][part] base pointers (bytes)
+  double *energy;          // trace: [(steps + 1) * R] (step t -> slot t) or energy pass: [R]
+  uint32_t *status;
+  uint32_t *flags;         // [n_rtiles][n_mtiles] published step counters (zeroed before launch)
+  int n, R, xp, Kp, Rp, n_mtiles, n_rtiles, k_chunks;
+  int steps, t0;           // steps to run; schedule offset
+  int buf0;                // V buffer holding V(t0)
+  const float *pumps;      // pumps[t] = a0 - a(t), computed on the host
+  float c0, dt, dta0;
+};
+
+template <int DT>
+struct DtTraits;
+template <>
+struct DtTraits<kTcFp8> {
+  static constexpr int kElem = 1, kParts = 1;
+};
+template <>
+struct DtTraits<kTcBf16> {
+  static constexpr int kElem = 2, kParts = 1;
+};
+template <>
+struct DtTraits<kTcBf16Split> {
+  static constexpr int kElem = 2, kParts = 2;
+};
+
+template <int DT, int VARIANT>
+struct Cfg {
+  static constexpr int kElem = DtTraits<DT>::kElem;
+  static constexpr int kAParts = DtTraits<DT>::kParts;
+  // V = sign(x) needs one part even when J is split; bSB's x is split with J.
+  static constexpr int kBParts = (DT == kTcBf16Split && VARIANT == 1) ? 2 : 1;
+  static constexpr int kKPerMma = 32 / kElem;  // 32 bytes of K per instruction
+  static constexpr int kMmaPerChunk = kChunkBytes / 32;
+};
+
+__host__ __device__ constexpr uint32_t make_idesc(int dt, int m, int n) {
+  // D = F32 (bits 4-5 = 1); A/B format: E4M3 = 0 (kind::f8f6f4) or BF16 = 1 (kind::f16);
+  // both K-major; N >> 3 at bits 17-22; M >> 4 at bits 24-28.
+  return (1u << 4) | ((dt == kTcFp8 ? 0u : 1u) << 7) | ((dt == kTcFp8 ? 0u : 1u) << 10) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : -1.0f; }
+
+__device__ __forceinline__ void sb_update(float f, float hv, float pump, float c0, float dt,
+                                          float dta0, float &x, float &y) {
+  const float fv = __fadd_rn(f, hv);
+  const float g = __fmul_rn(c0, fv);
+  const float force = __fmaf_rn(-pump, x, g);
+  y = __fmaf_rn(dt, force, y);
+  x = __fmaf_rn(dta0, y, x);
+  if (fabsf(x) > 1.0f) {
+    x = copysignf(1.0f, x);
+    y = 0.0f;
+  }
+}
+
+// Write element (r, i) of the next operand.
+template <int DT, int VARIANT>
+__device__ __forceinline__ void store_operand(uint8_t *const (&vb)[2], size_t idx, float x) {
+  if constexpr (DT == kTcFp8) {
+    vb[0][idx] = x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;  // E4M3 +1 / -1
+  } else if constexpr (Cfg<DT, VARIANT>::kBParts == 1) {
+    reinterpret_cast<uint16_t *>(vb[0])[idx] = x > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80;
+  } else {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(x, __bfloat162float(hi)));
+    reinterpret_cast<__nv_bfloat16 *>(vb[0])[idx] = hi;
+    reinterpret_cast<__nv_bfloat16 *>(vb[1])[idx] = lo;
+  }
+}
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Named barrier over the epilogue warps only (the producer and MMA lanes never join it).
+__device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+}
+
+// AND of a predicate over the epilogue warps (a named-barrier reduction), so that they all leave a
+// loop together and never strand one another at a later named barrier.
+__device__ __forceinline__ bool epi_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)(v ? 1 : 0)), "n"(kEpiThreads)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Bounded wait until a unit's published step counter reaches `target`. Polls with relaxed loads
+// (an acquire load per poll would order, and slow, everything else on this SM) and backs off;
+// the acquire fence is taken once the flag is seen.
+__device__ __forceinline__ bool wait_flag(const uint32_t *flag, uint32_t target) {
+  if (ld_relaxed(flag) < target) {
+    const long long t0 = clock64();
+    while (ld_relaxed(flag) < target) {
+      if (clock64() - t0 > ptx::kWaitCycles) return false;
+      __nanosleep(64);
+    }
+  }
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return true;
+}
+
+// One persistent launch runs `steps` SB steps. Unit (mt, rt) = spins [128 mt, 128 mt + 128) x
+// replicas [NR rt, NR rt + NR). Step t's contraction needs V(t) for the unit's replica tile over
+// all K, i.e. the chunks the units (*, rt) of the same replica column wrote at the end of step
+// t - 1: each unit publishes flags[rt][mt] = t after writing its chunk, and the producer waits for
+// flags[rt][chunk's unit] >= t before loading that chunk. Those same flags also order the reuse of
+// the ping-pong operand buffer (a unit overwrites V(t+1)'s buffer only after consuming all of V(t),
+// i.e. after every reader of V(t-1)'s chunk finished its step t-1 contraction).
+template <int DT, int VARIANT, int NR, int STAGES, int EMODE>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_constant__ TcArgs p) {
+  using C = Cfg<DT, VARIANT>;
+  constexpr int kATile = kBM * kChunkBytes;  // bytes per A part per stage
+  constexpr int kBTile = NR * kChunkBytes;   // bytes per B part per stage
+  constexpr int kStage = C::kAParts * kATile + C::kBParts * kBTile;
+  constexpr uint32_t kTx = (uint32_t)kStage;
+  constexpr uint32_t kCols = 4 * NR <= 32 ? 32 : (4 * NR <= 64 ? 64 : (4 * NR <= 128 ? 128 : (4 * NR <= 256 ? 256 : 512)));
+  constexpr uint32_t kIdesc = make_idesc(DT, kBM, NR);
+  constexpr int kHalf = NR / 2;               // columns per epilogue warp
+  static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
+  static_assert(4 * NR <= 512, "two accumulators + x + y must fit TMEM");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float ered[4][NR];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x % p.n_mtiles, rt = blockIdx.x / p.n_mtiles;
+  const int m0 = mt * kBM, r0 = rt * NR;
+  constexpr bool kEOnly = EMODE == kEmodeEnergy;   // one contraction, energies only
+  constexpr bool want_e = EMODE != kEmodeStep;      // per-replica energies of s(t)
+  const int nsteps = kEOnly ? 1 : p.steps;
+  uint32_t *col_flags = p.flags + (size_t)rt * p.n_mtiles;
+  bool ok = true;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full_bar[s], 1);
+      ptx::mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&accf_bar[b], 1);
+      ptx::mbar_init(&acce_bar[b], kEpiWarps);
+    }
+    ptx::fence_mbar_init();
+    for (int a = 0; a < C::kAParts; ++a) ptx::prefetch_tmap(&p.tmA[a]);
+    for (int b = 0; b < C::kBParts; ++b) {
+      ptx::prefetch_tmap(&p.tmB[0][b]);
+      ptx::prefetch_tmap(&p.tmB[1][b]);
+    }
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(&tmem_base_sh, kCols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+  // columns: accumulators [0, NR) and [NR, 2NR), x [2NR, 3NR), y [3NR, 4NR)
+  const uint32_t t_x = tmem + 2 * NR, t_y = tmem + 3 * NR;
+
+  if (warp == 0) {
+    // ---------------- TMA producer (lane 0 issues; the warp polls the column's flags) ----------------
+    uint32_t g = 0;  // chunks issued so far (the MMA lane counts identically)
+    int pre = 0;     // chunks of the coming step whose J part is already in flight
+    for (int ls = 0; ls < nsteps; ++ls) {
+      const int buf = (p.buf0 + ls) & 1;
+      if (ls > 0) {
+        // every unit of this replica column must have published V(ls): poll all flags at once
+        bool fl = ok;
+        for (int u = lane; u < p.n_mtiles && fl; u += 32) fl = wait_flag(col_flags + u, (uint32_t)ls);
+        if (!__all_sync(0xffffffffu, fl)) ok = false;
+        if (!ok) break;
+        ptx::fence_proxy_async_global();
+      }
+      if (lane == 0) {
+        for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          uint8_t *st = smem + s * kStage;
+          const int kx = kc * (kChunkBytes / C::kElem);
+          if (kc >= pre) {
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) { ok = false; break; }
+            ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+            for (int a = 0; a < C::kAParts; ++a)
+              ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+          }
+          for (int b = 0; b < C::kBParts; ++b)
+            ptx::tma_load_2d(st + C::kAParts * kATile + b * kBTile, &p.tmB[buf][b], kx, r0, &full_bar[s]);
+        }
+        // J does not change between steps: start the next step's first J tiles now.
+        pre = 0;
+        if (ok && ls + 1 < nsteps) {
+          const int npre = p.k_chunks < STAGES ? p.k_chunks : STAGES;
+          for (int kc = 0; kc < npre; ++kc) {
+            const uint32_t gg = g + kc;
+            const int s = gg % STAGES;
+            const uint32_t use = gg / STAGES;
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) { ok = false; break; }
+            ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+            for (int a = 0; a < C::kAParts; ++a)
+              ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
+                               &full_bar[s]);
+            ++pre;
+          }
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) break;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      uint32_t g = 0;
+      for (int ls = 0; ls < nsteps && ok; ++ls) {
+        const int ab = ls & 1;
+        const uint32_t t_acc = tmem + ab * NR;
+        if (ls >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((ls >> 1) - 1) & 1)) { ok = false; break; }
+        ptx::tc_fence_after();
+        for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+          ptx::tc_fence_after();
+          const uint32_t sa = ptx::smem_u32(smem + s * kStage);
+          const uint32_t sb = sa + C::kAParts * kATile;
+          int prod = 0;
+#pragma unroll
+          for (int a = 0; a < C::kAParts; ++a) {
+#pragma unroll
+            for (int b = 0; b < C::kBParts; ++b) {
+              if (a + b > 1) continue;  // lo * lo is below the FP32 accumulator's resolution
+#pragma unroll
+              for (int k = 0; k < C::kMmaPerChunk; ++k) {
+                const uint64_t ad = ptx::smem_desc_sw128(sa + a * kATile + k * 32);
+                const uint64_t bd = ptx::smem_desc_sw128(sb + b * kBTile + k * 32);
+                const uint32_t acc = (kc > 0 || prod > 0 || k > 0) ? 1u : 0u;
+                if constexpr (DT == kTcFp8)
+                  ptx::mma_f8(t_acc, ad, bd, kIdesc, acc);
+                else
+                  ptx::mma_f16(t_acc, ad, bd, kIdesc, acc);
+              }
+              ++prod;
+            }
+          }
+          ptx::mma_commit(&empty_bar[s]);
+        }
+        ptx::mma_commit(&accf_bar[ab]);
+      }
+    }
+  } else {
+    // ---------------- epilogue: 8 warps, two per TMEM lane quadrant ----------------
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int c_lo = half * kHalf;
+    const int row = m0 + 32 * q + lane;
+    const uint32_t lane_off = (uint32_t)(32 * q) << 16;
+    const float hv = (p.h && row < p.n) ? p.h[row] : 0.0f;
+    if constexpr (!kEOnly) {
+      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
+        uint32_t vx[16], vy[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          const bool in = row < p.n && r < p.R;
+          vx[j] = __float_as_uint(in ? p.x[(size_t)r * p.xp + row] : 0.0f);
+          vy[j] = __float_as_uint(in ? p.y[(size_t)r * p.xp + row] : 0.0f);
+        }
+        ptx::tmem_st16(t_x + lane_off + c, vx);
+        ptx::tmem_st16(t_y + lane_off + c, vy);
+      }
+      ptx::tmem_st_wait();
+    }
+    for (int ls = 0; ls < nsteps; ++ls) {
+      const int t = p.t0 + ls;
+      const int buf = (p.buf0 + ls) & 1;
+      const int ab = ls & 1;
+      const uint32_t t_acc = tmem + ab * NR;
+      const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1);
+      if (!epi_all(got)) { ok = false; break; }
+      ptx::tc_fence_after();
+      const float pump = kEOnly ? 0.0f : p.pumps[t];
+      uint8_t *const vnext[2] = {p.v[buf ^ 1][0], p.v[buf ^ 1][1]};
+      // TMEM -> registers, software-pipelined: chunk i + 1 is in flight while chunk i is computed
+      constexpr int kChunks = kHalf / 16;
+      uint32_t va[2][16], vx[2][16], vy[2][16];
+      ptx::tmem_ld16(t_acc + lane_off + c_lo, va[0]);
+      if constexpr (!kEOnly) {
+        ptx::tmem_ld16(t_x + lane_off + c_lo, vx[0]);
+        ptx::tmem_ld16(t_y + lane_off + c_lo, vy[0]);
+      }
+      ptx::tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < kChunks; ++i) {
+        const int cur = i & 1;
+        const int c = c_lo + 16 * i;
+        if (i + 1 < kChunks) {
+          ptx::tmem_ld16(t_acc + lane_off + c + 16, va[cur ^ 1]);
+          if constexpr (!kEOnly) {
+            ptx::tmem_ld16(t_x + lane_off + c + 16, vx[cur ^ 1]);
+            ptx::tmem_ld16(t_y + lane_off + c + 16, vy[cur ^ 1]);
+          }
+        }
+        float e2[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          const bool in = row < p.n && r < p.R;
+          const float f = __uint_as_float(va[cur][j]);
+          float x, y;
+          if constexpr (kEOnly) {
+            x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
+            y = 0.0f;
+          } else {
+            x = __uint_as_float(vx[cur][j]);
+            y = __uint_as_float(vy[cur][j]);
+          }
+          // 2 x (energy contribution) of s(t): -s f - 2 h s, an integer for integer J and h
+          if constexpr (want_e) {
+            const float sg = sgnf(x);
+            e2[j] = in ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
+          }
+          if (!kEOnly && in) {
+            sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
+            store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
+          }
+          vx[cur][j] = __float_as_uint(x);
+          vy[cur][j] = __float_as_uint(y);
+        }
+        if constexpr (!kEOnly) {
+          ptx::tmem_st16(t_x + lane_off + c, vx[cur]);
+          ptx::tmem_st16(t_y + lane_off + c, vy[cur]);
+        }
+        if constexpr (want_e) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float v = e2[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) ered[q][c + j] = v;
+          }
+        }
+        ptx::tmem_ld_wait();
+      }
+      if constexpr (!kEOnly) ptx::tmem_st_wait();
+      // the accumulator may be overwritten from here on
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&acce_bar[ab]);
+      // publish this unit's V(t+1) chunk to the replica column
+      epi_sync();
+      if (!kEOnly && threadIdx.x == kEpiFirstThread) {
+        ptx::fence_proxy_async_global();
+        __threadfence();
+        st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
+      }
+      if constexpr (want_e) {
+        for (int c = threadIdx.x - kEpiFirstThread; c < NR; c += kEpiThreads) {
+          const int r = r0 + c;
+          if (r < p.R) {
+            double *slot = kEOnly ? p.energy : p.energy + (size_t)t * p.R;
+            const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
+            atomicAdd(slot + r, 0.5 * sum);
+          }
+        }
+        epi_sync();  // ered is rewritten by the next step
+      }
+    }
+    // write the state back
+    if (!kEOnly && ok) {
+      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
+        uint32_t vx[16], vy[16];
+        ptx::tmem_ld16(t_x + lane_off + c, vx);
+        ptx::tmem_ld16(t_y + lane_off + c, vy);
+        ptx::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          if (row < p.n && r < p.R) {
+            p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
+            p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
+          }
+        }
+      }
+    }
+  }
+  if (!ok) atomicOr(p.status, kErrWaitTimeout);
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, kCols);
+  }
+}
+
+// Pipeline depth: as many stages as fit 200 KB of shared memory (at most 8).
+template <int DT, int VARIANT, int NR>
+constexpr int tc_stages() {
+  constexpr int kStage = Cfg<DT, VARIANT>::kAParts * kBM * kChunkBytes + Cfg<DT, VARIANT>::kBParts * NR * kChunkBytes;
+  return (200 * 1024) / kStage > 8 ? 8 : (200 * 1024) / kStage;
+}
+
+template <int DT, int VARIANT, int NR>
+constexpr size_t tc_smem() {
+  constexpr int kStage = Cfg<DT, VARIANT>::kAParts * kBM * kChunkBytes + Cfg<DT, VARIANT>::kBParts * NR * kChunkBytes;
+  return (size_t)tc_stages<DT, VARIANT, NR>() * kStage + 1024;
+}
+
+// Kernel for one epilogue mode; MODES is the bit set of modes this build instantiates.
+template <int DT, int VARIANT, int NR, int MODES>
+inline bool tc_lookup(int emode, const void **k, size_t *smem) {
+  constexpr int S = tc_stages<DT, VARIANT, NR>();
+  *smem = tc_smem<DT, VARIANT, NR>();
+  *k = nullptr;
+  if constexpr ((MODES & 1) != 0)
+    if (emode == kEmodeStep) *k = reinterpret_cast<const void *>(&tc_sb_kernel<DT, VARIANT, NR, S, kEmodeStep>);
+  if constexpr ((MODES & 2) != 0)
+    if (emode == kEmodeStepTrace) *k = reinterpret_cast<const void *>(&tc_sb_kernel<DT, VARIANT, NR, S, kEmodeStepTrace>);
+  if constexpr ((MODES & 4) != 0)
+    if (emode == kEmodeEnergy) *k = reinterpret_cast<const void *>(&tc_sb_kernel<DT, VARIANT, NR, S, kEmodeEnergy>);
+  return *k != nullptr;
+}
+
+}  // namespace tck
+}  // namespace sbk

@@ -1,0 +1,24 @@
+// Instantiations of the tcgen05 SB kernel for BF16 hi + lo operands (real couplings: dSB, and bSB with x split too).
+#include "sb_tc_kernel.cuh"
+
+namespace sbk {
+
+bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem) {
+  if (variant == 2) {
+    switch (nr) {
+      case 32: return tck::tc_lookup<kTcBf16Split, 2, 32, 3>(emode, k, smem);
+      case 64: return tck::tc_lookup<kTcBf16Split, 2, 64, 3>(emode, k, smem);
+      case 128: return tck::tc_lookup<kTcBf16Split, 2, 128, 3>(emode, k, smem);
+    }
+  }
+  if (variant == 1) {
+    switch (nr) {
+      case 32: return tck::tc_lookup<kTcBf16Split, 1, 32, 1>(emode, k, smem);
+      case 64: return tck::tc_lookup<kTcBf16Split, 1, 64, 1>(emode, k, smem);
+      case 128: return tck::tc_lookup<kTcBf16Split, 1, 128, 1>(emode, k, smem);
+    }
+  }
+  return false;
+}
+
+}  // namespace sbk
