@@ -112,17 +112,19 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-bool encode_2d(CUtensorMap *m, void *base, int elem, uint64_t inner, uint64_t outer, uint32_t box_rows) {
+bool encode_2d(CUtensorMap *m, void *base, int elem, uint64_t inner, uint64_t outer, uint32_t box_rows,
+               bool store_tile = false) {
   auto enc = get_encode();
   if (!enc) return false;
   const cuuint64_t dims[2] = {inner, outer};
   const cuuint64_t strides[1] = {inner * (uint64_t)elem};
-  const cuuint32_t box[2] = {(cuuint32_t)(kChunkBytes / elem), box_rows};
+  // loads: one 128-byte swizzled K chunk; stores: the unit's whole 128-spin row, unswizzled
+  const cuuint32_t box[2] = {(cuuint32_t)(store_tile ? kBM : kChunkBytes / elem), box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(m, elem == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                          base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                         store_tile ? CU_TENSOR_MAP_SWIZZLE_NONE : CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
@@ -247,6 +249,9 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
         return fail("cuTensorMapEncodeTiled(V)", cudaSuccess);
       g.v[b][pp] = e->v[b][pp];
     }
+  for (int b = 0; b < 2; ++b)
+    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, (uint64_t)e->Kp, (uint64_t)e->Rp, (uint32_t)nr, true))
+      return fail("cuTensorMapEncodeTiled(V store)", cudaSuccess);
   g.flags = e->flags;
   g.n = s.n;
   g.R = s.R;
@@ -358,6 +363,9 @@ cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
       !encode_2d(&g.tmB[0][0], e.v[0][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr) ||
       !encode_2d(&g.tmB[1][0], e.v[1][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr))
     return cudaErrorInvalidValue;
+  if (!encode_2d(&g.tmS[0], e.v[0][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr, true) ||
+      !encode_2d(&g.tmS[1], e.v[1][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr, true))
+    return cudaErrorInvalidValue;
   g.v[0][0] = e.v[0][0];
   g.v[1][0] = e.v[1][0];
   g.flags = e.flags;
@@ -369,8 +377,11 @@ cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
   g.n_mtiles = e.n_mtiles;
   g.n_rtiles = e.n_rtiles;
   g.k_chunks = e.Kp / kChunkBytes;
-  cudaError_t ce = cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem);
-  if (ce != cudaSuccess) return ce;
+  cudaError_t ce = cudaSuccess;
+  for (int m = 0; m < 3; ++m)
+    if (e.kernel[m] &&
+        (ce = cudaFuncSetAttribute(e.kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem)) != cudaSuccess)
+      return ce;
   convert_j_kernel<<<grid_1d((size_t)e.Np * e.Kp), 256, 0, st>>>(ext.J, ext.n, ext.jp, e.a[0], nullptr, e.Np, e.Kp,
                                                                  kTcFp8);
   if ((ce = cudaGetLastError()) != cudaSuccess) return ce;

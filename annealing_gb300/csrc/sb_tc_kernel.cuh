@@ -52,6 +52,7 @@ constexpr int kChunkBytes = 128; // K bytes per stage (one 128-byte swizzle atom
 struct alignas(64) TcArgs {
   CUtensorMap tmA[2];      // J operand parts: [Np rows][Kp] K-major
   CUtensorMap tmB[2][2];   // V operand [buffer][part]: [Rp rows][Kp] K-major
+  CUtensorMap tmS[2];      // V operand [buffer], part 0, unswizzled 128-spin x NR boxes (TMA store)
   float *x, *y;            // [R][xp] state (read at start, written at the end)
   const float *h;          // [n] or null
   uint8_t *v[2][2];        // V operand [buffer][part] base pointers (bytes)
@@ -187,6 +188,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   constexpr int kATile = kBM * kChunkBytes;  // bytes per A part per stage
   constexpr int kBTile = NR * kChunkBytes;   // bytes per B part per stage
   constexpr int kStage = C::kAParts * kATile + C::kBParts * kBTile;
+  // Single-part operands (FP8 / BF16 signs) leave the epilogue through a shared-memory tile and one
+  // TMA store per unit per step; split operands are stored element by element.
+  constexpr bool kStageV = C::kBParts == 1;
+  constexpr int kVRow = kBM * C::kElem;      // bytes of one replica row of the unit's V tile
   constexpr uint32_t kTx = (uint32_t)kStage;
   constexpr uint32_t kCols = 4 * NR <= 32 ? 32 : (4 * NR <= 64 ? 64 : (4 * NR <= 128 ? 128 : (4 * NR <= 256 ? 256 : 512)));
   constexpr uint32_t kIdesc = make_idesc(DT, kBM, NR);
@@ -238,52 +243,65 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
 
   if (warp == 0) {
     // ---------------- TMA producer (lane 0 issues; the warp polls the column's flags) ----------------
+    // Every lane runs the same loop and meets the others only at warp-collective points, so a
+    // lane that gives up on a wait never strands the rest.
     uint32_t g = 0;  // chunks issued so far (the MMA lane counts identically)
     int pre = 0;     // chunks of the coming step whose J part is already in flight
-    for (int ls = 0; ls < nsteps; ++ls) {
+    for (int ls = 0; ls < nsteps && ok; ++ls) {
       const int buf = (p.buf0 + ls) & 1;
-      if (ls > 0) {
-        // every unit of this replica column must have published V(ls): poll all flags at once
-        bool fl = ok;
-        for (int u = lane; u < p.n_mtiles && fl; u += 32) fl = wait_flag(col_flags + u, (uint32_t)ls);
-        if (!__all_sync(0xffffffffu, fl)) ok = false;
-        if (!ok) break;
-        ptx::fence_proxy_async_global();
-      }
-      if (lane == 0) {
-        for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+      int ready = ls == 0 ? p.n_mtiles : 0;  // units of this column known to have published V(ls)
+      for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++g) {
+        const int kx = kc * (kChunkBytes / C::kElem);
+        if (kx / kBM >= ready) {
+          // poll the next 32 units of the column at once (one L2 round trip for all of them)
+          const int u = ready + lane;
+          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls) : true;
+          if (!__all_sync(0xffffffffu, fl)) ok = false;
+          ready = ready + 32 < p.n_mtiles ? ready + 32 : p.n_mtiles;
+          ptx::fence_proxy_async_global();
+        }
+        if (lane == 0 && ok) {
           const int s = g % STAGES;
           const uint32_t use = g / STAGES;
           uint8_t *st = smem + s * kStage;
-          const int kx = kc * (kChunkBytes / C::kElem);
+          bool issue = true;
           if (kc >= pre) {
-            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) { ok = false; break; }
-            ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
-            for (int a = 0; a < C::kAParts; ++a)
-              ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+              ok = false;
+              issue = false;
+            } else {
+              ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+              for (int a = 0; a < C::kAParts; ++a)
+                ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+            }
           }
-          for (int b = 0; b < C::kBParts; ++b)
-            ptx::tma_load_2d(st + C::kAParts * kATile + b * kBTile, &p.tmB[buf][b], kx, r0, &full_bar[s]);
+          if (issue)
+            for (int b = 0; b < C::kBParts; ++b)
+              ptx::tma_load_2d(st + C::kAParts * kATile + b * kBTile, &p.tmB[buf][b], kx, r0, &full_bar[s]);
         }
-        // J does not change between steps: start the next step's first J tiles now.
-        pre = 0;
-        if (ok && ls + 1 < nsteps) {
-          const int npre = p.k_chunks < STAGES ? p.k_chunks : STAGES;
-          for (int kc = 0; kc < npre; ++kc) {
-            const uint32_t gg = g + kc;
-            const int s = gg % STAGES;
-            const uint32_t use = gg / STAGES;
-            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) { ok = false; break; }
-            ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
-            for (int a = 0; a < C::kAParts; ++a)
-              ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
-                               &full_bar[s]);
-            ++pre;
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      }
+      // J does not change between steps: start the next step's first J tiles now.
+      pre = 0;
+      if (lane == 0 && ok && ls + 1 < nsteps) {
+        const int npre = p.k_chunks < STAGES ? p.k_chunks : STAGES;
+        for (int kc = 0; kc < npre; ++kc) {
+          const uint32_t gg = g + kc;
+          const int s = gg % STAGES;
+          const uint32_t use = gg / STAGES;
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            ok = false;
+            break;
           }
+          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+          for (int a = 0; a < C::kAParts; ++a)
+            ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
+                             &full_bar[s]);
+          ++pre;
         }
       }
+      pre = __shfl_sync(0xffffffffu, pre, 0);
       ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-      if (!ok) break;
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -358,39 +376,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       ptx::tc_fence_after();
       const float pump = kEOnly ? 0.0f : p.pumps[t];
       uint8_t *const vnext[2] = {p.v[buf ^ 1][0], p.v[buf ^ 1][1]};
-      // TMEM -> registers, software-pipelined: chunk i + 1 is in flight while chunk i is computed
+      uint8_t *const vtile = smem + STAGES * kStage;  // [NR][kVRow] staging tile
       constexpr int kChunks = kHalf / 16;
-      uint32_t va[2][16], vx[2][16], vy[2][16];
-      ptx::tmem_ld16(t_acc + lane_off + c_lo, va[0]);
-      if constexpr (!kEOnly) {
-        ptx::tmem_ld16(t_x + lane_off + c_lo, vx[0]);
-        ptx::tmem_ld16(t_y + lane_off + c_lo, vy[0]);
-      }
-      ptx::tmem_ld_wait();
-#pragma unroll
+#pragma unroll 1
       for (int i = 0; i < kChunks; ++i) {
-        const int cur = i & 1;
         const int c = c_lo + 16 * i;
-        if (i + 1 < kChunks) {
-          ptx::tmem_ld16(t_acc + lane_off + c + 16, va[cur ^ 1]);
-          if constexpr (!kEOnly) {
-            ptx::tmem_ld16(t_x + lane_off + c + 16, vx[cur ^ 1]);
-            ptx::tmem_ld16(t_y + lane_off + c + 16, vy[cur ^ 1]);
-          }
+        uint32_t va[16], vx[16], vy[16];
+        ptx::tmem_ld16(t_acc + lane_off + c, va);
+        if constexpr (!kEOnly) {
+          ptx::tmem_ld16(t_x + lane_off + c, vx);
+          ptx::tmem_ld16(t_y + lane_off + c, vy);
         }
+        ptx::tmem_ld_wait();
         float e2[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int r = r0 + c + j;
           const bool in = row < p.n && r < p.R;
-          const float f = __uint_as_float(va[cur][j]);
+          const float f = __uint_as_float(va[j]);
           float x, y;
           if constexpr (kEOnly) {
             x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
             y = 0.0f;
           } else {
-            x = __uint_as_float(vx[cur][j]);
-            y = __uint_as_float(vy[cur][j]);
+            x = __uint_as_float(vx[j]);
+            y = __uint_as_float(vy[j]);
           }
           // 2 x (energy contribution) of s(t): -s f - 2 h s, an integer for integer J and h
           if constexpr (want_e) {
@@ -399,14 +409,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           }
           if (!kEOnly && in) {
             sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
-            store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
+            if constexpr (!kStageV) store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
           }
-          vx[cur][j] = __float_as_uint(x);
-          vy[cur][j] = __float_as_uint(y);
+          if constexpr (kStageV && !kEOnly) {
+            // every element of the tile is written (zero outside the problem) so the padding stays 0
+            uint8_t *dst = vtile + (c + j) * kVRow + (row - m0) * C::kElem;
+            if constexpr (DT == kTcFp8)
+              *dst = in ? (x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8) : (uint8_t)0;
+            else
+              *reinterpret_cast<uint16_t *>(dst) = in ? (x > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80) : (uint16_t)0;
+          }
+          vx[j] = __float_as_uint(x);
+          vy[j] = __float_as_uint(y);
         }
         if constexpr (!kEOnly) {
-          ptx::tmem_st16(t_x + lane_off + c, vx[cur]);
-          ptx::tmem_st16(t_y + lane_off + c, vy[cur]);
+          ptx::tmem_st16(t_x + lane_off + c, vx);
+          ptx::tmem_st16(t_y + lane_off + c, vy);
         }
         if constexpr (want_e) {
 #pragma unroll
@@ -417,7 +435,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             if (lane == 0) ered[q][c + j] = v;
           }
         }
-        ptx::tmem_ld_wait();
       }
       if constexpr (!kEOnly) ptx::tmem_st_wait();
       // the accumulator may be overwritten from here on
@@ -425,8 +442,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(&acce_bar[ab]);
       // publish this unit's V(t+1) chunk to the replica column
+      if constexpr (kStageV && !kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> TMA store
       epi_sync();
       if (!kEOnly && threadIdx.x == kEpiFirstThread) {
+        if constexpr (kStageV) {
+          ptx::tma_store_2d(&p.tmS[buf ^ 1], vtile, m0, r0);
+          ptx::bulk_commit();
+          ptx::bulk_wait_all();  // the tile is in global memory (and may be rewritten next step)
+        }
         ptx::fence_proxy_async_global();
         __threadfence();
         st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
@@ -472,15 +495,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
 
 // Pipeline depth: as many stages as fit 200 KB of shared memory (at most 8).
 template <int DT, int VARIANT, int NR>
+constexpr int tc_vtile_bytes() {
+  return Cfg<DT, VARIANT>::kBParts == 1 ? NR * kBM * Cfg<DT, VARIANT>::kElem : 0;
+}
+
+template <int DT, int VARIANT, int NR>
 constexpr int tc_stages() {
   constexpr int kStage = Cfg<DT, VARIANT>::kAParts * kBM * kChunkBytes + Cfg<DT, VARIANT>::kBParts * NR * kChunkBytes;
-  return (200 * 1024) / kStage > 8 ? 8 : (200 * 1024) / kStage;
+  constexpr int kBudget = 216 * 1024 - tc_vtile_bytes<DT, VARIANT, NR>();
+  return kBudget / kStage > 8 ? 8 : kBudget / kStage;
 }
 
 template <int DT, int VARIANT, int NR>
 constexpr size_t tc_smem() {
   constexpr int kStage = Cfg<DT, VARIANT>::kAParts * kBM * kChunkBytes + Cfg<DT, VARIANT>::kBParts * NR * kChunkBytes;
-  return (size_t)tc_stages<DT, VARIANT, NR>() * kStage + 1024;
+  return (size_t)tc_stages<DT, VARIANT, NR>() * kStage + tc_vtile_bytes<DT, VARIANT, NR>() + 1024;
 }
 
 // Kernel for one epilogue mode; MODES is the bit set of modes this build instantiates.
