@@ -4,9 +4,9 @@ The solver is the C ABI in include/sb.h, implemented by annealing_gb300/libsbsol
 kernels for sm_103a + C++ host code). This package holds the ctypes binding (sb.py), the in-tree
 build (_build.py) and the synthetic instance generators (instances.py).
 """
-from .sb import (ASB, BSB, DSB, FIELD_AUTO, FIELD_FP32, FIELD_TC, INIT_REFERENCE, INIT_UNIFORM,
+from .sb import (ASB, BSB, DSB, Batch, FIELD_AUTO, FIELD_FP32, FIELD_TC, INIT_REFERENCE, INIT_UNIFORM,
                  Context, Params, Plan, Problem, Result, SBError, lib, pump)
 
-__all__ = ["ASB", "BSB", "DSB", "FIELD_AUTO", "FIELD_FP32", "FIELD_TC", "INIT_REFERENCE",
+__all__ = ["ASB", "BSB", "DSB", "Batch", "FIELD_AUTO", "FIELD_FP32", "FIELD_TC", "INIT_REFERENCE",
            "INIT_UNIFORM", "Context", "Params", "Plan", "Problem", "Result", "SBError", "lib",
            "pump"]

@@ -18,6 +18,7 @@
 #include "sb.h"
 #include "sb_host.h"
 #include "sb_internal.h"
+#include "sb_ctx.h"
 #include "sb_serve.h"
 
 namespace {
@@ -26,18 +27,6 @@ thread_local std::string g_thread_error;
 
 void sbh::set_thread_error(const std::string &e) { g_thread_error = e; }
 const char *sbh::thread_error() { return g_thread_error.c_str(); }
-
-struct sb_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  std::mutex mu;
-  std::string last_error;
-  int64_t hbm_budget = 0;
-  int max_inflight = 64;
-  sb_plan *cached = nullptr;  // most recent sb_solve plan, reused when the shape matches
-  sbs::Server *server = nullptr;
-};
 
 struct PlanKey {
   int n, R, steps, variant, mode, dtype, init, trace, trace_all, has_h;

@@ -1,0 +1,440 @@
+// Host side of the grouped tensor-core path: many dSB instances of uneven size advanced together.
+// Used by sb_batch_* (a fixed batch, all instances run the same number of steps) and by the
+// serving loop (instances admitted and retired while others run).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sb_grouped.cuh"
+#include "sb_grouped.h"
+#include "sb_host.h"
+
+namespace sbk {
+namespace {
+using namespace tck;
+
+__global__ void g_convert_kernel(const float *J, int n, uint8_t *a, int Np, int Kp) {
+  const size_t total = (size_t)Np * Kp;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = k / Kp, j = k % Kp;
+    const float v = (i < (size_t)n && j < (size_t)n) ? J[i * n + j] : 0.0f;
+    a[k] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+  }
+}
+
+__global__ void g_signs_kernel(const float *x, int n, int R, int xp, uint8_t *v, int Kp) {
+  const size_t total = (size_t)n * R;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / n, i = k % n;
+    v[r * Kp + i] = x[r * xp + i] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+  }
+}
+
+int grid1(size_t total) {
+  size_t g = (total + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+bool encode_fp8(CUtensorMap *m, void *base, uint64_t inner, uint64_t outer, uint32_t rows) {
+  auto enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {inner, outer};
+  const cuuint64_t strides[1] = {inner};
+  const cuuint32_t box[2] = {(cuuint32_t)kChunkBytes, rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NR, int EMODE>
+const void *gk() {
+  return reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), EMODE>);
+}
+
+bool grouped_kernel_for(int nr, int emode, const void **k, size_t *smem) {
+  switch (nr) {
+    case 32: *k = emode == kEmodeEnergy ? gk<32, kEmodeEnergy>() : gk<32, kEmodeStep>(); *smem = grouped_smem<32>(); return true;
+    case 64: *k = emode == kEmodeEnergy ? gk<64, kEmodeEnergy>() : gk<64, kEmodeStep>(); *smem = grouped_smem<64>(); return true;
+    case 128: *k = emode == kEmodeEnergy ? gk<128, kEmodeEnergy>() : gk<128, kEmodeStep>(); *smem = grouped_smem<128>(); return true;
+  }
+  return false;
+}
+
+int device_sms() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+
+bool grouped_supports(const sb_problem *p, const sb_params *prm) {
+  return prm->variant == SB_DSB && p->integer_valued && p->max_abs_j <= 16 && p->n <= 65536 &&
+         prm->replicas <= 4096 && (int64_t)p->n * 16 < (1 << 24);
+}
+
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr) {
+  const int64_t Np = (n + 127) / 128 * 128, Kp = Np, Rp = (R + nr - 1) / nr * nr, xp = (n + 3) / 4 * 4;
+  return Np * Kp + 2 * Rp * Kp + 2 * (int64_t)R * xp * 4 + (int64_t)n * 4 + (int64_t)R * 8 + (int64_t)steps * 4 + 4096;
+}
+
+Grouped::~Grouped() { clear(); }
+
+void Grouped::clear() {
+  for (auto &g : insts) free_instance(g);
+  insts.clear();
+  cudaFree(d_insts);
+  cudaFree(d_items);
+  cudaFree(d_status);
+  cudaFree(d_stage);
+  if (graph) cudaGraphExecDestroy(graph);
+  d_insts = nullptr;
+  d_items = nullptr;
+  d_status = nullptr;
+  d_stage = nullptr;
+  graph = nullptr;
+  stage_bytes = 0;
+  cap_insts = cap_items = 0;
+}
+
+void Grouped::free_instance(GHost &g) {
+  cudaFree(g.a);
+  cudaFree(g.v[0]);
+  cudaFree(g.v[1]);
+  cudaFree(g.x);
+  cudaFree(g.y);
+  cudaFree(g.h);
+  cudaFree(g.energy);
+  cudaFree(g.pumps);
+  g.a = g.v[0] = g.v[1] = nullptr;
+  g.x = g.y = g.h = g.pumps = nullptr;
+  g.energy = nullptr;
+}
+
+sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err) {
+  GHost g;
+  g.tag = tag;
+  g.prob = p;
+  g.n = p->n;
+  g.R = prm->replicas;
+  g.steps = prm->steps;
+  g.t0 = t0;
+  g.Np = (g.n + 127) / 128 * 128;
+  g.Kp = g.Np;
+  g.Rp = (g.R + nr - 1) / nr * nr;
+  g.xp = (g.n + 3) / 4 * 4;
+  g.c0 = prm->c0 > 0.0f ? prm->c0 : sb_default_c0(p);
+  g.dt = prm->dt;
+  g.dta0 = prm->dt * prm->a0;
+  cudaError_t e;
+  auto fail = [&](const char *what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    free_instance(g);
+    return e == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
+  };
+  const size_t xs = (size_t)g.R * g.xp * sizeof(float), vb = (size_t)g.Rp * g.Kp;
+  if ((e = cudaMalloc(&g.a, (size_t)g.Np * g.Kp)) != cudaSuccess) return fail("cudaMalloc(J operand)");
+  if ((e = cudaMalloc(&g.v[0], vb)) != cudaSuccess) return fail("cudaMalloc(V)");
+  if ((e = cudaMalloc(&g.v[1], vb)) != cudaSuccess) return fail("cudaMalloc(V)");
+  if ((e = cudaMalloc(&g.x, xs)) != cudaSuccess) return fail("cudaMalloc(x)");
+  if ((e = cudaMalloc(&g.y, xs)) != cudaSuccess) return fail("cudaMalloc(y)");
+  if ((e = cudaMalloc(&g.energy, (size_t)g.R * sizeof(double))) != cudaSuccess) return fail("cudaMalloc(energy)");
+  if ((e = cudaMalloc(&g.pumps, (size_t)(g.steps > 0 ? g.steps : 1) * sizeof(float))) != cudaSuccess)
+    return fail("cudaMalloc(pumps)");
+  if (p->h) {
+    if ((e = cudaMalloc(&g.h, (size_t)g.n * sizeof(float))) != cudaSuccess) return fail("cudaMalloc(h)");
+    if ((e = cudaMemcpyAsync(g.h, p->h, (size_t)g.n * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return fail("upload h");
+  }
+  // couplings: FP32 through a staging buffer, converted to FP8 on the device
+  const size_t jb = (size_t)g.n * g.n * sizeof(float);
+  if (jb > stage_bytes) {
+    cudaFree(d_stage);
+    d_stage = nullptr;
+    stage_bytes = 0;
+    if ((e = cudaMalloc(&d_stage, jb)) != cudaSuccess) return fail("cudaMalloc(staging)");
+    stage_bytes = jb;
+  }
+  if ((e = cudaMemcpyAsync(d_stage, p->J, jb, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
+  g_convert_kernel<<<grid1((size_t)g.Np * g.Kp), 256, 0, st>>>(d_stage, g.n, g.a, g.Np, g.Kp);
+  std::vector<float> pumps((size_t)(g.steps > 0 ? g.steps : 1), 0.0f);
+  for (int t = 0; t < g.steps; ++t) pumps[t] = sb_pump(prm->a0, t, g.steps);
+  if ((e = cudaMemcpyAsync(g.pumps, pumps.data(), pumps.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
+      cudaSuccess)
+    return fail("upload pumps");
+  // the staging buffer and the pump vector are reused / freed: finish the copies now
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("synchronize");
+  if ((e = cudaMemsetAsync(g.v[0], 0, vb, st)) != cudaSuccess) return fail("memset");
+  if ((e = cudaMemsetAsync(g.v[1], 0, vb, st)) != cudaSuccess) return fail("memset");
+  if ((e = cudaMemsetAsync(g.x, 0, xs, st)) != cudaSuccess) return fail("memset");
+  if ((e = cudaMemsetAsync(g.y, 0, xs, st)) != cudaSuccess) return fail("memset");
+  if (!encode_fp8(&g.desc.tmA, g.a, (uint64_t)g.Kp, (uint64_t)g.Np, kBM) ||
+      !encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr) ||
+      !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr)) {
+    e = cudaErrorInvalidValue;
+    return fail("cuTensorMapEncodeTiled");
+  }
+  g.desc.v[0] = g.v[0];
+  g.desc.v[1] = g.v[1];
+  g.desc.x = g.x;
+  g.desc.y = g.y;
+  g.desc.h = g.h;
+  g.desc.energy = g.energy;
+  g.desc.pumps = g.pumps;
+  g.desc.n = g.n;
+  g.desc.Kp = g.Kp;
+  g.desc.R = g.R;
+  g.desc.Rp = g.Rp;
+  g.desc.xp = g.xp;
+  g.desc.t0 = t0;
+  g.desc.c0 = g.c0;
+  g.desc.dt = g.dt;
+  g.desc.dta0 = g.dta0;
+  g.seed = seed;
+  insts.push_back(g);
+  dirty = true;
+  return init_state(insts.back(), seed, err);
+}
+
+sb_status Grouped::init_state(GHost &g, uint64_t seed, std::string &err) {
+  cudaError_t e = launch_init_uniform(g.x, g.y, g.n, g.R, g.xp, seed, st);
+  if (e == cudaSuccess) {
+    g_signs_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.Kp);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    err = std::string("initial state: ") + cudaGetErrorString(e);
+    return SB_ERR_CUDA;
+  }
+  // step t of the instance reads buffer t & 1 (t = tick - t0), so V(0) goes to buffer 0
+  return SB_OK;
+}
+
+sb_status Grouped::retile(int new_nr, std::string &err) {
+  if (new_nr == nr) return SB_OK;
+  nr = new_nr;
+  for (auto &g : insts) {
+    cudaFree(g.v[0]);
+    cudaFree(g.v[1]);
+    g.v[0] = g.v[1] = nullptr;
+    g.Rp = (g.R + nr - 1) / nr * nr;
+    const size_t vb = (size_t)g.Rp * g.Kp;
+    cudaError_t e;
+    if ((e = cudaMalloc(&g.v[0], vb)) != cudaSuccess || (e = cudaMalloc(&g.v[1], vb)) != cudaSuccess) {
+      err = "cudaMalloc(V)";
+      return SB_ERR_OOM;
+    }
+    cudaMemsetAsync(g.v[0], 0, vb, st);
+    cudaMemsetAsync(g.v[1], 0, vb, st);
+    if (!encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr) ||
+        !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr)) {
+      err = "cuTensorMapEncodeTiled";
+      return SB_ERR_CUDA;
+    }
+    g.desc.v[0] = g.v[0];
+    g.desc.v[1] = g.v[1];
+    g.desc.Rp = g.Rp;
+  }
+  dirty = true;
+  return SB_OK;
+}
+
+void Grouped::remove(int idx) {
+  free_instance(insts[idx]);
+  insts.erase(insts.begin() + idx);
+  dirty = true;
+}
+
+sb_status Grouped::sync_tables(std::string &err) {
+  if (!dirty) return SB_OK;
+  cudaError_t e;
+  if ((int)insts.size() > cap_insts) {
+    cudaFree(d_insts);
+    cap_insts = std::max<int>((int)insts.size(), 2 * cap_insts);
+    if ((e = cudaMalloc(&d_insts, (size_t)cap_insts * sizeof(GInst))) != cudaSuccess) {
+      cap_insts = 0;
+      err = "cudaMalloc(instance table)";
+      return SB_ERR_OOM;
+    }
+  }
+  std::vector<GInst> descs(insts.size());
+  std::vector<GItem> items;
+  for (size_t i = 0; i < insts.size(); ++i) {
+    descs[i] = insts[i].desc;
+    const GHost &g = insts[i];
+    for (int m0 = 0; m0 < g.Np; m0 += kBM)
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{(int)i, m0, r0, g.Kp / kChunkBytes});
+  }
+  if (order == 0) {
+    // longest first, dealt round-robin to the persistent CTAs
+    std::stable_sort(items.begin(), items.end(), [](const GItem &a, const GItem &b) { return a.kchunks > b.kchunks; });
+  }
+  if ((int)items.size() > cap_items) {
+    cudaFree(d_items);
+    cap_items = std::max<int>((int)items.size(), 2 * cap_items);
+    if ((e = cudaMalloc(&d_items, (size_t)cap_items * sizeof(GItem))) != cudaSuccess) {
+      cap_items = 0;
+      err = "cudaMalloc(item table)";
+      return SB_ERR_OOM;
+    }
+  }
+  n_items = (int)items.size();
+  if (!d_status) {
+    if ((e = cudaMalloc(&d_status, sizeof(uint32_t))) != cudaSuccess) return SB_ERR_OOM;
+    cudaMemsetAsync(d_status, 0, sizeof(uint32_t), st);
+  }
+  if (!descs.empty() &&
+      (e = cudaMemcpyAsync(d_insts, descs.data(), descs.size() * sizeof(GInst), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+    err = "upload instance table";
+    return SB_ERR_CUDA;
+  }
+  if (!items.empty() &&
+      (e = cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(GItem), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+    err = "upload item table";
+    return SB_ERR_CUDA;
+  }
+  // the host vectors go out of scope: make the copies complete first
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    err = std::string("synchronize: ") + cudaGetErrorString(e);
+    return SB_ERR_CUDA;
+  }
+  if (graph) {
+    cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
+  dirty = false;
+  return SB_OK;
+}
+
+cudaError_t Grouped::launch(int tick, int emode) {
+  const void *k = nullptr;
+  size_t smem = 0;
+  if (!grouped_kernel_for(nr, emode, &k, &smem)) return cudaErrorInvalidValue;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    static std::map<const void *, bool> done;
+    if (!done[k]) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      done[k] = true;
+    }
+  }
+  if (n_items == 0) return cudaSuccess;
+  const int grid = std::min(n_items, device_sms());
+  const GInst *pi = d_insts;
+  const GItem *pit = d_items;
+  int ni = n_items;
+  uint32_t *ps = d_status;
+  void *args[] = {(void *)&pi, (void *)&pit, (void *)&ni, (void *)&tick, (void *)&ps};
+  ++launches;
+  return cudaLaunchKernel(k, dim3(grid), dim3(kTcThreads), args, smem, st);
+}
+
+cudaError_t Grouped::run_steps(int tick0, int count, bool use_graph) {
+  if (count <= 0) return cudaSuccess;
+  if (!use_graph) {
+    for (int s = 0; s < count; ++s) {
+      cudaError_t e = launch(tick0 + s, kEmodeStep);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  if (!graph || graph_tick0 != tick0 || graph_count != count) {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    // kernel attributes are set before the capture starts
+    const void *k = nullptr;
+    size_t smem = 0;
+    grouped_kernel_for(nr, kEmodeStep, &k, &smem);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const int64_t l0 = launches;
+    for (int s = 0; s < count && e == cudaSuccess; ++s) e = launch(tick0 + s, kEmodeStep);
+    cudaError_t e2 = cudaStreamEndCapture(st, &gr);
+    launches = l0;
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (gr) cudaGraphDestroy(gr);
+      return e != cudaSuccess ? e : e2;
+    }
+    e = cudaGraphInstantiate(&graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {
+      graph = nullptr;
+      return e;
+    }
+    graph_tick0 = tick0;
+    graph_count = count;
+  }
+  launches += count;
+  return cudaGraphLaunch(graph, st);
+}
+
+cudaError_t Grouped::energy_pass(int tick) {
+  for (auto &g : insts) {
+    cudaError_t e = cudaMemsetAsync(g.energy, 0, (size_t)g.R * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+  }
+  return launch(tick, kEmodeEnergy);
+}
+
+// ---- autotuning: replica tile and item order, timed on the batch itself ----
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<int, int>> g_tune_cache;
+}  // namespace
+
+std::string Grouped::tune_key() const {
+  int64_t chunks = 0;
+  int rmax = 0;
+  for (const auto &g : insts) {
+    chunks += (int64_t)(g.Np / kBM) * (g.Kp / kChunkBytes);
+    rmax = std::max(rmax, g.R);
+  }
+  // bucket by total work (log2) and replica count
+  int b = 0;
+  while ((int64_t(1) << b) < chunks) ++b;
+  return std::to_string(rmax) + ":" + std::to_string(b) + ":" + std::to_string(insts.size() > 64 ? 2 : insts.size() > 8 ? 1 : 0);
+}
+
+std::vector<std::pair<int, int>> Grouped::candidates(int R) {
+  std::vector<std::pair<int, int>> c;
+  std::vector<int> nrs;
+  if (R <= 32) nrs = {32};
+  else if (R <= 64) nrs = {64, 32};
+  else nrs = {128, 64};
+  for (int v : nrs)
+    for (int o : {0, 1}) c.push_back({v, o});
+  return c;
+}
+
+}  // namespace sbk

@@ -1,0 +1,222 @@
+// Grouped tcgen05 SB step over many instances of uneven size (dSB, FP8 E4M3 operands).
+//
+// The batched workloads of the benchmark spec (hundreds of instances with N from 64 to 16384, each
+// with its own replicas, and the serving stream) do not fit the one-unit-per-SM residency of
+// the single-instance kernel (sb_tc_kernel.cuh): their state is far larger than TMEM. Here one
+// launch advances every instance by one SB step:
+//   * work item = (instance, 128-spin tile, NR-replica tile); the CTAs of a persistent grid (one
+//     per SM) walk a cost-sorted item list round-robin;
+//   * warp 0 (lane 0) streams each item's J tile and V tile with 2-D TMA through the shared-memory
+//     ring, using the instance's tensor maps, which live in device memory next to its descriptor;
+//   * warp 1 (lane 0) issues tcgen05.mma (kind::f8f6f4) into one of two TMEM accumulators, so the
+//     epilogue of item k overlaps the contraction of item k + 1;
+//   * 8 epilogue warps read the accumulator, load x and y from global memory (coalesced), apply
+//     the dSB update in the oracle's operation order, store x and y and the next operand.
+// The kernel boundary orders the steps; the step loop is captured in a CUDA graph. Each instance
+// carries its own schedule (pump table) and its own step counter offset, so instances admitted at
+// different times advance side by side (continuous batching). Every wait is bounded.
+#pragma once
+#include "sb_grouped.h"
+#include "sb_tc_kernel.cuh"
+
+namespace sbk {
+
+namespace tck {
+
+template <int NR, int STAGES, int EMODE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    grouped_kernel(const GInst *__restrict__ insts, const GItem *__restrict__ items, int n_items, int tick,
+                   uint32_t *status) {
+  using C = Cfg<kTcFp8, 2>;
+  constexpr int kATile = kBM * kChunkBytes;
+  constexpr int kBTile = NR * kChunkBytes;
+  constexpr int kStage = kATile + kBTile;
+  constexpr uint32_t kTx = (uint32_t)kStage;
+  constexpr uint32_t kCols = 2 * NR <= 32 ? 32 : (2 * NR <= 64 ? 64 : (2 * NR <= 128 ? 128 : 256));
+  constexpr uint32_t kIdesc = make_idesc(kTcFp8, kBM, NR);
+  constexpr int kHalf = NR / 2;
+  constexpr bool kEOnly = EMODE == kEmodeEnergy;
+  static_assert(NR == 32 || NR == 64 || NR == 128, "replica tile");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float ered[4][NR];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  bool ok = true;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full_bar[s], 1);
+      ptx::mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&accf_bar[b], 1);
+      ptx::mbar_init(&acce_bar[b], kEpiWarps);
+    }
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(&tmem_base_sh, kCols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer ----------------
+      uint32_t g = 0;
+      for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        const GItem w = items[it];
+        const GInst *in = insts + w.inst;
+        const int buf = (tick - in->t0) & 1;
+        for (int kc = 0; kc < w.kchunks; ++kc, ++g) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          uint8_t *st = smem + s * kStage;
+          ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
+          ptx::tma_load_2d(st, &in->tmA, kc * kChunkBytes, w.m0, &full_bar[s]);
+          ptx::tma_load_2d(st + kATile, &in->tmB[buf], kc * kChunkBytes, w.r0, &full_bar[s]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      uint32_t g = 0;
+      int li = 0;
+      for (int it = blockIdx.x; it < n_items && ok; it += gridDim.x, ++li) {
+        const int kchunks = items[it].kchunks;
+        const int ab = li & 1;
+        const uint32_t t_acc = tmem + ab * NR;
+        if (li >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((li >> 1) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        for (int kc = 0; kc < kchunks; ++kc, ++g) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (!ptx::mbar_wait(&full_bar[s], use & 1)) {
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t sa = ptx::smem_u32(smem + s * kStage);
+#pragma unroll
+          for (int k = 0; k < C::kMmaPerChunk; ++k)
+            ptx::mma_f8(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sa + kATile + k * 32), kIdesc,
+                        (kc > 0 || k > 0) ? 1u : 0u);
+          ptx::mma_commit(&empty_bar[s]);
+        }
+        ptx::mma_commit(&accf_bar[ab]);
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int c_lo = half * kHalf;
+    const uint32_t lane_off = (uint32_t)(32 * q) << 16;
+    int li = 0;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++li) {
+      const GItem w = items[it];
+      const GInst *in = insts + w.inst;
+      const int ab = li & 1;
+      const uint32_t t_acc = tmem + ab * NR;
+      const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(li >> 1) & 1);
+      if (!epi_all(got)) {
+        ok = false;
+        break;
+      }
+      ptx::tc_fence_after();
+      const int t = tick - in->t0;
+      const int n = in->n, R = in->R, xp = in->xp, Kp = in->Kp;
+      const int row = w.m0 + 32 * q + lane;
+      const float hv = (in->h && row < n) ? in->h[row] : 0.0f;
+      const float pump = kEOnly ? 0.0f : in->pumps[t];
+      const float c0 = in->c0, dt = in->dt, dta0 = in->dta0;
+      float *xs = in->x, *ys = in->y;
+      uint8_t *vn = in->v[(t + 1) & 1];
+#pragma unroll 1
+      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
+        uint32_t va[16];
+        ptx::tmem_ld16(t_acc + lane_off + c, va);
+        ptx::tmem_ld_wait();
+        float e2[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = w.r0 + c + j;
+          const bool ins = row < n && r < R;
+          const float f = __uint_as_float(va[j]);
+          const size_t k = (size_t)r * xp + row;
+          float x = ins ? xs[k] : 0.0f;
+          if constexpr (kEOnly) {
+            const float sg = sgnf(x);
+            e2[j] = ins ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
+          } else {
+            if (ins) {
+              float y = ys[k];
+              sb_update(f, hv, pump, c0, dt, dta0, x, y);
+              xs[k] = x;
+              ys[k] = y;
+              vn[(size_t)r * Kp + row] = x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+            }
+          }
+        }
+        if constexpr (kEOnly) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float v = e2[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) ered[q][c + j] = v;
+          }
+        }
+      }
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&acce_bar[ab]);
+      if constexpr (kEOnly) {
+        epi_sync();
+        for (int c = threadIdx.x - kEpiFirstThread; c < NR; c += kEpiThreads) {
+          const int r = w.r0 + c;
+          if (r < R) {
+            const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
+            atomicAdd(in->energy + r, 0.5 * sum);
+          }
+        }
+        epi_sync();
+      }
+    }
+  }
+  if (!ok) atomicOr(status, kErrWaitTimeout);
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, kCols);
+  }
+}
+
+template <int NR>
+constexpr int grouped_stages() {
+  return (208 * 1024) / (kBM * kChunkBytes + NR * kChunkBytes) > 8 ? 8 : (208 * 1024) / (kBM * kChunkBytes + NR * kChunkBytes);
+}
+
+template <int NR>
+constexpr size_t grouped_smem() {
+  return (size_t)grouped_stages<NR>() * (kBM * kChunkBytes + NR * kChunkBytes) + 1024;
+}
+
+}  // namespace tck
+}  // namespace sbk

@@ -1,0 +1,99 @@
+// Host-side state of the grouped tensor-core path (sb_grouped.cu).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "sb.h"
+
+namespace sbk {
+
+// Per-instance descriptor read by the grouped kernel (device memory, 64-byte aligned for the
+// tensor maps).
+struct alignas(64) GInst {
+  CUtensorMap tmA;       // J operand FP8 [Np][Kp], 128 x 128-byte boxes, 128B swizzle
+  CUtensorMap tmB[2];    // V operand FP8 [Rp][Kp] buffers, 128-byte x NR boxes
+  uint8_t *v[2];         // the V buffers
+  float *x, *y;          // state [R][xp]
+  const float *h;        // fields or null
+  double *energy;        // [R] energies (energy pass)
+  const float *pumps;    // [steps] a0 - a(t)
+  int n, Kp, R, Rp, xp;
+  int t0;                // the instance's step t = tick - t0
+  float c0, dt, dta0;
+  int pad_;
+};
+
+// One work item: a 128-spin x NR-replica tile of one instance.
+struct GItem {
+  int inst, m0, r0, kchunks;
+};
+
+// dSB with integer |J| <= 16 (exact FP8 operands) and n * 16 < 2^24 (exact FP32 accumulation).
+bool grouped_supports(const sb_problem *p, const sb_params *prm);
+// device bytes one instance holds while resident
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr);
+
+struct GHost {
+  int tag = 0;                  // caller's index / ticket
+  const sb_problem *prob = nullptr;
+  int n = 0, R = 0, steps = 0, t0 = 0, Np = 0, Kp = 0, Rp = 0, xp = 0;
+  float c0 = 0, dt = 0, dta0 = 0;
+  uint64_t seed = 0;
+  uint8_t *a = nullptr, *v[2] = {nullptr, nullptr};
+  float *x = nullptr, *y = nullptr, *h = nullptr, *pumps = nullptr;
+  double *energy = nullptr;
+  GInst desc;
+};
+
+class Grouped {
+ public:
+  explicit Grouped(cudaStream_t s, int replica_tile, int item_order) : st(s), nr(replica_tile), order(item_order) {}
+  ~Grouped();
+  // Uploads p (host), converts J to FP8, seeds the state. t0: the tick at which its step 0 runs.
+  sb_status add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err);
+  void remove(int idx);
+  // Changes the replica tile (reallocates the operand buffers; the state must be re-initialised).
+  sb_status retile(int new_nr, std::string &err);
+  void clear();
+  // Re-uploads the instance / item tables after add / remove (synchronous).
+  sb_status sync_tables(std::string &err);
+  // Steps ticks [tick0, tick0 + count) for every resident instance (a CUDA graph when use_graph).
+  cudaError_t run_steps(int tick0, int count, bool use_graph);
+  // Energies of every resident instance's current spins (instances must be at step t = tick - t0).
+  cudaError_t energy_pass(int tick);
+  sb_status init_state(GHost &g, uint64_t seed, std::string &err);
+  std::string tune_key() const;
+  static std::vector<std::pair<int, int>> candidates(int R);
+  void set_order(int o) {
+    if (o != order) {
+      order = o;
+      dirty = true;
+    }
+  }
+
+  cudaStream_t st;
+  int nr, order;
+  std::vector<GHost> insts;
+  int64_t launches = 0;
+  int n_items = 0;
+  uint32_t *d_status = nullptr;
+
+ private:
+  cudaError_t launch(int tick, int emode);
+  void free_instance(GHost &g);
+  GInst *d_insts = nullptr;
+  GItem *d_items = nullptr;
+  int cap_insts = 0, cap_items = 0;
+  float *d_stage = nullptr;
+  size_t stage_bytes = 0;
+  bool dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  int graph_tick0 = -1, graph_count = -1;
+};
+
+}  // namespace sbk

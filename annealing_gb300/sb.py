@@ -153,6 +153,12 @@ _SIGS = {
     "sb_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(ResultStruct), C.c_int32]),
     "sb_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sb_serving_stats_get": (C.c_int, [C.c_void_p, C.POINTER(ServingStats)]),
+    "sb_batch_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.c_int32, C.POINTER(Params),
+                                  C.POINTER(C.c_void_p)]),
+    "sb_batch_run": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(ResultStruct)]),
+    "sb_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sb_solve_batch": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.c_int32, C.POINTER(Params),
+                                 C.POINTER(ResultStruct)]),
     "sb_dsb_solve_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -346,6 +352,39 @@ class Plan:
             pass
 
 
+class Batch:
+    """Many instances solved together by the grouped tensor-core kernel (sb_batch_*)."""
+
+    def __init__(self, ctx: "Context", problems, params: Params, want_state: bool = False):
+        self.ctx, self.problems, self.params, self.want_state = ctx, list(problems), params, want_state
+        self._arr = (ProblemStruct * len(self.problems))(*[p.s for p in self.problems])
+        h = C.c_void_p()
+        _check(lib().sb_batch_create(ctx.h, self._arr, len(self.problems), C.byref(params), C.byref(h)), ctx.h)
+        self.h = h
+
+    def run(self, seed: Optional[int] = None):
+        bufs = [_ResultBuffers(p.n, self.params, self.want_state) for p in self.problems]
+        arr = (ResultStruct * len(bufs))(*[b.r for b in bufs])
+        sd = self.params.seed if seed is None else seed
+        _check(lib().sb_batch_run(self.h, sd, arr), self.ctx.h)
+        out = []
+        for b, r in zip(bufs, arr):
+            b.r = r
+            out.append(b.result())
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            lib().sb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One device, one stream (cudaStream_t as an integer handle, or None for an owned one)."""
 
@@ -363,6 +402,9 @@ class Context:
 
     def plan(self, problem: Problem, params: Params, want_state: bool = False) -> Plan:
         return Plan(self, problem, params, want_state)
+
+    def batch(self, problems, params: Params, want_state: bool = False) -> Batch:
+        return Batch(self, problems, params, want_state)
 
     def submit(self, problem: Problem, params: Params) -> int:
         t = C.c_uint64()

@@ -207,6 +207,22 @@ sb_status sb_plan_destroy(sb_plan *plan);
 /* bytes of HBM a plan for (p, params) would hold */
 int64_t sb_plan_footprint(const sb_problem *p, const sb_params *params);
 
+/* ---- batches: many instances of uneven size, solved together ----
+ * The reference runs one instance per program run and its trials one after another
+ * (SB/CUDA_GPU/m2_opt.cu:152). A batch advances every instance, with all of its replicas, in one
+ * grouped tensor-core launch per SB step (dSB, integer |J| <= 16 on exact FP8 operands), the step
+ * loop replayed from a CUDA graph; the replica tile and work order are chosen by timing the
+ * candidates on the batch itself (cached per shape). params is shared; instance k uses seed
+ * seed + k; results[k] is filled as sb_solve would fill it (arrays sized for instance k). The
+ * problems must stay alive until sb_batch_destroy. */
+typedef struct sb_batch sb_batch;
+sb_status sb_batch_create(sb_ctx *ctx, const sb_problem *problems, int32_t count,
+                          const sb_params *params, sb_batch **out);
+sb_status sb_batch_run(sb_batch *batch, uint64_t seed, sb_result *results);
+sb_status sb_batch_destroy(sb_batch *batch);
+sb_status sb_solve_batch(sb_ctx *ctx, const sb_problem *problems, int32_t count,
+                         const sb_params *params, sb_result *results);
+
 /* ---- serving: continuous batching ----
  * sb_submit copies the problem, queues it and returns a ticket at once. A worker thread admits
  * queued requests while the context's HBM budget and in-flight limit allow, runs all admitted
@@ -238,7 +254,7 @@ sb_status sb_serving_stats_get(sb_ctx *ctx, sb_serving_stats *out);
  * d_energies [replicas] (final energies), all on `stream` (a cudaStream_t, NULL = legacy default
  * stream) of the current device. c0 must be given (> 0; sb_default_c0 on the host problem gives
  * the usual value). The call returns when the work has finished.
- * Scratch is one fixed array of 8,454,400 bytes in the library's device memory, held by every GPU
+ * Scratch is one fixed array of 8,455,168 bytes in the library's device memory, held by every GPU
  * that loads the library until the process exits; hence the limits n <= 2048, replicas <= 1024,
  * steps <= 16384 (larger sizes return SB_ERR_INVALID_ARG). The first call on a device looks up
  * the array's device address; make that first call before any stream capture. All calls share the

@@ -1,0 +1,55 @@
+"""Grouped tensor-core batches (sb_batch_*): every instance bit-exact against the CPU oracle."""
+import numpy as np
+import pytest
+
+import annealing_gb300 as sb
+from annealing_gb300 import instances
+from oracle import binding as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def make_instances(ns, jmax=4, with_h=(2,)):
+    out = []
+    for k, n in enumerate(ns):
+        J = instances.erdos_renyi(n, 0.3 + 0.1 * (k % 5), seed=50 + k, jmax=jmax, allow_zero=jmax > 1)
+        h = np.random.default_rng(k).integers(-3, 4, n).astype(np.float32) if k in with_h else None
+        out.append((J, h))
+    return out
+
+
+@pytest.mark.parametrize("R", [64, 32, 100])
+def test_batch_matches_oracle(ctx, R):
+    ns = [64, 100, 129, 300, 513, 1000]
+    insts = make_instances(ns)
+    probs = [sb.Problem.from_dense(J, h) for J, h in insts]
+    steps, seed = 30, 100
+    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
+    batch = ctx.batch(probs, prm, want_state=True)
+    res = batch.run()
+    for k, ((J, h), p, r) in enumerate(zip(insts, probs, res)):
+        x, y = orc.init_uniform(J.shape[0], R, seed + k)
+        orc.sb_run_f32(2, J, h, x, y, steps, 1.0, p.default_c0(), 1.25)
+        np.testing.assert_array_equal(r.final_x, x, err_msg=f"instance {k}")
+        np.testing.assert_array_equal(r.final_y, y, err_msg=f"instance {k}")
+        np.testing.assert_array_equal(r.replica_energies, orc.energies_of_x(J, h, x))
+        assert r.energy_check_ok and r.best_energy_i64 == r.best_energy
+    again = batch.run()
+    for r, r2 in zip(res, again):
+        np.testing.assert_array_equal(r.final_x, r2.final_x)
+    batch.close()
+
+
+def test_batch_rejects_real_couplings(ctx):
+    J, h = instances.gaussian(64, seed=1)
+    prm = sb.Params.default(sb.DSB, steps=10, replicas=32, field_mode=sb.FIELD_TC)
+    with pytest.raises(sb.SBError) as e:
+        ctx.batch([sb.Problem.from_dense(J, h)], prm)
+    assert e.value.status == 6
+
+
+def test_batch_profile_reports_step_kernel_time(ctx):
+    probs = [sb.Problem.from_dense(J, h) for J, h in make_instances([256, 700])]
+    prm = sb.Params.default(sb.DSB, steps=12, replicas=64, field_mode=sb.FIELD_TC, profile=1)
+    res = ctx.batch(probs, prm).run()
+    assert res[0].kernel_ms_avg > 0 and res[0].steps_per_launch == 1
