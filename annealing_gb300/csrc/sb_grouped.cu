@@ -113,6 +113,9 @@ void Grouped::clear() {
   cudaFree(d_items);
   cudaFree(d_status);
   cudaFree(d_stage);
+  cudaFree(d_sub_items);
+  d_sub_items = nullptr;
+  cap_sub = 0;
   if (graph) cudaGraphExecDestroy(graph);
   d_insts = nullptr;
   d_items = nullptr;
@@ -332,7 +335,9 @@ sb_status Grouped::sync_tables(std::string &err) {
   return SB_OK;
 }
 
-cudaError_t Grouped::launch(int tick, int emode) {
+cudaError_t Grouped::launch(int tick, int emode) { return launch_items(d_items, n_items, tick, emode); }
+
+cudaError_t Grouped::launch_items(const GItem *items_ptr, int count, int tick, int emode) {
   const void *k = nullptr;
   size_t smem = 0;
   if (!grouped_kernel_for(nr, emode, &k, &smem)) return cudaErrorInvalidValue;
@@ -346,11 +351,11 @@ cudaError_t Grouped::launch(int tick, int emode) {
       done[k] = true;
     }
   }
-  if (n_items == 0) return cudaSuccess;
-  const int grid = std::min(n_items, device_sms());
+  if (count == 0) return cudaSuccess;
+  const int grid = std::min(count, device_sms());
   const GInst *pi = d_insts;
-  const GItem *pit = d_items;
-  int ni = n_items;
+  const GItem *pit = items_ptr;
+  int ni = count;
   uint32_t *ps = d_status;
   void *args[] = {(void *)&pi, (void *)&pit, (void *)&ni, (void *)&tick, (void *)&ps};
   ++launches;
@@ -404,6 +409,32 @@ cudaError_t Grouped::energy_pass(int tick) {
     if (e != cudaSuccess) return e;
   }
   return launch(tick, kEmodeEnergy);
+}
+
+cudaError_t Grouped::energy_pass_for(const std::vector<int> &idx, int tick) {
+  std::vector<GItem> items;
+  for (int i : idx) {
+    const GHost &g = insts[i];
+    cudaError_t e = cudaMemsetAsync(g.energy, 0, (size_t)g.R * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    for (int m0 = 0; m0 < g.Np; m0 += kBM)
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{i, m0, r0, g.Kp / kChunkBytes});
+  }
+  if (items.empty()) return cudaSuccess;
+  if ((int)items.size() > cap_sub) {
+    cudaFree(d_sub_items);
+    cap_sub = std::max<int>((int)items.size(), 2 * cap_sub);
+    cudaError_t e = cudaMalloc(&d_sub_items, (size_t)cap_sub * sizeof(GItem));
+    if (e != cudaSuccess) {
+      cap_sub = 0;
+      return e;
+    }
+  }
+  cudaError_t e = cudaMemcpyAsync(d_sub_items, items.data(), items.size() * sizeof(GItem), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = launch_items(d_sub_items, (int)items.size(), tick, kEmodeEnergy);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);  // `items` is a host temporary
 }
 
 // ---- autotuning: replica tile and item order, timed on the batch itself ----

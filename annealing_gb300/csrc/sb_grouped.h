@@ -66,6 +66,14 @@ class Grouped {
   cudaError_t run_steps(int tick0, int count, bool use_graph);
   // Energies of every resident instance's current spins (instances must be at step t = tick - t0).
   cudaError_t energy_pass(int tick);
+  // The same for a subset of resident instances (indices into insts).
+  cudaError_t energy_pass_for(const std::vector<int> &idx, int tick);
+  // Index of the resident instance with this tag, or -1.
+  int find(int tag) const {
+    for (size_t i = 0; i < insts.size(); ++i)
+      if (insts[i].tag == tag) return (int)i;
+    return -1;
+  }
   sb_status init_state(GHost &g, uint64_t seed, std::string &err);
   std::string tune_key() const;
   static std::vector<std::pair<int, int>> candidates(int R);
@@ -85,6 +93,9 @@ class Grouped {
 
  private:
   cudaError_t launch(int tick, int emode);
+  cudaError_t launch_items(const GItem *items, int count, int tick, int emode);
+  GItem *d_sub_items = nullptr;
+  int cap_sub = 0;
   void free_instance(GHost &g);
   GInst *d_insts = nullptr;
   GItem *d_items = nullptr;

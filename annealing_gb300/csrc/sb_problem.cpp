@@ -1,11 +1,13 @@
 // Host-side problem handling: graph reader, coefficients, schedule, exact energy evaluators.
 // No CUDA here; everything in this file works without a GPU.
 #include <math.h>
+#include <algorithm>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sb.h"
@@ -432,4 +434,79 @@ extern "C" sb_status sb_load_graph_ex(const char *path, const sb_graph_opts *opt
 
 extern "C" sb_status sb_load_graph(const char *path, sb_problem *out) {
   return sb_load_graph_ex(path, nullptr, out);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Seeded random instances (Erdos-Renyi G(n, p) with integer or +-1 couplings), generated from a
+// counter hash of (seed, i, j) so every row is independent: parallel over host threads and
+// identical for any thread count.
+
+namespace {
+inline uint64_t mix(uint64_t z) {
+  z ^= z >> 30;
+  z *= 0xBF58476D1CE4E5B9ULL;
+  z ^= z >> 27;
+  z *= 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return z;
+}
+}  // namespace
+
+extern "C" sb_status sb_problem_random(sb_problem *p, int32_t n, double density, int32_t jmax,
+                                       int32_t field_max, uint64_t seed) {
+  if (!p || n <= 0 || n > 65536 || !(density >= 0.0 && density <= 1.0) || jmax < 1 || field_max < 0)
+    return SB_ERR_INVALID_ARG;
+  memset(p, 0, sizeof(*p));
+  const size_t nn = (size_t)n * (size_t)n;
+  p->J = (float *)malloc(nn * sizeof(float));
+  if (!p->J) return SB_ERR_OOM;
+  if (field_max > 0) {
+    p->h = (float *)malloc((size_t)n * sizeof(float));
+    if (!p->h) {
+      free(p->J);
+      p->J = nullptr;
+      return SB_ERR_OOM;
+    }
+  }
+  const uint64_t thr = density >= 1.0 ? ~0ULL : (uint64_t)(density * 18446744073709551616.0);
+  const unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+  std::vector<std::thread> th;
+  for (unsigned w = 0; w < nt; ++w)
+    th.emplace_back([=] {
+      for (int i = (int)w; i < n; i += (int)nt) {
+        float *Ji = p->J + (size_t)i * n;
+        Ji[i] = 0.0f;
+        for (int j = i + 1; j < n; ++j) {
+          const uint64_t z = mix(seed * 0x9E3779B97F4A7C15ULL + ((uint64_t)i << 32) + (uint64_t)j + 1);
+          float w8 = 0.0f;
+          if (density >= 1.0 || mix(z ^ 0x5851F42D4C957F2DULL) < thr) {
+            if (jmax == 1)
+              w8 = (z & 1) ? 1.0f : -1.0f;
+            else
+              w8 = (float)((int64_t)(z % (uint64_t)(2 * jmax + 1)) - jmax);
+          }
+          Ji[j] = w8;
+        }
+      }
+    });
+  for (auto &t : th) t.join();
+  // lower triangle from the upper one
+  th.clear();
+  for (unsigned w = 0; w < nt; ++w)
+    th.emplace_back([=] {
+      for (int i = (int)w; i < n; i += (int)nt) {
+        float *Ji = p->J + (size_t)i * n;
+        for (int j = 0; j < i; ++j) Ji[j] = p->J[(size_t)j * n + i];
+      }
+    });
+  for (auto &t : th) t.join();
+  if (p->h)
+    for (int i = 0; i < n; ++i) {
+      const uint64_t z = mix(seed * 0xD1B54A32D192ED03ULL + (uint64_t)i + 7);
+      p->h[i] = (float)((int64_t)(z % (uint64_t)(2 * field_max + 1)) - field_max);
+    }
+  p->n = n;
+  p->lib_owned = 1;
+  sbh::problem_scan(p);
+  return SB_OK;
 }

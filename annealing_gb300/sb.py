@@ -132,6 +132,8 @@ _SIGS = {
                                   C.POINTER(C.c_float)]),
     "sb_problem_wrap": (C.c_int, [C.POINTER(ProblemStruct), C.c_int32, C.c_void_p, C.c_void_p]),
     "sb_problem_free": (None, [C.POINTER(ProblemStruct)]),
+    "sb_problem_random": (C.c_int, [C.POINTER(ProblemStruct), C.c_int32, C.c_double, C.c_int32, C.c_int32,
+                                    C.c_uint64]),
     "sb_coupling_std": (C.c_double, [C.POINTER(ProblemStruct)]),
     "sb_default_c0": (C.c_float, [C.POINTER(ProblemStruct)]),
     "sb_pump": (C.c_float, [C.c_float, C.c_int32, C.c_int32]),
@@ -222,6 +224,14 @@ class Problem:
         st = ProblemStruct()
         _check(lib().sb_problem_wrap(C.byref(st), n, J_ptr, h_ptr or None))
         return cls(st, owner=keepalive)
+
+    @classmethod
+    def random(cls, n: int, density: float = 1.0, jmax: int = 1, field_max: int = 0,
+               seed: int = 1234) -> "Problem":
+        """Seeded G(n, density) instance: couplings +-1 (jmax = 1) or uniform in [-jmax, jmax]."""
+        st = ProblemStruct()
+        _check(lib().sb_problem_random(C.byref(st), n, density, jmax, field_max, seed))
+        return cls(st)
 
     @classmethod
     def load(cls, path: str, index_base: int = -1, n: int = 0, strict: bool = False) -> "Problem":

@@ -181,6 +181,13 @@ sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, const float 
  * unchanged while p is used; J must already be symmetric with a zero diagonal). */
 sb_status sb_problem_wrap(sb_problem *p, int32_t n, float *J, float *h);
 void sb_problem_free(sb_problem *p);
+/* Seeded random instance, generated on the host threads: each pair i < j is an edge with
+ * probability `density`; an edge's coupling is +-1 (jmax == 1) or uniform in [-jmax, jmax];
+ * field_max > 0 adds fields h_i uniform in [-field_max, field_max]. The same seed gives the same
+ * instance on any machine and thread count (the generators of SA_naive/CUDA_GPU/tests/fully.py
+ * and NMFA/CUDA_GPU/tests/fully.py play this role in the reference, unseeded). */
+sb_status sb_problem_random(sb_problem *p, int32_t n, double density, int32_t jmax,
+                            int32_t field_max, uint64_t seed);
 /* std of the off-diagonal couplings and the default c0 for that problem */
 double sb_coupling_std(const sb_problem *p);
 float sb_default_c0(const sb_problem *p);
@@ -224,13 +231,20 @@ sb_status sb_solve_batch(sb_ctx *ctx, const sb_problem *problems, int32_t count,
                          const sb_params *params, sb_result *results);
 
 /* ---- serving: continuous batching ----
- * sb_submit copies the problem, queues it and returns a ticket at once. A worker thread admits
- * queued requests while the context's HBM budget and in-flight limit allow, runs all admitted
- * requests' steps together (one grouped launch per step over every resident request), retires
- * each request at its own step budget and frees its memory for the next. */
+ * sb_submit queues a request and returns a ticket at once; the problem (and its J / h) must stay
+ * alive until sb_poll has returned the request's final status. A worker thread admits queued
+ * requests in arrival order while the context's HBM budget and in-flight limit allow, and
+ * advances every admitted request together (one grouped tensor-core launch per step over all
+ * resident requests, each on its own schedule), so requests that arrive while others run join
+ * them at the next step. Each request retires at its own step budget (energies, best spins, exact
+ * host re-check) and its device memory goes to the next. dSB requests with integer |J| <= 16 use
+ * the grouped engine; others are solved one at a time between steps. Results equal those of
+ * sb_solve with the same parameters (field_mode SB_FIELD_TC for the grouped ones). */
 sb_status sb_submit(sb_ctx *ctx, const sb_problem *p, const sb_params *params, uint64_t *ticket);
-/* SB_OK when finished (res filled; the ticket is released), SB_ERR_PENDING otherwise.
- * res->best_spins etc. must hold n / replicas entries. wait_ms < 0 blocks until done. */
+/* SB_OK when finished (res filled; the ticket is released), SB_ERR_PENDING otherwise, or the
+ * request's error (SB_ERR_CANCELLED after sb_cancel). res->best_spins / replica_energies must hold
+ * n / replicas entries; res->total_ms is the latency from sb_submit to the result, device_ms the
+ * time from admission to retirement. wait_ms < 0 blocks until done. */
 sb_status sb_poll(sb_ctx *ctx, uint64_t ticket, sb_result *res, int32_t wait_ms);
 sb_status sb_cancel(sb_ctx *ctx, uint64_t ticket);
 /* latency of every finished request in submission order: arrival->result ms, and queue stats */
