@@ -44,6 +44,12 @@ WORKLOADS = {
     "batched-bsb": ("bsb", 8192, 256, 3000, "tc",
                     "batched bSB: complete N=8192, J ~ N(0,1/N), h ~ N(0,0.1), R=256, 3000 steps, "
                     "BF16 hi+lo tensor-core field"),
+    "uneven-batch": ("dsb", 0, 64, 1500, "grouped",
+                     "uneven batch: 512 instances, N ~ U[64,4096], Erdos-Renyi density ~ U[0.05,1], "
+                     "J = +-1, R=64, 1500 steps, one grouped tensor-core launch per step"),
+    "serving": ("dsb", 0, 32, 0, "serving",
+                "serving stream: Poisson arrivals at 200/s, N log-uniform in [128,16384], density "
+                "~ U[0.01,1], J ~ U{-8..8}, R=32, step budget ~ U[500,4000]"),
 }
 
 
@@ -313,6 +319,181 @@ def run_ours(args, rank, world, local_rank):
     ctx.close()
 
 
+def batch_instances(seed_base=1234, count=512):
+    """The uneven-batch instances (library generator, seeded 1234 + k)."""
+    import annealing_gb300 as sb
+    from annealing_gb300 import instances
+
+    spec = instances.uneven_batch(count, seed=seed_base)
+    return [sb.Problem.random(n, d, 1, 0, seed=s) for n, d, s in spec]
+
+
+def run_batch(args, rank, world, local_rank):
+    import torch
+
+    import annealing_gb300 as sb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    variant, _, R, sb_steps, field, desc = WORKLOADS[args.workload]
+    probs = batch_instances()
+    n_sum = sum(p.n for p in probs)
+    stream = torch.cuda.current_stream(dev)
+    ctx = sb.Context(local_rank, stream=stream.cuda_stream)
+    prm = sb.Params.default(sb.DSB, steps=sb_steps, replicas=R, seed=1234 + 1000 * rank, field_mode=sb.FIELD_TC)
+    t0 = time.perf_counter()
+    batch = ctx.batch(probs, prm)
+    setup_s = time.perf_counter() - t0
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for k in range(args.warmup):
+        batch.run(seed=10 + k)
+    barrier()
+    times, launches, quality = [], 0, []
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = batch.run(seed=100 + k)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            launches += res[0].kernel_launches
+            quality.append(all(r.energy_check_ok for r in res))
+        barrier()
+    total_ms = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    updates = float(n_sum) * R * sb_steps
+    value = world * updates * args.steps / (total_ms * 1e-3)
+    # roofline: one profiled run, event pair around every grouped step launch
+    prm_p = sb.Params.default(sb.DSB, steps=24, replicas=R, seed=7, field_mode=sb.FIELD_TC, profile=1)
+    bp = ctx.batch(probs, prm_p)
+    bp.run()
+    rp = bp.run(seed=8)
+    bp.close()
+    hbm, bf16, src = peaks()
+    np_kp = sum(((p.n + 127) // 128 * 128) ** 2 for p in probs)
+    bytes_per_launch = np_kp + sum(p.n for p in probs) * R * 17.0  # FP8 J + (x, y in/out, next operand)
+    achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": "grouped_kernel (one launch per SB step)",
+            "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
+            "peak_source": f"{src} HBM copy"}
+    # e2e: sb_solve_batch from host buffers every step (upload, convert, run, results back)
+    e2e_ms = []
+    for k in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        ctx.batch(probs, prm).run(seed=200 + k)
+        e2e_ms.append(1e3 * (time.perf_counter() - t1))
+    e2e_total = float(sum(e2e_ms))
+    if rank != 0:
+        return
+    line = {
+        "metric": "SB spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp8e4m3 field (f32 accumulate), f32 state", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "instances": len(probs), "sum_n": n_sum, "replicas": R,
+                   "sb_steps": sb_steps, "parallelism": f"replicas-only x{world}",
+                   "l2": "inputs (2.9 GB of J) larger than L2; 256 MB flush between runs"},
+        "e2e": {"value": world * updates * args.steps / (e2e_total * 1e-3), "unit": "spin-updates/s",
+                "h2d_bytes_per_step": int(sum(p.n * p.n * 4 for p in probs)),
+                "d2h_bytes_per_step": int(sum(p.n + 8 * R for p in probs)),
+                "ms_per_step": e2e_total / args.steps},
+        "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary(),
+        "quality": {"energy_check_ok": all(quality)}, "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, rank, world, local_rank):
+    import threading as th
+
+    import torch
+
+    import annealing_gb300 as sb
+    from annealing_gb300 import instances
+
+    torch.cuda.set_device(local_rank)
+    variant, _, R, _, field, desc = WORKLOADS[args.workload]
+    count = args.requests
+    stream = instances.serving_stream(count=count, seed=1234 + rank)
+    # a pool of distinct instances drawn from the request-size distribution; each request takes
+    # the pool instance nearest its own N (the pool keeps host memory bounded)
+    rng = np.random.default_rng(99)
+    pool_n = sorted(set(int(v) for v in np.exp(rng.uniform(np.log(128), np.log(16384), size=args.pool))))
+    pool = [sb.Problem.random(n, float(rng.uniform(0.01, 1.0)), 8, 0, seed=5000 + i) for i, n in enumerate(pool_n)]
+    pool_arr = np.array(pool_n)
+    ctx = sb.Context(local_rank)
+    # warm-up: a few requests through the server (kernels, allocator)
+    for k in range(args.warmup):
+        p = pool[0]
+        prm = sb.Params.default(sb.DSB, steps=100, replicas=R, seed=k, field_mode=sb.FIELD_TC)
+        ctx.poll(ctx.submit(p, prm), p.n, prm, wait_ms=-1)
+    reqs = []
+    for (arr, n, dens, steps, seed) in stream:
+        i = int(np.argmin(np.abs(pool_arr - n)))
+        reqs.append((arr, pool[i], sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed,
+                                                     field_mode=sb.FIELD_TC)))
+    tickets = [None] * len(reqs)
+    t_start = time.perf_counter()
+
+    def producer():
+        for k, (arr, p, prm) in enumerate(reqs):
+            now = time.perf_counter() - t_start
+            if arr > now:
+                time.sleep(arr - now)
+            tickets[k] = ctx.submit(p, prm)
+
+    with ClockSampler(local_rank) as clk:
+        pt = th.Thread(target=producer)
+        pt.start()
+        results = [None] * len(reqs)
+        for k in range(len(reqs)):
+            while tickets[k] is None:
+                time.sleep(0.001)
+            arr, p, prm = reqs[k]
+            results[k] = ctx.poll(tickets[k], p.n, prm, wait_ms=-1)
+        pt.join()
+        makespan = time.perf_counter() - t_start
+    lat = np.array([r.total_ms for r in results])
+    updates = float(sum(p.n * R * prm.steps for _, p, prm in reqs))
+    stats = ctx.serving_stats()
+    if rank != 0:
+        return
+    line = {
+        "metric": "SB spin-updates/s (serving stream)", "value": updates / makespan,
+        "unit": "spin-updates/s", "n_gpus": world, "steps": len(reqs), "warmup": args.warmup,
+        "ms_per_step": 1e3 * makespan / len(reqs), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp8e4m3 field (f32 accumulate), f32 state",
+        "data": "synthetic (seeded Poisson stream; sizes from a pool of distinct instances)",
+        "config": {"workload": desc, "requests": len(reqs), "rate_per_s": 200.0,
+                   "pool_instances": len(pool), "replicas": R},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+        "makespan_s": makespan, "arrival_span_s": reqs[-1][0],
+        "requests_per_s": len(reqs) / makespan, "serving": stats,
+        "quality": {"energy_check_ok": all(r.energy_check_ok for r in results)},
+        "clocks": clk.summary(),
+        "e2e": {"value": updates / makespan, "unit": "spin-updates/s",
+                "h2d_bytes_per_step": int(np.mean([p.n * p.n * 4 for _, p, _ in reqs])),
+                "d2h_bytes_per_step": int(np.mean([p.n + 8 * R for _, p, _ in reqs]))},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -321,6 +502,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched-dsb")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=2000, help="serving workload: stream length")
+    ap.add_argument("--pool", type=int, default=64, help="serving workload: distinct instances")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -331,6 +514,10 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "uneven-batch":
+        run_batch(args, rank, world, local_rank)
+    elif args.workload == "serving":
+        run_serving(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1 and args.impl == "ours":
