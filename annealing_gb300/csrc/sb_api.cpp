@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <mutex>
 #include <string>
@@ -48,6 +49,8 @@ struct sb_plan {
   double *denergy = nullptr;
   uint32_t *dstatus = nullptr;
   float *dpump = nullptr;  // [steps] a0 - a(t), the schedule every kernel reads
+  float *dxk = nullptr;    // [kTopK][xp] rows of the best candidates (real-valued J)
+  double *dek = nullptr;   // [kTopK] their FP64 energies
   sbk::TcEngine *tc = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -55,6 +58,8 @@ struct sb_plan {
 };
 
 namespace {
+
+constexpr int kTopK = 8;  // replicas whose energy is recomputed in FP64 for real-valued couplings
 
 #define SB_CUDA(call)                                                                       \
   do {                                                                                      \
@@ -160,7 +165,11 @@ void plan_free_device(sb_plan *pl) {
   cudaFree(pl->denergy);
   cudaFree(pl->dstatus);
   cudaFree(pl->dpump);
+  cudaFree(pl->dxk);
+  cudaFree(pl->dek);
   pl->dpump = nullptr;
+  pl->dxk = nullptr;
+  pl->dek = nullptr;
   if (pl->ev0) cudaEventDestroy(pl->ev0);
   if (pl->ev1) cudaEventDestroy(pl->ev1);
   pl->graph = nullptr;
@@ -267,22 +276,25 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   return SB_OK;
 }
 
-// Energy pass over state x into slot (R doubles).
-cudaError_t enqueue_energy(sb_plan *pl, const float *x, double *slot, cudaStream_t st, int t) {
+// Energy pass over state x into slot (R doubles). FP32 fields (exact for integer J), FP64 on
+// request; rows: replicas in x (x has R rows unless given).
+cudaError_t enqueue_energy(sb_plan *pl, const float *x, double *slot, cudaStream_t st, int t, bool fp64 = false,
+                           int rows = -1) {
   if (pl->tc && pl->dtype != sbk::kTcBf16Split && pl->prm.variant == SB_DSB && t >= 0)
     return sbk::tc_energy(pl->tc, t, x, pl->dh, slot, pl->dstatus, st);
   sbk::PlainEnergy a;
+  const int R = rows > 0 ? rows : pl->R;
   a.n = pl->n;
-  a.R = pl->R;
+  a.R = R;
   a.jp = pl->jp;
   a.xp = pl->xp;
-  a.rb = pl->R < 8 ? pl->R : 8;
+  a.rb = R < 8 ? R : 8;
   a.J = pl->dJ;
   a.h = pl->dh;
   a.x = x;
   a.energy = slot;
   a.status = pl->dstatus;
-  return sbk::launch_plain_energy(a, !pl->integral, st);
+  return sbk::launch_plain_energy(a, fp64, st);
 }
 
 // Everything between the initial state and the final energy. Plain path: steps x (step kernel
@@ -439,15 +451,40 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
     launches += pl->launches_in_loop;
   }
   double *final_slot = pl->denergy + (tr ? (size_t)p.steps * R : 0);
-  SB_CUDA(enqueue_energy(pl, final_x(pl), final_slot, st, p.steps));
+  // Integer couplings: the FP32 field is exact. Real couplings: FP32 energies rank the replicas
+  // and the best kTopK are recomputed in FP64 (FP64 on every replica would cost more than the
+  // solve on this part).
+  const bool refine = !pl->integral;
+  SB_CUDA(enqueue_energy(pl, final_x(pl), final_slot, st, p.steps, refine && R <= kTopK));
   ++launches;
-  SB_CUDA(cudaEventRecord(pl->ev1, st));
   std::vector<double> e_final((size_t)R);
   uint32_t status = 0;
   SB_CUDA(cudaMemcpyAsync(e_final.data(), final_slot, (size_t)R * sizeof(double),
                           cudaMemcpyDeviceToHost, st));
   SB_CUDA(cudaMemcpyAsync(&status, pl->dstatus, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SB_CUDA(cudaStreamSynchronize(st));
+  if (refine && R > kTopK && status == 0) {
+    std::vector<int> order((size_t)R);
+    for (int r = 0; r < R; ++r) order[r] = r;
+    std::partial_sort(order.begin(), order.begin() + kTopK, order.end(),
+                      [&](int a, int b) { return e_final[a] < e_final[b]; });
+    if (!pl->dxk) {
+      SB_CUDA(cudaMalloc(&pl->dxk, (size_t)kTopK * pl->xp * sizeof(float)));
+      SB_CUDA(cudaMalloc(&pl->dek, (size_t)kTopK * sizeof(double)));
+    }
+    for (int q = 0; q < kTopK; ++q)
+      SB_CUDA(cudaMemcpyAsync(pl->dxk + (size_t)q * pl->xp, final_x(pl) + (size_t)order[q] * pl->xp,
+                              (size_t)pl->xp * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    SB_CUDA(cudaMemsetAsync(pl->dek, 0, (size_t)kTopK * sizeof(double), st));
+    SB_CUDA(enqueue_energy(pl, pl->dxk, pl->dek, st, -1, true, kTopK));
+    ++launches;
+    double ek[kTopK];
+    SB_CUDA(cudaMemcpyAsync(ek, pl->dek, sizeof(ek), cudaMemcpyDeviceToHost, st));
+    SB_CUDA(cudaStreamSynchronize(st));
+    for (int q = 0; q < kTopK; ++q) e_final[order[q]] = ek[q];
+    // the best replica is chosen among the FP64-refined candidates
+  }
+  SB_CUDA(cudaEventRecord(pl->ev1, st));
   if (status != 0) {
     err = "device status " + std::to_string(status) +
           ((status & sbk::kErrWaitTimeout) ? " (a bounded wait timed out)" : "");
@@ -456,6 +493,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   int best = 0;
   for (int r = 1; r < R; ++r)
     if (e_final[r] < e_final[best]) best = r;
+  SB_CUDA(cudaEventSynchronize(pl->ev1));
   std::vector<float> xb((size_t)n);
   SB_CUDA(cudaMemcpyAsync(xb.data(), final_x(pl) + (size_t)best * pl->xp, (size_t)n * sizeof(float),
                           cudaMemcpyDeviceToHost, st));

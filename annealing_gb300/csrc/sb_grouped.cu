@@ -12,6 +12,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sb_grouped.cuh"
@@ -83,6 +84,43 @@ bool grouped_kernel_for(int nr, int emode, const void **k, size_t *smem) {
   return false;
 }
 
+// E4M3 code of the integer v, |v| <= 16: 1.m x 2^(e - 7) with a 3-bit mantissa (every integer up
+// to 16 has at most 4 significant bits).
+uint8_t fp8_code(int v) {
+  if (v == 0) return 0;
+  const uint8_t sign = v < 0 ? 0x80 : 0;
+  int a = v < 0 ? -v : v;
+  int e = 0;
+  while ((2 << e) <= a) ++e;                // a in [2^e, 2^(e+1))
+  const int m = ((a << 3) >> e) - 8;        // (a / 2^e - 1) * 8, exact for these integers
+  return (uint8_t)(sign | ((e + 7) << 3) | m);
+}
+
+void pack_fp8(const float *J, int n, uint8_t *dst, int Np, int Kp) {
+  uint8_t lut[33];
+  for (int v = -16; v <= 16; ++v) lut[v + 16] = fp8_code(v);
+  // about 2 M elements per thread; several admissions pack at once
+  const unsigned want = (unsigned)std::max<int64_t>(1, (int64_t)Np * Kp / (2 << 20));
+  const unsigned nt = std::max(1u, std::min({std::thread::hardware_concurrency() / 2, want, 16u}));
+  const int rows_per = (Np + (int)nt - 1) / (int)nt;
+  std::vector<std::thread> th;
+  for (unsigned w = 0; w < nt; ++w)
+    th.emplace_back([=, &lut] {
+      const int r0 = (int)w * rows_per, r1 = std::min(Np, r0 + rows_per);
+      for (int i = r0; i < r1; ++i) {
+        uint8_t *d = dst + (size_t)i * Kp;
+        if (i >= n) {
+          memset(d, 0, Kp);
+          continue;
+        }
+        const float *Ji = J + (size_t)i * n;
+        for (int j = 0; j < n; ++j) d[j] = lut[(int)Ji[j] + 16];
+        memset(d + n, 0, Kp - n);
+      }
+    });
+  for (auto &t : th) t.join();
+}
+
 int device_sms() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -113,6 +151,10 @@ void Grouped::clear() {
   cudaFree(d_items);
   cudaFree(d_status);
   cudaFree(d_stage);
+  cudaStreamSynchronize(st);
+  cudaFreeHost(stg_.pin);
+  stg_.pin = nullptr;
+  stg_.bytes = 0;
   cudaFree(d_sub_items);
   d_sub_items = nullptr;
   cap_sub = 0;
@@ -126,28 +168,27 @@ void Grouped::clear() {
   cap_insts = cap_items = 0;
 }
 
-void Grouped::free_instance(GHost &g) {
-  cudaFree(g.a);
-  cudaFree(g.v[0]);
-  cudaFree(g.v[1]);
-  cudaFree(g.x);
-  cudaFree(g.y);
-  cudaFree(g.h);
-  cudaFree(g.energy);
-  cudaFree(g.pumps);
+void Grouped::free_instance(GHost &g) { release(g, st); }
+
+// Stream-ordered frees: the memory returns to the device pool once `s` passes this point, with no
+// device-wide synchronisation (plain cudaFree would stall every stream).
+void Grouped::release(GHost &g, cudaStream_t s) {
+  for (void *ptr : {(void *)g.a, (void *)g.v[0], (void *)g.v[1], (void *)g.x, (void *)g.y, (void *)g.h,
+                    (void *)g.energy, (void *)g.pumps})
+    if (ptr) cudaFreeAsync(ptr, s);
   g.a = g.v[0] = g.v[1] = nullptr;
   g.x = g.y = g.h = g.pumps = nullptr;
   g.energy = nullptr;
 }
 
-sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err) {
-  GHost g;
+sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
+                           cudaStream_t st, Staging &stg, std::string &err) {
   g.tag = tag;
   g.prob = p;
   g.n = p->n;
   g.R = prm->replicas;
   g.steps = prm->steps;
-  g.t0 = t0;
+  g.t0 = 0;
   g.Np = (g.n + 127) / 128 * 128;
   g.Kp = g.Np;
   g.Rp = (g.R + nr - 1) / nr * nr;
@@ -158,34 +199,37 @@ sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed,
   cudaError_t e;
   auto fail = [&](const char *what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
-    free_instance(g);
+    release(g, st);
     return e == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
   };
   const size_t xs = (size_t)g.R * g.xp * sizeof(float), vb = (size_t)g.Rp * g.Kp;
-  if ((e = cudaMalloc(&g.a, (size_t)g.Np * g.Kp)) != cudaSuccess) return fail("cudaMalloc(J operand)");
-  if ((e = cudaMalloc(&g.v[0], vb)) != cudaSuccess) return fail("cudaMalloc(V)");
-  if ((e = cudaMalloc(&g.v[1], vb)) != cudaSuccess) return fail("cudaMalloc(V)");
-  if ((e = cudaMalloc(&g.x, xs)) != cudaSuccess) return fail("cudaMalloc(x)");
-  if ((e = cudaMalloc(&g.y, xs)) != cudaSuccess) return fail("cudaMalloc(y)");
-  if ((e = cudaMalloc(&g.energy, (size_t)g.R * sizeof(double))) != cudaSuccess) return fail("cudaMalloc(energy)");
-  if ((e = cudaMalloc(&g.pumps, (size_t)(g.steps > 0 ? g.steps : 1) * sizeof(float))) != cudaSuccess)
+  if ((e = cudaMallocAsync(&g.a, (size_t)g.Np * g.Kp, st)) != cudaSuccess) return fail("cudaMalloc(J operand)");
+  if ((e = cudaMallocAsync(&g.v[0], vb, st)) != cudaSuccess) return fail("cudaMalloc(V)");
+  if ((e = cudaMallocAsync(&g.v[1], vb, st)) != cudaSuccess) return fail("cudaMalloc(V)");
+  if ((e = cudaMallocAsync(&g.x, xs, st)) != cudaSuccess) return fail("cudaMalloc(x)");
+  if ((e = cudaMallocAsync(&g.y, xs, st)) != cudaSuccess) return fail("cudaMalloc(y)");
+  if ((e = cudaMallocAsync(&g.energy, (size_t)g.R * sizeof(double), st)) != cudaSuccess) return fail("cudaMalloc(energy)");
+  if ((e = cudaMallocAsync(&g.pumps, (size_t)(g.steps > 0 ? g.steps : 1) * sizeof(float), st)) != cudaSuccess)
     return fail("cudaMalloc(pumps)");
   if (p->h) {
-    if ((e = cudaMalloc(&g.h, (size_t)g.n * sizeof(float))) != cudaSuccess) return fail("cudaMalloc(h)");
+    if ((e = cudaMallocAsync(&g.h, (size_t)g.n * sizeof(float), st)) != cudaSuccess) return fail("cudaMalloc(h)");
     if ((e = cudaMemcpyAsync(g.h, p->h, (size_t)g.n * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return fail("upload h");
   }
-  // couplings: FP32 through a staging buffer, converted to FP8 on the device
-  const size_t jb = (size_t)g.n * g.n * sizeof(float);
-  if (jb > stage_bytes) {
-    cudaFree(d_stage);
-    d_stage = nullptr;
-    stage_bytes = 0;
-    if ((e = cudaMalloc(&d_stage, jb)) != cudaSuccess) return fail("cudaMalloc(staging)");
-    stage_bytes = jb;
+  // couplings: packed to FP8 E4M3 on the host threads (integers |J| <= 16 are exact, see
+  // fp8_code) into a pinned staging buffer, then one copy into the padded operand layout: a
+  // quarter of the bytes of an FP32 upload.
+  const size_t ab = (size_t)g.Np * g.Kp;
+  if (ab > stg.bytes) {
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("synchronize");
+    cudaFreeHost(stg.pin);
+    stg.pin = nullptr;
+    stg.bytes = 0;
+    if ((e = cudaMallocHost(&stg.pin, ab)) != cudaSuccess) return fail("cudaMallocHost(staging)");
+    stg.bytes = ab;
   }
-  if ((e = cudaMemcpyAsync(d_stage, p->J, jb, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
-  g_convert_kernel<<<grid1((size_t)g.Np * g.Kp), 256, 0, st>>>(d_stage, g.n, g.a, g.Np, g.Kp);
+  pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
+  if ((e = cudaMemcpyAsync(g.a, stg.pin, ab, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
   std::vector<float> pumps((size_t)(g.steps > 0 ? g.steps : 1), 0.0f);
   for (int t = 0; t < g.steps; ++t) pumps[t] = sb_pump(prm->a0, t, g.steps);
   if ((e = cudaMemcpyAsync(g.pumps, pumps.data(), pumps.size() * sizeof(float), cudaMemcpyHostToDevice, st)) !=
@@ -215,17 +259,40 @@ sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed,
   g.desc.R = g.R;
   g.desc.Rp = g.Rp;
   g.desc.xp = g.xp;
-  g.desc.t0 = t0;
+  g.desc.t0 = 0;
   g.desc.c0 = g.c0;
   g.desc.dt = g.dt;
   g.desc.dta0 = g.dta0;
   g.seed = seed;
-  insts.push_back(g);
-  dirty = true;
-  return init_state(insts.back(), seed, err);
+  sb_status s = init_state_on(g, seed, st, err);
+  if (s != SB_OK) {
+    release(g, st);
+    return s;
+  }
+  // the instance is complete before another stream uses it
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("synchronize");
+  return SB_OK;
 }
 
-sb_status Grouped::init_state(GHost &g, uint64_t seed, std::string &err) {
+void Grouped::attach(GHost &g, int t0) {
+  g.t0 = t0;
+  g.desc.t0 = t0;
+  insts.push_back(g);
+  dirty = true;
+}
+
+sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err) {
+  GHost g;
+  sb_status s = prepare(g, p, prm, seed, tag, nr, st, stg_, err);
+  if (s != SB_OK) return s;
+  attach(g, t0);
+  return SB_OK;
+}
+
+
+sb_status Grouped::init_state(GHost &g, uint64_t seed, std::string &err) { return init_state_on(g, seed, st, err); }
+
+sb_status Grouped::init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err) {
   cudaError_t e = launch_init_uniform(g.x, g.y, g.n, g.R, g.xp, seed, st);
   if (e == cudaSuccess) {
     g_signs_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.Kp);
@@ -243,13 +310,13 @@ sb_status Grouped::retile(int new_nr, std::string &err) {
   if (new_nr == nr) return SB_OK;
   nr = new_nr;
   for (auto &g : insts) {
-    cudaFree(g.v[0]);
-    cudaFree(g.v[1]);
+    cudaFreeAsync(g.v[0], st);
+    cudaFreeAsync(g.v[1], st);
     g.v[0] = g.v[1] = nullptr;
     g.Rp = (g.R + nr - 1) / nr * nr;
     const size_t vb = (size_t)g.Rp * g.Kp;
     cudaError_t e;
-    if ((e = cudaMalloc(&g.v[0], vb)) != cudaSuccess || (e = cudaMalloc(&g.v[1], vb)) != cudaSuccess) {
+    if ((e = cudaMallocAsync(&g.v[0], vb, st)) != cudaSuccess || (e = cudaMallocAsync(&g.v[1], vb, st)) != cudaSuccess) {
       err = "cudaMalloc(V)";
       return SB_ERR_OOM;
     }

@@ -50,12 +50,28 @@ struct GHost {
   GInst desc;
 };
 
+// Pinned host staging for packed couplings (one per thread that prepares instances).
+struct Staging {
+  uint8_t *pin = nullptr;
+  size_t bytes = 0;
+  ~Staging() {
+    if (pin) cudaFreeHost(pin);
+  }
+};
+
 class Grouped {
  public:
   explicit Grouped(cudaStream_t s, int replica_tile, int item_order) : st(s), nr(replica_tile), order(item_order) {}
   ~Grouped();
   // Uploads p (host), converts J to FP8, seeds the state. t0: the tick at which its step 0 runs.
   sb_status add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err);
+  // The two halves of add: prepare builds a complete instance on stream `st` (any thread; memory
+  // from the stream-ordered pool), attach makes it resident from tick t0 (the engine's thread).
+  static sb_status prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
+                           cudaStream_t st, Staging &stg, std::string &err);
+  void attach(GHost &g, int t0);
+  static void release(GHost &g, cudaStream_t s);
+  static sb_status init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err);
   void remove(int idx);
   // Changes the replica tile (reallocates the operand buffers; the state must be re-initialised).
   sb_status retile(int new_nr, std::string &err);
@@ -102,6 +118,7 @@ class Grouped {
   int cap_insts = 0, cap_items = 0;
   float *d_stage = nullptr;
   size_t stage_bytes = 0;
+  Staging stg_;
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
   int graph_tick0 = -1, graph_count = -1;

@@ -74,13 +74,29 @@ struct Server {
   std::thread worker;
   std::map<int, sbk::Grouped *> groups;
   std::vector<Req *> resident;
+  // admission runs on its own thread and stream: requests are prepared (allocated, uploaded,
+  // seeded) while the worker keeps stepping the resident ones, then attached at a tick boundary
+  static constexpr int kPreparers = 4;
+  std::thread preparer[kPreparers];
+  cudaStream_t pst[kPreparers] = {};
+  sbk::Staging stg[kPreparers];
+  std::vector<std::pair<Req *, sbk::GHost>> ready;
+  int preparing = 0;
+  void prepare_loop(int w);
+  void attach_ready();
   int tick = 0;
   sb_serving_stats stats{};
   sb_ctx *solo = nullptr;  // requests outside the grouped engine
   Clock::time_point t_start = Clock::now();
+  // exact host re-checks run on their own threads so the device loop never waits for them
+  std::vector<std::thread> checkers;
+  std::deque<std::pair<Req *, sb_status>> check_q;
+  std::condition_variable check_cv;
+  bool check_stop = false;
+  void check_loop();
 
   void run();
-  bool admit_some();
+
   void retire(int at_tick);
   void finish(Req *r, sb_status s, const std::string &err);
   void solve_alone(Req *r);
@@ -118,56 +134,89 @@ void Server::solve_alone(Req *r) {
   finish(r, s, s == SB_OK ? "" : std::string(sb_last_error(solo)));
 }
 
-// Moves requests from the queue into the grouped engines (first come, first served; a request
-// that does not fit the budget waits, and so does everything behind it).
-bool Server::admit_some() {
-  std::vector<Req *> take;
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    while (!queue.empty()) {
-      Req *r = queue.front();
-      if (r->cancel) {
-        queue.pop_front();
-        r->state = kCancelled;
-        r->status = SB_ERR_CANCELLED;
-        r->done = Clock::now();
-        ++stats.cancelled;
-        done_cv.notify_all();
-        continue;
+// Admission thread: takes requests in arrival order while the in-flight limit and the HBM budget
+// allow (a request that does not fit waits, and so does everything behind it), prepares each on
+// its own stream, and hands it to the worker.
+void Server::prepare_loop(int w) {
+  cudaSetDevice(device);
+  for (;;) {
+    Req *r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      for (;;) {
+        if (stop) return;
+        while (!queue.empty() && queue.front()->cancel) {
+          Req *c = queue.front();
+          queue.pop_front();
+          c->state = kCancelled;
+          c->status = SB_ERR_CANCELLED;
+          c->done = Clock::now();
+          ++stats.cancelled;
+          done_cv.notify_all();
+        }
+        if (!queue.empty()) {
+          Req *f = queue.front();
+          const int inflight = (int)resident.size() + (int)ready.size() + preparing;
+          const bool fits = used + f->bytes <= budget || inflight == 0;
+          if (inflight < max_inflight && fits) {
+            queue.pop_front();
+            used += f->bytes;
+            ++preparing;
+            r = f;
+            break;
+          }
+        }
+        cv.wait_for(lk, std::chrono::milliseconds(20));
       }
-      if ((int)resident.size() + (int)take.size() >= max_inflight) break;
-      if (used + r->bytes > budget && !(resident.empty() && take.empty())) break;
-      queue.pop_front();
-      used += r->bytes;
-      take.push_back(r);
     }
-  }
-  for (Req *r : take) {
     r->admitted = Clock::now();
+    const auto tp = Clock::now();
     if (r->nr == 0) {
       solve_alone(r);
       std::lock_guard<std::mutex> lk(mu);
       used -= r->bytes;
+      --preparing;
+      cv.notify_all();
       continue;
     }
-    sbk::Grouped *&g = groups[r->nr];
-    if (!g) g = new sbk::Grouped(st, r->nr, 0);
+    sbk::GHost g;
     std::string err;
-    sb_status s = g->add(r->prob, &r->prm, r->prm.seed, tick, (int)r->ticket, err);
+    const sb_status s =
+        sbk::Grouped::prepare(g, r->prob, &r->prm, r->prm.seed, (int)r->ticket, r->nr, pst[w], stg[w], err);
     if (s != SB_OK) {
       {
         std::lock_guard<std::mutex> lk(mu);
         used -= r->bytes;
+        --preparing;
       }
       finish(r, s, err);
       continue;
     }
     std::lock_guard<std::mutex> lk(mu);
+    --preparing;
+    stats.admit_ms += std::chrono::duration<double, std::milli>(Clock::now() - tp).count();
+    ready.push_back({r, g});
+    cv.notify_all();
+  }
+}
+
+// Worker: makes prepared requests resident; they take their first step at the current tick.
+void Server::attach_ready() {
+  std::vector<std::pair<Req *, sbk::GHost>> take;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    take.swap(ready);
+  }
+  for (auto &rg : take) {
+    Req *r = rg.first;
+    sbk::Grouped *&g = groups[r->nr];
+    if (!g) g = new sbk::Grouped(st, r->nr, 0);
+    g->attach(rg.second, tick);
+    std::lock_guard<std::mutex> lk(mu);
     r->state = kResident;
     resident.push_back(r);
     stats.peak_inflight = std::max<int64_t>(stats.peak_inflight, (int64_t)resident.size());
   }
-  return !take.empty();
 }
 
 // Retires every resident request whose step budget ends at `at_tick`, and drops cancelled ones.
@@ -197,20 +246,24 @@ void Server::retire(int at_tick) {
     cudaMemcpyAsync(r->energies.data(), gi.energy, (size_t)gi.R * sizeof(double), cudaMemcpyDeviceToHost, st);
   }
   cudaStreamSynchronize(st);
-  for (Req *r : fin) {
+  std::vector<std::vector<float>> xbs(fin.size());
+  for (size_t q = 0; q < fin.size(); ++q) {
+    Req *r = fin[q];
     sbk::Grouped *g = groups[r->nr];
     const sbk::GHost &gi = g->insts[g->find((int)r->ticket)];
     int b = 0;
     for (int k = 1; k < gi.R; ++k)
       if (r->energies[k] < r->energies[b]) b = k;
-    std::vector<float> xb(gi.n);
-    cudaMemcpyAsync(xb.data(), gi.x + (size_t)b * gi.xp, (size_t)gi.n * sizeof(float), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
     r->best_r = b;
     r->best = r->energies[b];
-    r->spins.resize(gi.n);
-    for (int i = 0; i < gi.n; ++i) r->spins[i] = xb[i] > 0.0f ? 1 : -1;
-    if (sb_energy_i64(r->prob, r->spins.data(), &r->e64) == SB_OK) r->ok = (double)r->e64 == r->best ? 1 : 0;
+    xbs[q].resize(gi.n);
+    cudaMemcpyAsync(xbs[q].data(), gi.x + (size_t)b * gi.xp, (size_t)gi.n * sizeof(float), cudaMemcpyDeviceToHost, st);
+  }
+  cudaStreamSynchronize(st);
+  for (size_t q = 0; q < fin.size(); ++q) {
+    Req *r = fin[q];
+    r->spins.resize(xbs[q].size());
+    for (size_t i = 0; i < xbs[q].size(); ++i) r->spins[i] = xbs[q][i] > 0.0f ? 1 : -1;
   }
   // free the finished and the cancelled
   std::vector<Req *> out = fin;
@@ -226,10 +279,13 @@ void Server::retire(int at_tick) {
       resident.erase(std::find(resident.begin(), resident.end(), r));
     }
   }
-  for (Req *r : fin) {
-    if (status & sbk::kErrWaitTimeout) finish(r, SB_ERR_TIMEOUT, "a device wait timed out");
-    else finish(r, r->status, r->status == SB_OK ? "" : "device error");
+  cv.notify_all();  // room for the next admission
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (Req *r : fin)
+      check_q.push_back({r, (status & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : r->status});
   }
+  check_cv.notify_all();
   for (Req *r : gone) finish(r, SB_ERR_CANCELLED, "cancelled");
 }
 
@@ -239,12 +295,12 @@ void Server::run() {
     {
       std::unique_lock<std::mutex> lk(mu);
       if (stop) break;
-      if (queue.empty() && resident.empty()) {
-        cv.wait_for(lk, std::chrono::milliseconds(50));
+      if (ready.empty() && resident.empty()) {
+        cv.wait_for(lk, std::chrono::milliseconds(20));
         continue;
       }
     }
-    admit_some();
+    attach_ready();
     if (resident.empty()) continue;
     const auto t0 = Clock::now();
     std::string err;
@@ -270,9 +326,27 @@ void Server::run() {
       ++tick;
     }
     for (Req *r : resident) r->ticks += nt;
+    stats.ticks += nt;
     cudaStreamSynchronize(st);
     retire(tick);
     stats.busy_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+  }
+}
+
+void Server::check_loop() {
+  for (;;) {
+    std::pair<Req *, sb_status> job;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      check_cv.wait(lk, [&] { return check_stop || !check_q.empty(); });
+      if (check_q.empty()) return;
+      job = check_q.front();
+      check_q.pop_front();
+    }
+    Req *r = job.first;
+    if (job.second == SB_OK && sb_energy_i64(r->prob, r->spins.data(), &r->e64) == SB_OK)
+      r->ok = (double)r->e64 == r->best ? 1 : 0;
+    finish(r, job.second, job.second == SB_OK ? "" : "device error");
   }
 }
 
@@ -282,17 +356,29 @@ sb_status server_create(Server **out, int device, int64_t hbm_budget, int max_in
   s->budget = hbm_budget;
   s->max_inflight = max_inflight;
   cudaSetDevice(device);
-  if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+  bool streams_ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess;
+  for (int w = 0; w < Server::kPreparers; ++w)
+    streams_ok = streams_ok && cudaStreamCreateWithFlags(&s->pst[w], cudaStreamNonBlocking) == cudaSuccess;
+  if (!streams_ok) {
     delete s;
     err = "cudaStreamCreate";
     return SB_ERR_CUDA;
   }
+  // keep freed blocks in the stream-ordered pool instead of returning them at every sync
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = (uint64_t)(hbm_budget > 0 ? hbm_budget : 0);
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   sb_device_opts o;
   memset(&o, 0, sizeof(o));
   o.device = device;
-  o.stream = s->st;
+  o.stream = s->pst[0];  // solo solves run on an admission thread
   if (sb_create(&s->solo, &o) != SB_OK) s->solo = nullptr;
   s->worker = std::thread([s] { s->run(); });
+  for (int w = 0; w < Server::kPreparers; ++w) s->preparer[w] = std::thread([s, w] { s->prepare_loop(w); });
+  const unsigned nc = std::max(2u, std::min(8u, std::thread::hardware_concurrency() / 2));
+  for (unsigned k = 0; k < nc; ++k) s->checkers.emplace_back([s] { s->check_loop(); });
   *out = s;
   return SB_OK;
 }
@@ -305,11 +391,22 @@ void server_destroy(Server *s) {
   }
   s->cv.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  for (auto &t : s->preparer)
+    if (t.joinable()) t.join();
+  for (auto &rg : s->ready) sbk::Grouped::release(rg.second, s->pst[0]);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->check_stop = true;
+  }
+  s->check_cv.notify_all();
+  for (auto &t : s->checkers) t.join();
   cudaSetDevice(s->device);
   for (auto &kv : s->groups) delete kv.second;
   for (auto &kv : s->reqs) delete kv.second;
   if (s->solo) sb_destroy(s->solo);
+  for (auto ps : s->pst) cudaStreamSynchronize(ps);
   cudaStreamDestroy(s->st);
+  for (auto ps : s->pst) cudaStreamDestroy(ps);
   delete s;
 }
 

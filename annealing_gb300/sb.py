@@ -117,6 +117,8 @@ class ServingStats(C.Structure):
         ("grouped_launches", C.c_int64),
         ("busy_ms", C.c_double),
         ("peak_inflight", C.c_int64),
+        ("ticks", C.c_int64),
+        ("admit_ms", C.c_double),
     ]
 
 

@@ -136,7 +136,9 @@ typedef struct sb_params {
 /* Results. The caller owns every array; any of them may be NULL. */
 typedef struct sb_result {
   int8_t *best_spins;          /* [n]  +1 / -1 of the lowest-energy replica (final state) */
-  double *replica_energies;    /* [replicas] final-state energy of each replica */
+  double *replica_energies;    /* [replicas] final-state energy of each replica: exact for integer
+                                  couplings; for real couplings from the FP32 field, except the 8
+                                  lowest, which are recomputed in FP64 (best_energy is FP64) */
   double *energy_trace;        /* [steps + 1] min-over-replicas energy of s(t), t = 0..steps (trace) */
   double *energy_trace_all;    /* [(steps + 1) * replicas] (trace_all) */
   float *final_x;              /* [replicas * n] final positions, replica-major */
@@ -253,6 +255,8 @@ typedef struct sb_serving_stats {
   int64_t grouped_launches;     /* device steps run by the serving loop */
   double busy_ms;               /* time the worker had work resident */
   int64_t peak_inflight;
+  int64_t ticks;                /* SB steps the resident set advanced */
+  double admit_ms;              /* summed time spent preparing requests (several threads) */
 } sb_serving_stats;
 sb_status sb_serving_stats_get(sb_ctx *ctx, sb_serving_stats *out);
 
