@@ -118,6 +118,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def reduce_max(value: float, world: int) -> float:
+    """Max of a per-rank number over all ranks (NCCL on CUDA tensors, gloo on CPU tensors)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def weak_scaling_value(units_per_rank: float, world: int, steps: int, max_total_ms: float) -> float:
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return world * units_per_rank * steps / (max_total_ms * 1e-3)
+
+
 def make_problem(name):
     from annealing_gb300 import instances
 
@@ -156,7 +174,7 @@ def run_reference(args, rank, world):
         return
     J, h = make_problem(args.workload)
     variant, n, R, steps, field, desc = WORKLOADS[args.workload]
-    budget = max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
+    budget = args.cpu_budget or max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_sample(args.workload, J, h, budget_s=budget / 4)
     vals, samples = [], []
@@ -225,12 +243,8 @@ def run_ours(args, rank, world, local_rank):
             results.append(r)
         barrier()
         wall = time.perf_counter() - wall0
-    total_ms = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * R * sb_steps * args.steps / (total_ms * 1e-3)
+    total_ms = reduce_max(float(sum(times)), world)
+    value = weak_scaling_value(float(n) * R * sb_steps, world, args.steps, total_ms)
 
     # ---- roofline of the dominant kernel: one profiled solve (event pair around each launch) ----
     prm_p = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=fmode, seed=77, profile=1)
@@ -274,12 +288,8 @@ def run_ours(args, rank, world, local_rank):
         t0 = time.perf_counter()
         r = ctx.solve(pw, prm)  # H2D of J, solve, D2H of spins / energies; returns when done
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_total = float(sum(e2e_ms))
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * n * R * sb_steps * args.steps / (e2e_total * 1e-3)
+    e2e_total = reduce_max(float(sum(e2e_ms)), world)
+    e2e_value = weak_scaling_value(float(n) * R * sb_steps, world, args.steps, e2e_total)
     h2d = J.nbytes + (h.nbytes if h is not None else 0)
     d2h = n + 8 * R + 4  # best spins (int8), replica energies (f64), status word
 
@@ -368,13 +378,9 @@ def run_batch(args, rank, world, local_rank):
             launches += res[0].kernel_launches
             quality.append(all(r.energy_check_ok for r in res))
         barrier()
-    total_ms = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(float(sum(times)), world)
     updates = float(n_sum) * R * sb_steps
-    value = world * updates * args.steps / (total_ms * 1e-3)
+    value = weak_scaling_value(updates, world, args.steps, total_ms)
     # roofline: one profiled run, event pair around every grouped step launch
     prm_p = sb.Params.default(sb.DSB, steps=24, replicas=R, seed=7, field_mode=sb.FIELD_TC, profile=1)
     bp = ctx.batch(probs, prm_p)
@@ -396,7 +402,7 @@ def run_batch(args, rank, world, local_rank):
         t1 = time.perf_counter()
         ctx.batch(probs, prm).run(seed=200 + k)
         e2e_ms.append(1e3 * (time.perf_counter() - t1))
-    e2e_total = float(sum(e2e_ms))
+    e2e_total = reduce_max(float(sum(e2e_ms)), world)
     if rank != 0:
         return
     line = {
@@ -503,6 +509,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched-dsb")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--requests", type=int, default=2000, help="serving workload: stream length")
+    ap.add_argument("--cpu-budget", type=float, default=0.0,
+                    help="seconds of CPU work per reference-arm step (default: fit the run in ~1 min)")
     ap.add_argument("--pool", type=int, default=64, help="serving workload: distinct instances")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -511,7 +519,7 @@ def main():
     if world > 1 and args.impl == "ours":
         import torch
 
-        torch.distributed.init_process_group("nccl")
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.workload == "uneven-batch":
