@@ -151,6 +151,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int c = c_lo; c < c_lo + kHalf; c += 16) {
         uint32_t va[16];
         ptx::tmem_ld16(t_acc + lane_off + c, va);
+        // all of the chunk's state loads first: they are independent and may all be in flight
+        // (interleaving them with the stores below would serialise them on possible aliasing)
+        float xv[16], yv[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = w.r0 + c + j;
+          const bool ins = row < n && r < R;
+          const size_t k = (size_t)r * xp + row;
+          xv[j] = ins ? xs[k] : 0.0f;
+          if constexpr (!kEOnly) yv[j] = ins ? ys[k] : 0.0f;
+        }
         ptx::tmem_ld_wait();
         float e2[16];
 #pragma unroll
@@ -158,18 +169,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const int r = w.r0 + c + j;
           const bool ins = row < n && r < R;
           const float f = __uint_as_float(va[j]);
-          const size_t k = (size_t)r * xp + row;
-          float x = ins ? xs[k] : 0.0f;
+          float x = xv[j];
           if constexpr (kEOnly) {
             const float sg = sgnf(x);
             e2[j] = ins ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
           } else {
-            if (ins) {
-              float y = ys[k];
-              sb_update(f, hv, pump, c0, dt, dta0, x, y);
-              xs[k] = x;
-              ys[k] = y;
-              vn[(size_t)r * Kp + row] = x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+            float y = yv[j];
+            sb_update(f, hv, pump, c0, dt, dta0, x, y);
+            xv[j] = x;
+            yv[j] = y;
+          }
+        }
+        if constexpr (!kEOnly) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int r = w.r0 + c + j;
+            if (row < n && r < R) {
+              const size_t k = (size_t)r * xp + row;
+              xs[k] = xv[j];
+              ys[k] = yv[j];
+              vn[(size_t)r * Kp + row] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
             }
           }
         }

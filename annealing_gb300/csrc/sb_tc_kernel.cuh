@@ -366,6 +366,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       }
       ptx::tmem_st_wait();
     }
+    float pump_next = (!kEOnly && nsteps > 0) ? p.pumps[p.t0] : 0.0f;
     for (int ls = 0; ls < nsteps; ++ls) {
       const int t = p.t0 + ls;
       const int buf = (p.buf0 + ls) & 1;
@@ -374,7 +375,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1);
       if (!epi_all(got)) { ok = false; break; }
       ptx::tc_fence_after();
-      const float pump = kEOnly ? 0.0f : p.pumps[t];
+      // the schedule value was fetched one step ahead (a global load on the critical path otherwise)
+      const float pump = pump_next;
+      if (!kEOnly && ls + 1 < nsteps) pump_next = p.pumps[t + 1];
       uint8_t *const vnext[2] = {p.v[buf ^ 1][0], p.v[buf ^ 1][1]};
       uint8_t *const vtile = smem + STAGES * kStage;  // [NR][kVRow] staging tile
       constexpr int kChunks = kHalf / 16;
