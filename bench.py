@@ -53,6 +53,17 @@ WORKLOADS = {
 }
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
+# each dominant kernel; the summaries, with the commands, are the files named here.
+NCU_TRAFFIC = {
+    # plain dSB, N=2000, R=1: bytes per launch (ncu runs the launch with cold caches)
+    "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
+    # uneven batch: measured bytes per algorithmic byte on a 48-instance batch (441.2 MB of
+    # 451.8 MB); the launch of the full batch is scaled by its algorithmic bytes
+    "uneven-batch": (441.2 / 451.8, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
+}
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -270,7 +281,8 @@ def run_ours(args, rank, world, local_rank):
         bytes_per_launch = 4.0 * n * n + 16.0 * n * R
         achieved = bytes_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "kernel": "plain_step_kernel",
+                "frac": achieved / hbm, "traffic": NCU_TRAFFIC["plain-dsb"][0] if n == 2000 and R == 1 else None,
+                "traffic_source": NCU_TRAFFIC["plain-dsb"][1], "kernel": "plain_step_kernel",
                 "launch_ms": rp.kernel_ms_avg, "peak_source": f"{src} HBM copy",
                 "note": "J (16 MB) is L2-resident between steps; the fraction is of HBM bandwidth"}
 
@@ -346,7 +358,9 @@ def run_batch(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     variant, _, R, sb_steps, field, desc = WORKLOADS[args.workload]
-    probs = batch_instances()
+    probs = batch_instances(count=args.instances)
+    if args.instances != 512:
+        desc = desc.replace("512 instances", f"{args.instances} instances")
     n_sum = sum(p.n for p in probs)
     stream = torch.cuda.current_stream(dev)
     ctx = sb.Context(local_rank, stream=stream.cuda_stream)
@@ -392,7 +406,9 @@ def run_batch(args, rank, world, local_rank):
     bytes_per_launch = np_kp + sum(p.n for p in probs) * R * 17.0  # FP8 J + (x, y in/out, next operand)
     achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": "grouped_kernel (one launch per SB step)",
+            "traffic": NCU_TRAFFIC["uneven-batch"][0] * bytes_per_launch,
+            "traffic_source": NCU_TRAFFIC["uneven-batch"][1] + " (48-instance capture, scaled by algorithmic bytes)",
+            "kernel": "grouped_kernel (one launch per SB step)",
             "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
             "peak_source": f"{src} HBM copy"}
     # e2e: sb_solve_batch from host buffers every step (upload, convert, run, results back)
@@ -412,7 +428,8 @@ def run_batch(args, rank, world, local_rank):
         "dtype": "fp8e4m3 field (f32 accumulate), f32 state", "data": "synthetic (seeded)",
         "config": {"workload": desc, "instances": len(probs), "sum_n": n_sum, "replicas": R,
                    "sb_steps": sb_steps, "parallelism": f"replicas-only x{world}",
-                   "l2": "inputs (2.9 GB of J) larger than L2; 256 MB flush between runs"},
+                   "l2": f"inputs ({np_kp / 1e9:.2f} GB of FP8 J) "
+                   + ("larger than L2" if np_kp > 129e6 else "smaller than L2") + "; 256 MB flush between runs"},
         "e2e": {"value": world * updates * args.steps / (e2e_total * 1e-3), "unit": "spin-updates/s",
                 "h2d_bytes_per_step": int(sum(p.n * p.n * 4 for p in probs)),
                 "d2h_bytes_per_step": int(sum(p.n + 8 * R for p in probs)),
@@ -512,7 +529,15 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=0.0,
                     help="seconds of CPU work per reference-arm step (default: fit the run in ~1 min)")
     ap.add_argument("--pool", type=int, default=64, help="serving workload: distinct instances")
+    ap.add_argument("--sb-steps", type=int, default=0,
+                    help="smaller case for profiling: SB steps per solve (default: the workload's)")
+    ap.add_argument("--instances", type=int, default=512,
+                    help="uneven-batch workload: instance count (smaller cases for profiling)")
     args = ap.parse_args()
+    if args.sb_steps > 0 and args.workload != "serving":
+        v, n, R, _, field, desc = WORKLOADS[args.workload]
+        WORKLOADS[args.workload] = (v, n, R, args.sb_steps, field,
+                                    desc.replace(f"{_} steps", f"{args.sb_steps} steps"))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
