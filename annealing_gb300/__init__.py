@@ -5,8 +5,9 @@ kernels for sm_103a + C++ host code). This package holds the ctypes binding (sb.
 build (_build.py) and the synthetic instance generators (instances.py).
 """
 from .sb import (ASB, BSB, DSB, Batch, FIELD_AUTO, FIELD_FP32, FIELD_TC, INIT_REFERENCE, INIT_UNIFORM,
-                 Context, Params, Plan, Problem, Result, SBError, lib, pump)
+                 OPERAND_AUTO, OPERAND_BF16, OPERAND_BF16X2, OPERAND_FP4, OPERAND_FP8, Context, Params, Plan,
+                 Problem, Result, SBError, lib, pump)
 
 __all__ = ["ASB", "BSB", "DSB", "Batch", "FIELD_AUTO", "FIELD_FP32", "FIELD_TC", "INIT_REFERENCE",
-           "INIT_UNIFORM", "Context", "Params", "Plan", "Problem", "Result", "SBError", "lib",
+           "INIT_UNIFORM", "OPERAND_AUTO", "OPERAND_BF16", "OPERAND_BF16X2", "OPERAND_FP4", "OPERAND_FP8", "Context", "Params", "Plan", "Problem", "Result", "SBError", "lib",
            "pump"]

@@ -112,14 +112,38 @@ sb_status resolve_mode(const sb_problem *p, const sb_params *prm, int &mode, int
     err = "aSB runs on the plain FP32 path only";
     return SB_ERR_UNSUPPORTED;
   }
+  const int want = prm->operand_dtype;
+  if (want < SB_OPERAND_AUTO || want > SB_OPERAND_FP4) {
+    err = "unknown operand_dtype";
+    return SB_ERR_INVALID_ARG;
+  }
   if (prm->variant == SB_DSB) {
-    if (p->integer_valued && p->max_abs_j <= 16)
-      dtype = sbk::kTcFp8;
-    else if (p->integer_valued && p->max_abs_j <= 256)
-      dtype = sbk::kTcBf16;
-    else
-      dtype = sbk::kTcBf16Split;
+    const bool fp4 = p->integer_valued && p->max_abs_j <= 4 && sbk::tc_fp4_fits(p->n, prm->replicas);
+    if (want == SB_OPERAND_AUTO) {
+      if (fp4)
+        dtype = sbk::kTcFp4;
+      else if (p->integer_valued && p->max_abs_j <= 16)
+        dtype = sbk::kTcFp8;
+      else if (p->integer_valued && p->max_abs_j <= 256)
+        dtype = sbk::kTcBf16;
+      else
+        dtype = sbk::kTcBf16Split;
+    } else {
+      const bool exact = want == SB_OPERAND_FP4    ? fp4
+                         : want == SB_OPERAND_FP8  ? (p->integer_valued && p->max_abs_j <= 16)
+                         : want == SB_OPERAND_BF16 ? (p->integer_valued && p->max_abs_j <= 256)
+                                                   : true;
+      if (!exact) {
+        err = "the requested operand_dtype is not exact for these couplings (or, for FP4, this size)";
+        return SB_ERR_UNSUPPORTED;
+      }
+      dtype = want;  // sb_operand_dtype and TcDtype share their codes
+    }
   } else {
+    if (want != SB_OPERAND_AUTO && want != SB_OPERAND_BF16X2) {
+      err = "bSB on tensor cores runs the BF16 hi+lo operands only";
+      return SB_ERR_UNSUPPORTED;
+    }
     dtype = sbk::kTcBf16Split;
     if (prm->trace || prm->trace_all) {
       err = "per-step energy traces of bSB are produced by the plain FP32 path only";

@@ -34,6 +34,9 @@ void tc_destroy(TcEngine *e);
 // Re-converts new couplings (same n) into an existing engine's J operand.
 cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st);
 int64_t tc_footprint(const TcSetup &s);
+// True when the packed-E2M1 kernel runs this shape (dSB, its units fit the SMs and a unit's J rows
+// fit shared memory).
+bool tc_fp4_fits(int n, int R);
 // Builds the step-0 operand (sign(x) or x hi/lo) from the initial state.
 cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st);
 // The whole step loop in one persistent cooperative launch: x / y live in TMEM between steps,

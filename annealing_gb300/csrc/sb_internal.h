@@ -57,7 +57,7 @@ cudaError_t launch_pad_rows_f32(const float *src, float *dst, int n, int jp, cud
 
 // ---------------------------------------------------------------------------------------------
 // Tensor-core (tcgen05) path. See sb_tc.cu.
-enum TcDtype : int { kTcFp8 = 1, kTcBf16 = 2, kTcBf16Split = 3 };
+enum TcDtype : int { kTcFp8 = 1, kTcBf16 = 2, kTcBf16Split = 3, kTcFp4 = 4 };
 
 struct TcPlanInfo;  // opaque, defined in sb_tc.cu
 }  // namespace sbk

@@ -37,6 +37,7 @@
 #include <string>
 
 #include "sb_host.h"
+#include "sb_tc_fp4.cuh"
 #include "sb_tc_kernel.cuh"
 
 namespace sbk {
@@ -46,6 +47,7 @@ namespace sbk {
 bool tc_kernel_fp8(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_bf16(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem);
+bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem);
 
 namespace {
 using namespace tck;
@@ -90,6 +92,29 @@ __global__ void prepare_v_kernel(const float *x, int n, int R, int xp, uint8_t *
   }
 }
 
+// Packed E2M1 operands: byte b of a row holds spins 2b (low nibble) and 2b + 1 (high nibble).
+__global__ void convert_j_fp4_kernel(const float *J, int n, int jp, uint8_t *a, int Np, int Kb) {
+  const size_t total = (size_t)Np * Kb;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = k / Kb, j = 2 * (k % Kb);
+    const float v0 = (i < (size_t)n && j < (size_t)n) ? J[i * jp + j] : 0.0f;
+    const float v1 = (i < (size_t)n && j + 1 < (size_t)n) ? J[i * jp + j + 1] : 0.0f;
+    a[k] = (uint8_t)((e2m1_code(v0) & 0xFu) | ((e2m1_code(v1) & 0xFu) << 4));
+  }
+}
+
+__global__ void prepare_v_fp4_kernel(const float *x, int n, int R, int xp, uint8_t *v, int Kb) {
+  const size_t total = (size_t)R * Kb;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / Kb, i = 2 * (k % Kb);
+    const uint32_t c0 = i < (size_t)n ? (x[r * xp + i] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+    const uint32_t c1 = i + 1 < (size_t)n ? (x[r * xp + i + 1] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+    v[k] = (uint8_t)(c0 | (c1 << 4));
+  }
+}
+
 int grid_1d(size_t total) {
   size_t g = (total + 255) / 256;
   if (g > 152 * 32) g = 152 * 32;
@@ -113,13 +138,13 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 bool encode_2d(CUtensorMap *m, void *base, int elem, uint64_t inner, uint64_t outer, uint32_t box_rows,
-               bool store_tile = false) {
+               bool store_tile = false, uint32_t store_inner = kBM) {
   auto enc = get_encode();
   if (!enc) return false;
   const cuuint64_t dims[2] = {inner, outer};
   const cuuint64_t strides[1] = {inner * (uint64_t)elem};
   // loads: one 128-byte swizzled K chunk; stores: the unit's whole 128-spin row, unswizzled
-  const cuuint32_t box[2] = {(cuuint32_t)(store_tile ? kBM : kChunkBytes / elem), box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)(store_tile ? store_inner : kChunkBytes / elem), box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(m, elem == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                          base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -145,12 +170,16 @@ struct TcEngine {
 
 namespace {
 
-bool pick(TcEngine *e, int dt, int variant, int nr) {
+// Kp: K extent in spins (a multiple of 256 for packed E2M1 operands, of 128 otherwise).
+int kp_for(int dt, int n) { return dt == kTcFp4 ? (n + 255) / 256 * 256 : (n + 127) / 128 * 128; }
+
+bool pick(TcEngine *e, int dt, int variant, int nr, int n) {
   size_t smem = 0;
   for (int m = 0; m < 3; ++m) {
     const void *k = nullptr;
     bool ok;
-    if (dt == kTcFp8) ok = tc_kernel_fp8(variant, nr, m, &k, &smem);
+    if (dt == kTcFp4) ok = tc_kernel_fp4(variant, nr, m, kp_for(dt, n) / 256, &k, &smem);
+    else if (dt == kTcFp8) ok = tc_kernel_fp8(variant, nr, m, &k, &smem);
     else if (dt == kTcBf16) ok = tc_kernel_bf16(variant, nr, m, &k, &smem);
     else ok = tc_kernel_split(variant, nr, m, &k, &smem);
     e->kernel[m] = ok ? k : nullptr;
@@ -179,7 +208,19 @@ int choose_nr(int n, int R, int sms) {
 
 size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * sizeof(uint32_t) + 255) / 256 * 256; }
 
+bool tc_fp4_fits(int n, int R) {
+  const int nr = choose_nr(n, R, sm_count());
+  const void *k = nullptr;
+  size_t smem = 0;
+  return nr > 0 && tc_kernel_fp4(2, nr, kEmodeStep, kp_for(kTcFp4, n) / 256, &k, &smem);
+}
+
 int64_t tc_footprint(const TcSetup &s) {
+  if (s.dtype == kTcFp4) {
+    const int64_t Np = (s.n + kBM - 1) / kBM * kBM, Kb = kp_for(kTcFp4, s.n) / 2;
+    const int64_t Rp = (s.R + 127) / 128 * 128;
+    return Np * Kb + 2 * Rp * Kb + 4096;
+  }
   const int elem = s.dtype == kTcFp8 ? 1 : 2;
   const int64_t Np = (s.n + kBM - 1) / kBM * kBM, Kp = (s.n + 127) / 128 * 128;
   const int64_t Rp = (s.R + 127) / 128 * 128;
@@ -208,14 +249,16 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
   TcEngine *e = new TcEngine();
   e->s = s;
   e->nr = nr;
-  if (!pick(e, s.dtype, s.variant, nr)) {
+  if (!pick(e, s.dtype, s.variant, nr, s.n)) {
     delete e;
-    err = "no kernel for this dtype / variant";
+    err = "no kernel for this dtype / variant / size";
     return SB_ERR_UNSUPPORTED;
   }
-  const int elem = s.dtype == kTcFp8 ? 1 : 2;
+  const bool fp4 = s.dtype == kTcFp4;
+  const int elem = (s.dtype == kTcFp8 || fp4) ? 1 : 2;
   e->Np = (s.n + kBM - 1) / kBM * kBM;
-  e->Kp = (s.n + 127) / 128 * 128;
+  e->Kp = kp_for(s.dtype, s.n);
+  const uint64_t row_elems = fp4 ? (uint64_t)e->Kp / 2 : (uint64_t)e->Kp;  // operand row: bytes (E2M1 pairs) or elements
   e->Rp = (s.R + nr - 1) / nr * nr;
   e->n_mtiles = e->Np / kBM;
   e->n_rtiles = e->Rp / nr;
@@ -228,7 +271,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     return ce == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
   };
   cudaError_t ce;
-  const size_t abytes = (size_t)e->Np * e->Kp * elem, vbytes = (size_t)e->Rp * e->Kp * elem;
+  const size_t abytes = (size_t)e->Np * row_elems * elem, vbytes = (size_t)e->Rp * row_elems * elem;
   for (int a = 0; a < ap; ++a)
     if ((ce = cudaMalloc(&e->a[a], abytes)) != cudaSuccess) return fail("cudaMalloc(J operand)", ce);
   for (int b = 0; b < 2; ++b)
@@ -237,20 +280,20 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
       if ((ce = cudaMemsetAsync(e->v[b][pp], 0, vbytes, st)) != cudaSuccess) return fail("memset", ce);
     }
   if ((ce = cudaMalloc(&e->flags, flag_bytes(e))) != cudaSuccess) return fail("cudaMalloc(flags)", ce);
-  convert_j_kernel<<<grid_1d((size_t)e->Np * e->Kp), 256, 0, st>>>(dJ, s.n, jp, e->a[0], e->a[1], e->Np, e->Kp, s.dtype);
-  if ((ce = cudaGetLastError()) != cudaSuccess) return fail("convert_j_kernel", ce);
+  if ((ce = tc_reload(e, dJ, jp, st)) != cudaSuccess) return fail("convert_j_kernel", ce);
   TcArgs &g = e->args;
   memset(&g, 0, sizeof(g));
   for (int a = 0; a < ap; ++a)
-    if (!encode_2d(&g.tmA[a], e->a[a], elem, (uint64_t)e->Kp, (uint64_t)e->Np, kBM)) return fail("cuTensorMapEncodeTiled(J)", cudaSuccess);
+    if (!encode_2d(&g.tmA[a], e->a[a], elem, row_elems, (uint64_t)e->Np, kBM)) return fail("cuTensorMapEncodeTiled(J)", cudaSuccess);
   for (int b = 0; b < 2; ++b)
     for (int pp = 0; pp < bp; ++pp) {
-      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, (uint64_t)e->Kp, (uint64_t)e->Rp, (uint32_t)nr))
+      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, row_elems, (uint64_t)e->Rp, (uint32_t)nr))
         return fail("cuTensorMapEncodeTiled(V)", cudaSuccess);
       g.v[b][pp] = e->v[b][pp];
     }
+  // the unit's V tile: 128 spins = 128 elements, or 64 bytes of E2M1 pairs
   for (int b = 0; b < 2; ++b)
-    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, (uint64_t)e->Kp, (uint64_t)e->Rp, (uint32_t)nr, true))
+    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, row_elems, (uint64_t)e->Rp, (uint32_t)nr, true, fp4 ? kBM / 2 : kBM))
       return fail("cuTensorMapEncodeTiled(V store)", cudaSuccess);
   g.flags = e->flags;
   g.n = s.n;
@@ -260,7 +303,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
   g.Rp = e->Rp;
   g.n_mtiles = e->n_mtiles;
   g.n_rtiles = e->n_rtiles;
-  g.k_chunks = e->Kp * elem / kChunkBytes;
+  g.k_chunks = (int)(row_elems * elem / kChunkBytes);
   for (int m = 0; m < 3; ++m)
     if (e->kernel[m] &&
         (ce = cudaFuncSetAttribute(e->kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem)) != cudaSuccess)
@@ -280,6 +323,11 @@ void tc_destroy(TcEngine *e) {
 }
 
 cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st) {
+  if (e->s.dtype == kTcFp4) {
+    const int Kb = e->Kp / 2;
+    convert_j_fp4_kernel<<<grid_1d((size_t)e->Np * Kb), 256, 0, st>>>(dJ, e->s.n, jp, e->a[0], e->Np, Kb);
+    return cudaGetLastError();
+  }
   convert_j_kernel<<<grid_1d((size_t)e->Np * e->Kp), 256, 0, st>>>(dJ, e->s.n, jp, e->a[0], e->a[1], e->Np, e->Kp,
                                                                    e->s.dtype);
   return cudaGetLastError();
@@ -290,6 +338,11 @@ int tc_units(const TcEngine *e) { return e ? e->units : 0; }
 int tc_replica_tile(const TcEngine *e) { return e ? e->nr : 0; }
 
 cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st) {
+  if (e->s.dtype == kTcFp4) {
+    const int Kb = e->Kp / 2;
+    prepare_v_fp4_kernel<<<grid_1d((size_t)e->s.R * Kb), 256, 0, st>>>(x, e->s.n, e->s.R, e->s.xp, e->v[0][0], Kb);
+    return cudaGetLastError();
+  }
   prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(x, e->s.n, e->s.R, e->s.xp, e->v[0][0], e->v[0][1], e->Kp,
                                                                       e->s.dtype, e->s.variant);
   return cudaGetLastError();
@@ -346,7 +399,7 @@ cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
   TcEngine e;  // on the stack: every buffer below belongs to the caller
   e.s = TcSetup{2, kTcFp8, ext.n, ext.R, ext.xp};
   e.nr = choose_nr(ext.n, ext.R, sm_count());
-  if (e.nr == 0 || !pick(&e, kTcFp8, 2, e.nr)) return cudaErrorInvalidValue;
+  if (e.nr == 0 || !pick(&e, kTcFp8, 2, e.nr, ext.n)) return cudaErrorInvalidValue;
   e.Np = (ext.n + kBM - 1) / kBM * kBM;
   e.Kp = (ext.n + 127) / 128 * 128;
   e.Rp = (ext.R + e.nr - 1) / e.nr * e.nr;

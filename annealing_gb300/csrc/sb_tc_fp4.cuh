@@ -1,0 +1,332 @@
+// Tensor-core dSB step kernel with packed E2M1 operands and the couplings resident in shared memory.
+//
+// Same contraction as tc_sb_kernel (F[i][r] = sum_k J[i][k] sign(x[r][k]), the reference's per-step
+// field call SB/CUDA_GPU/m2_opt.cu:169 for all replicas at once) and the same persistent,
+// flag-ordered structure, with two changes that cut the operand traffic of a step by 4x:
+//   * operands are E2M1 (4-bit floats, two per byte): sign(x) is +-1 and every integer coupling
+//     with |J| <= 4 is exact, so the products and their FP32 sums are the integers the FP8 and
+//     INT8 forms give (bit-identical fields); the MMA is tcgen05 kind::mxf4 with every block scale
+//     1.0 (UE8M0 0x7F written once into TMEM);
+//   * a unit's J rows (128 spins x Kp/2 bytes, at most ~160 KB) are loaded into shared memory once
+//     per launch, so each SB step streams only the unit's V tile (NR replicas x Kp/2 bytes) from L2.
+// TMEM columns: accumulator [0, NR), x [NR, 2NR), y [2NR, 3NR), A scales [3NR, 3NR + 16),
+// B scales [3NR + 16, 3NR + 32). The nibble order inside a byte (spin 2j in the low half) is the
+// same for J and V, so the dot products do not depend on how the tensor core orders the pair.
+#pragma once
+#include "sb_tc_kernel.cuh"
+
+namespace sbk {
+namespace tck {
+
+// E2M1 code of a small integer (sign in bit 3; 1 -> 0x2, 2 -> 0x4, 3 -> 0x5, 4 -> 0x6), or 0xFF
+// when the value is not one of 0, +-1, +-2, +-3, +-4.
+__host__ __device__ inline uint8_t e2m1_code(float v) {
+  const float a = v < 0.0f ? -v : v;
+  uint8_t m;
+  if (a == 0.0f) return 0;
+  else if (a == 1.0f) m = 0x2;
+  else if (a == 2.0f) m = 0x4;
+  else if (a == 3.0f) m = 0x5;
+  else if (a == 4.0f) m = 0x6;
+  else return 0xFF;
+  return v < 0.0f ? (uint8_t)(m | 0x8) : m;
+}
+constexpr uint8_t kE2m1Plus = 0x2, kE2m1Minus = 0xA;
+
+// Block-scaled instruction descriptor: A and B E2M1 (code 1 for kind::mxf4) at bits 7-9 / 10-12,
+// both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, UE8M0 scales (bit 23), M >> 4 at bits
+// 24-28; scale-factor ids 0 (bits 4-5, 29-30); dense K = 64 (bit 31 = 0).
+__host__ __device__ constexpr uint32_t make_idesc_mxf4(int m, int n) {
+  return (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | (1u << 23) | ((uint32_t)(m >> 4) << 24);
+}
+
+constexpr int kFp4Stages = 4;  // V chunks in flight
+
+template <int NR>
+__host__ __device__ constexpr int fp4_btile() { return NR * kChunkBytes; }
+constexpr int kFp4ATile = kBM * kChunkBytes;  // one J chunk: 128 spins x 256 spins of K
+// Shared memory of one CTA for k_chunks 128-byte chunks of K (256 spins each).
+template <int NR>
+constexpr size_t fp4_smem(int k_chunks) {
+  return 1024 + (size_t)kFp4Stages * fp4_btile<NR>() + (size_t)k_chunks * kFp4ATile + (size_t)NR * (kBM / 2);
+}
+
+// flags / buffers as in tc_sb_kernel; p.k_chunks = Kp / 256 (Kp a multiple of 256, J and V rows of
+// Kp / 2 bytes); p.tmA / p.tmB load 128-byte x rows boxes, p.tmS stores the unit's 64-byte x NR tile.
+template <int NR, int EMODE>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_constant__ TcArgs p) {
+  constexpr int STAGES = kFp4Stages;
+  constexpr int kBTile = fp4_btile<NR>();
+  constexpr int kVRow = kBM / 2;  // bytes of one replica row of the unit's V tile
+  constexpr uint32_t kSf = 3 * NR;
+  constexpr uint32_t kCols = kSf + 32 <= 128 ? 128 : (kSf + 32 <= 256 ? 256 : 512);
+  constexpr uint32_t kIdesc = make_idesc_mxf4(kBM, NR);
+  constexpr int kHalf = NR / 2;
+  static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t *ring = smem;                                   // [STAGES][NR][128] V chunks
+  uint8_t *jres = smem + STAGES * kBTile;                  // [k_chunks][128][128] resident J
+  uint8_t *vtile = jres + (size_t)p.k_chunks * kFp4ATile;  // [NR][64] next V tile of this unit
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], a_bar, accf_bar, acce_bar;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ float ered[4][NR];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x % p.n_mtiles, rt = blockIdx.x / p.n_mtiles;
+  const int m0 = mt * kBM, r0 = rt * NR;
+  constexpr bool kEOnly = EMODE == kEmodeEnergy;
+  constexpr bool want_e = EMODE != kEmodeStep;
+  const int nsteps = kEOnly ? 1 : p.steps;
+  uint32_t *col_flags = p.flags + (size_t)rt * p.n_mtiles;
+  bool ok = true;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      ptx::mbar_init(&full_bar[s], 1);
+      ptx::mbar_init(&empty_bar[s], 1);
+    }
+    ptx::mbar_init(&a_bar, 1);
+    ptx::mbar_init(&accf_bar, 1);
+    ptx::mbar_init(&acce_bar, kEpiWarps);
+    ptx::fence_mbar_init();
+    ptx::prefetch_tmap(&p.tmA[0]);
+    ptx::prefetch_tmap(&p.tmB[0][0]);
+    ptx::prefetch_tmap(&p.tmB[1][0]);
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(&tmem_base_sh, kCols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+  const uint32_t t_acc = tmem, t_x = tmem + NR, t_y = tmem + 2 * NR;
+  if (warp >= 2) {
+    // every block scale = 2^0: UE8M0 0x7F in all bytes of the scale columns, all 128 lanes
+    uint32_t ones[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) ones[j] = 0x7F7F7F7Fu;
+    const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
+    ptx::tmem_st16(tmem + kSf + 16 * ((warp - 2) >> 2) + lane_off, ones);
+    ptx::tmem_st_wait();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      ptx::mbar_arrive_expect_tx(&a_bar, (uint32_t)(p.k_chunks * kFp4ATile));
+      for (int kc = 0; kc < p.k_chunks; ++kc)
+        ptx::tma_load_2d(jres + (size_t)kc * kFp4ATile, &p.tmA[0], kc * kChunkBytes, m0, &a_bar);
+    }
+    uint32_t g = 0;
+    for (int ls = 0; ls < nsteps && ok; ++ls) {
+      const int buf = (p.buf0 + ls) & 1;
+      int ready = ls == 0 ? p.n_mtiles : 0;  // units of this column known to have published V(ls)
+      for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++g) {
+        // chunk kc holds the spins of units 2 kc and 2 kc + 1
+        const int need = 2 * kc + 2 < p.n_mtiles ? 2 * kc + 2 : p.n_mtiles;
+        if (need > ready) {
+          const int u = ready + lane;
+          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls) : true;
+          if (!__all_sync(0xffffffffu, fl)) ok = false;
+          ready = ready + 32 < p.n_mtiles ? ready + 32 : p.n_mtiles;
+          ptx::fence_proxy_async_global();
+        }
+        if (lane == 0 && ok) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            ok = false;
+          } else {
+            ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)kBTile);
+            ptx::tma_load_2d(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes, r0, &full_bar[s]);
+          }
+        }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      ok = ptx::mbar_wait(&a_bar, 0);
+      uint32_t g = 0;
+      for (int ls = 0; ls < nsteps && ok; ++ls) {
+        if (ls >= 1 && !ptx::mbar_wait(&acce_bar, (uint32_t)(ls - 1) & 1)) { ok = false; break; }
+        ptx::tc_fence_after();
+        for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+          const int s = g % STAGES;
+          const uint32_t use = g / STAGES;
+          if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+          ptx::tc_fence_after();
+          const uint32_t sa = ptx::smem_u32(jres + (size_t)kc * kFp4ATile);
+          const uint32_t sb = ptx::smem_u32(ring + s * kBTile);
+#pragma unroll
+          for (int k = 0; k < kChunkBytes / 32; ++k)
+            ptx::mma_mxf4(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
+                          tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
+          ptx::mma_commit(&empty_bar[s]);
+        }
+        if (!ok) break;
+        ptx::mma_commit(&accf_bar);
+      }
+    }
+  } else {
+    // ---------------- epilogue: 8 warps, two per TMEM lane quadrant ----------------
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int c_lo = half * kHalf;
+    const int row = m0 + 32 * q + lane;
+    const uint32_t lane_off = (uint32_t)(32 * q) << 16;
+    const float hv = (p.h && row < p.n) ? p.h[row] : 0.0f;
+    const bool odd = (lane & 1) != 0;
+    if constexpr (!kEOnly) {
+      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
+        uint32_t vx[16], vy[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          const bool in = row < p.n && r < p.R;
+          vx[j] = __float_as_uint(in ? p.x[(size_t)r * p.xp + row] : 0.0f);
+          vy[j] = __float_as_uint(in ? p.y[(size_t)r * p.xp + row] : 0.0f);
+        }
+        ptx::tmem_st16(t_x + lane_off + c, vx);
+        ptx::tmem_st16(t_y + lane_off + c, vy);
+      }
+      ptx::tmem_st_wait();
+    }
+    float pump_next = (!kEOnly && nsteps > 0) ? p.pumps[p.t0] : 0.0f;
+    for (int ls = 0; ls < nsteps; ++ls) {
+      const int t = p.t0 + ls;
+      const int buf = (p.buf0 + ls) & 1;
+      const bool got = ptx::mbar_wait(&accf_bar, (uint32_t)ls & 1);
+      if (!epi_all(got)) { ok = false; break; }
+      ptx::tc_fence_after();
+      const float pump = pump_next;
+      if (!kEOnly && ls + 1 < nsteps) pump_next = p.pumps[t + 1];
+      constexpr int kChunks = kHalf / 16;
+#pragma unroll 1
+      for (int i = 0; i < kChunks; ++i) {
+        const int c = c_lo + 16 * i;
+        uint32_t va[16], vx[16], vy[16];
+        ptx::tmem_ld16(t_acc + lane_off + c, va);
+        if constexpr (!kEOnly) {
+          ptx::tmem_ld16(t_x + lane_off + c, vx);
+          ptx::tmem_ld16(t_y + lane_off + c, vy);
+        }
+        ptx::tmem_ld_wait();
+        float e2[16];
+        uint32_t nib_lo = 0, nib_hi = 0;  // this spin's next-operand nibbles for replicas c..c+7, c+8..c+15
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          const bool in = row < p.n && r < p.R;
+          const float f = __uint_as_float(va[j]);
+          float x, y;
+          if constexpr (kEOnly) {
+            x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
+            y = 0.0f;
+          } else {
+            x = __uint_as_float(vx[j]);
+            y = __uint_as_float(vy[j]);
+          }
+          if constexpr (want_e) {
+            const float sg = sgnf(x);
+            e2[j] = in ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
+          }
+          if constexpr (!kEOnly) {
+            if (in) sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
+            const uint32_t nib = in ? (x > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+            if (j < 8) nib_lo |= nib << (4 * j);
+            else nib_hi |= nib << (4 * (j - 8));
+          }
+          vx[j] = __float_as_uint(x);
+          vy[j] = __float_as_uint(y);
+        }
+        if constexpr (!kEOnly) {
+          ptx::tmem_st16(t_x + lane_off + c, vx);
+          ptx::tmem_st16(t_y + lane_off + c, vy);
+          // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte: the
+          // even lane writes replicas c..c+7, the odd lane c+8..c+15
+          const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
+          const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
+          const uint32_t lo_n = odd ? o_hi : nib_lo;  // even spin's nibbles for this lane's 8 replicas
+          const uint32_t hi_n = odd ? nib_hi : o_lo;  // odd spin's nibbles
+          uint8_t *dst = vtile + (size_t)(c + (odd ? 8 : 0)) * kVRow + ((32 * q + lane) >> 1);
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            dst[j * kVRow] = (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
+        }
+        if constexpr (want_e) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float v = e2[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) ered[q][c + j] = v;
+          }
+        }
+      }
+      if constexpr (!kEOnly) ptx::tmem_st_wait();
+      // the accumulator may be overwritten from here on
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&acce_bar);
+      if constexpr (!kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> TMA store
+      epi_sync();
+      if (!kEOnly && threadIdx.x == kEpiFirstThread) {
+        ptx::tma_store_2d(&p.tmS[buf ^ 1], vtile, m0 / 2, r0);
+        ptx::bulk_commit();
+        ptx::bulk_wait_all();  // the tile is in global memory (and may be rewritten next step)
+        ptx::fence_proxy_async_global();
+        __threadfence();
+        st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
+      }
+      if constexpr (want_e) {
+        for (int c = threadIdx.x - kEpiFirstThread; c < NR; c += kEpiThreads) {
+          const int r = r0 + c;
+          if (r < p.R) {
+            double *slot = kEOnly ? p.energy : p.energy + (size_t)t * p.R;
+            const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
+            atomicAdd(slot + r, 0.5 * sum);
+          }
+        }
+        epi_sync();  // ered is rewritten by the next step
+      }
+      // vtile is rewritten only in the next step's epilogue, whose accumulator needs this unit's
+      // own published chunk, i.e. the store above has completed
+    }
+    // write the state back
+    if (!kEOnly && ok) {
+      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
+        uint32_t vx[16], vy[16];
+        ptx::tmem_ld16(t_x + lane_off + c, vx);
+        ptx::tmem_ld16(t_y + lane_off + c, vy);
+        ptx::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int r = r0 + c + j;
+          if (row < p.n && r < p.R) {
+            p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
+            p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
+          }
+        }
+      }
+    }
+  }
+  if (!ok) atomicOr(p.status, kErrWaitTimeout);
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, kCols);
+  }
+}
+
+}  // namespace tck
+}  // namespace sbk

@@ -22,7 +22,8 @@ SB_OK, SB_ERR_PENDING = 0, 12
 ASB, BSB, DSB = 0, 1, 2
 FIELD_AUTO, FIELD_FP32, FIELD_TC = 0, 1, 2
 INIT_UNIFORM, INIT_REFERENCE = 0, 1
-DTYPE_NAMES = {0: "f32", 1: "fp8e4m3", 2: "bf16", 3: "bf16x2"}
+DTYPE_NAMES = {0: "f32", 1: "fp8e4m3", 2: "bf16", 3: "bf16x2", 4: "fp4e2m1"}
+OPERAND_AUTO, OPERAND_FP8, OPERAND_BF16, OPERAND_BF16X2, OPERAND_FP4 = 0, 1, 2, 3, 4
 VARIANTS = {"asb": ASB, "bsb": BSB, "dsb": DSB}
 
 
@@ -62,6 +63,7 @@ class Params(C.Structure):
         ("trace", C.c_int32),
         ("trace_all", C.c_int32),
         ("profile", C.c_int32),
+        ("operand_dtype", C.c_int32),
     ]
 
     @classmethod

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SB_ABI_VERSION 1
+#define SB_ABI_VERSION 2
 
 typedef enum sb_status {
   SB_OK = 0,
@@ -70,11 +70,24 @@ typedef enum sb_variant { SB_ASB = 0, SB_BSB = 1, SB_DSB = 2 } sb_variant;
  *  SB_FIELD_AUTO: tensor cores when replicas >= 32 and the problem allows an exact/declared
  *                 precision, otherwise the plain FP32 kernel.
  *  SB_FIELD_FP32: the plain fused FP32 kernel, one launch per step (the drop-in form).
- *  SB_FIELD_TC:   tcgen05 tensor cores. dSB with integer |J| <= 16: FP8 E4M3 operands, FP32
+ *  SB_FIELD_TC:   tcgen05 tensor cores. dSB with integer |J| <= 4 and n <= ~2300: packed E2M1
+ *                 operands with J resident in shared memory, FP32 accumulation (bit-exact).
+ *                 dSB with integer |J| <= 16: FP8 E4M3 operands, FP32
  *                 accumulation (bit-exact). dSB with integer |J| <= 256: BF16 operands (bit-exact).
  *                 dSB with real J: BF16 hi+lo split of J. bSB: BF16 hi+lo split of J and of x
  *                 (three products), FP32 accumulation. aSB is not offered on tensor cores. */
 typedef enum sb_field_mode { SB_FIELD_AUTO = 0, SB_FIELD_FP32 = 1, SB_FIELD_TC = 2 } sb_field_mode;
+
+/* Tensor-core operand type (sb_params.operand_dtype, sb_result.field_dtype_used). AUTO takes the
+ * narrowest exact type the couplings allow; a forced type must be exact for them as well
+ * (SB_ERR_UNSUPPORTED otherwise). */
+typedef enum sb_operand_dtype {
+  SB_OPERAND_AUTO = 0,
+  SB_OPERAND_FP8 = 1,    /* E4M3, integer |J| <= 16 */
+  SB_OPERAND_BF16 = 2,   /* integer |J| <= 256 */
+  SB_OPERAND_BF16X2 = 3, /* BF16 hi + lo, real J */
+  SB_OPERAND_FP4 = 4     /* packed E2M1, integer |J| <= 4, single-instance dSB */
+} sb_operand_dtype;
 
 /* Initial x, y.
  *  SB_INIT_UNIFORM:   x, y iid uniform in [-0.1, 0.1) from a counter-based hash of (seed, replica,
@@ -131,6 +144,7 @@ typedef struct sb_params {
   int32_t trace_all;       /* 1: record every replica's energy at every step */
   int32_t profile;         /* 1: run the step loop launch by launch (no CUDA graph) with a CUDA
                               event pair around every step kernel; fills kernel_ms_avg */
+  int32_t operand_dtype;   /* sb_operand_dtype for the tensor-core field (0: auto) */
 } sb_params;
 
 /* Results. The caller owns every array; any of them may be NULL. */
@@ -148,7 +162,7 @@ typedef struct sb_result {
   int64_t best_energy_i64;     /* exact host re-check (integer problems); 0 otherwise */
   int32_t best_replica;
   int32_t field_mode_used;     /* SB_FIELD_FP32 or SB_FIELD_TC */
-  int32_t field_dtype_used;    /* 0 fp32, 1 fp8 e4m3, 2 bf16, 3 bf16 hi+lo */
+  int32_t field_dtype_used;    /* 0 fp32, else the sb_operand_dtype used */
   int32_t energy_check_ok;     /* 1 when the host re-check agrees with the device energy */
   double device_ms;            /* CUDA-event time of init + step loop + final energy */
   double kernel_ms_avg;        /* profile == 1: average device time of one launch of the step kernel

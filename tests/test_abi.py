@@ -30,7 +30,7 @@ def test_every_declared_symbol_is_exported():
 
 
 def test_abi_version_and_status_strings():
-    assert lib().sb_abi_version() == 1
+    assert lib().sb_abi_version() == 2
     assert lib().sb_status_string(0) == b"ok"
     assert lib().sb_status_string(3) == b"parse error"
 

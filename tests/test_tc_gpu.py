@@ -1,7 +1,7 @@
 """Tensor-core (tcgen05) path against the CPU oracle, through the C ABI.
 
-dSB with integer couplings runs on FP8 E4M3 (|J| <= 16) or BF16 (|J| <= 256) operands with FP32
-accumulation: the field is exact, the update uses the oracle's operation order, so trajectories
+dSB with integer couplings runs on packed E2M1 (|J| <= 4, J resident in shared memory), FP8 E4M3
+(|J| <= 16) or BF16 (|J| <= 256) operands with FP32 accumulation: the field is exact, the update uses the oracle's operation order, so trajectories
 and energies are bit-exact. Real couplings use BF16 hi + lo splits and are compared with the FP64
 oracle for the first steps.
 """
@@ -31,15 +31,24 @@ def oracle_dsb(J, h, R, steps, seed, c0, trace=False):
     return x, y, None
 
 
+OPERAND = {"fp4e2m1": sb.OPERAND_FP4, "fp8e4m3": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16}
+
+
 @pytest.mark.parametrize("n,R,steps,jmax,dtype", [
     (96, 40, 30, 1, "fp8e4m3"),
     (300, 130, 40, 1, "fp8e4m3"),
     (129, 33, 25, 16, "fp8e4m3"),
     (257, 64, 25, 100, "bf16"),
+    # E2M1: K padded to 256 spins (n = 96, 300: padding chunks no unit writes), odd unit counts
+    (96, 40, 30, 1, "fp4e2m1"),
+    (300, 130, 40, 1, "fp4e2m1"),
+    (129, 33, 25, 4, "fp4e2m1"),
+    (600, 200, 25, 3, "fp4e2m1"),
+    (2300, 64, 12, 1, "fp4e2m1"),
 ])
 def test_dsb_integer_bit_exact(ctx, n, R, steps, jmax, dtype):
     J = instances.erdos_renyi(n, 0.6, seed=n + R, jmax=jmax, allow_zero=jmax > 1)
-    prob, res = solve_tc(ctx, J, None, sb.DSB, R, steps, seed=21)
+    prob, res = solve_tc(ctx, J, None, sb.DSB, R, steps, seed=21, operand_dtype=OPERAND[dtype])
     assert res.field_mode == sb.FIELD_TC and res.field_dtype == dtype
     x, y, _ = oracle_dsb(J, None, R, steps, 21, prob.default_c0())
     np.testing.assert_array_equal(res.final_x, x)
@@ -48,21 +57,25 @@ def test_dsb_integer_bit_exact(ctx, n, R, steps, jmax, dtype):
     assert res.energy_check_ok and res.best_energy_i64 == res.best_energy
 
 
-def test_dsb_with_field_and_trace(ctx):
+@pytest.mark.parametrize("dtype", ["fp8e4m3", "fp4e2m1"])
+def test_dsb_with_field_and_trace(ctx, dtype):
     n, R, steps = 200, 48, 30
     J = instances.complete_pm1(n, seed=12)
     h = np.random.default_rng(3).integers(-2, 3, n).astype(np.float32)
-    prob, res = solve_tc(ctx, J, h, sb.DSB, R, steps, seed=5, trace=1, trace_all=1)
+    prob, res = solve_tc(ctx, J, h, sb.DSB, R, steps, seed=5, trace=1, trace_all=1, operand_dtype=OPERAND[dtype])
+    assert res.field_dtype == dtype
     x, y, tra = oracle_dsb(J, h, R, steps, 5, prob.default_c0(), trace=True)
     np.testing.assert_array_equal(res.final_x, x)
     np.testing.assert_array_equal(res.energy_trace_all, tra)
     np.testing.assert_array_equal(res.energy_trace, tra.min(axis=1))
 
 
-def test_dsb_batched_2000_by_1024(ctx):
+@pytest.mark.parametrize("dtype", ["fp8e4m3", "fp4e2m1"])
+def test_dsb_batched_2000_by_1024(ctx, dtype):
     """The batched workload's shape (N = 2000 complete +-1, R = 1024) for 20 steps."""
     J = instances.complete_pm1(2000, seed=1234)
-    prob, res = solve_tc(ctx, J, None, sb.DSB, 1024, 20, seed=1234)
+    prob, res = solve_tc(ctx, J, None, sb.DSB, 1024, 20, seed=1234, operand_dtype=OPERAND[dtype])
+    assert res.field_dtype == dtype
     x, y, _ = oracle_dsb(J, None, 1024, 20, 1234, prob.default_c0())
     np.testing.assert_array_equal(res.final_x, x)
     np.testing.assert_array_equal(res.final_y, y)

@@ -32,7 +32,8 @@ def test_noalloc_matches_sb_solve_on_two_calls():
     h = np.random.default_rng(5).integers(-2, 3, n).astype(np.float32)
     ctx = sb.Context(0)
     prob = sb.Problem.from_dense(J, h)
-    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
+    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC,
+                            operand_dtype=sb.OPERAND_FP8)
     ref = ctx.solve(prob, prm, want_state=True)
     assert ref.field_dtype == "fp8e4m3"
     dJ, dh, dx, dy, de = _device_buffers(torch, J, h, R, n)
