@@ -166,6 +166,7 @@ struct TcEngine {
   TcArgs args{};
   const void *kernel[3] = {nullptr, nullptr, nullptr};  // by epilogue mode
   size_t smem = 0;
+  int threads = kTcThreads;
 };
 
 namespace {
@@ -206,7 +207,8 @@ int choose_nr(int n, int R, int sms) {
 
 }  // namespace
 
-size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * sizeof(uint32_t) + 255) / 256 * 256; }
+// one counter per unit (per unit and replica half for the E2M1 kernel)
+size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * 2 * sizeof(uint32_t) + 255) / 256 * 256; }
 
 bool tc_fp4_fits(int n, int R) {
   const int nr = choose_nr(n, R, sm_count());
@@ -256,6 +258,9 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
   }
   const bool fp4 = s.dtype == kTcFp4;
   const int elem = (s.dtype == kTcFp8 || fp4) ? 1 : 2;
+  // V boxes: the whole replica tile, or one replica half for the E2M1 kernel
+  const uint32_t vrows = fp4 ? (uint32_t)(nr >= 64 ? nr / 2 : nr) : (uint32_t)nr;
+  if (fp4) e->threads = kFp4Threads;
   e->Np = (s.n + kBM - 1) / kBM * kBM;
   e->Kp = kp_for(s.dtype, s.n);
   const uint64_t row_elems = fp4 ? (uint64_t)e->Kp / 2 : (uint64_t)e->Kp;  // operand row: bytes (E2M1 pairs) or elements
@@ -287,13 +292,13 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     if (!encode_2d(&g.tmA[a], e->a[a], elem, row_elems, (uint64_t)e->Np, kBM)) return fail("cuTensorMapEncodeTiled(J)", cudaSuccess);
   for (int b = 0; b < 2; ++b)
     for (int pp = 0; pp < bp; ++pp) {
-      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, row_elems, (uint64_t)e->Rp, (uint32_t)nr))
+      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, row_elems, (uint64_t)e->Rp, vrows))
         return fail("cuTensorMapEncodeTiled(V)", cudaSuccess);
       g.v[b][pp] = e->v[b][pp];
     }
   // the unit's V tile: 128 spins = 128 elements, or 64 bytes of E2M1 pairs
   for (int b = 0; b < 2; ++b)
-    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, row_elems, (uint64_t)e->Rp, (uint32_t)nr, true, fp4 ? kBM / 2 : kBM))
+    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, row_elems, (uint64_t)e->Rp, vrows, true, fp4 ? kBM / 2 : kBM))
       return fail("cuTensorMapEncodeTiled(V store)", cudaSuccess);
   g.flags = e->flags;
   g.n = s.n;
@@ -353,7 +358,7 @@ static cudaError_t launch(TcEngine *e, int emode, const TcArgs &a, cudaStream_t 
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3((unsigned)e->units);
-  cfg.blockDim = dim3(kTcThreads);
+  cfg.blockDim = dim3((unsigned)e->threads);
   cfg.dynamicSmemBytes = e->smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];

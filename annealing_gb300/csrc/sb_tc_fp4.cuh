@@ -2,15 +2,19 @@
 //
 // Same contraction as tc_sb_kernel (F[i][r] = sum_k J[i][k] sign(x[r][k]), the reference's per-step
 // field call SB/CUDA_GPU/m2_opt.cu:169 for all replicas at once) and the same persistent,
-// flag-ordered structure, with two changes that cut the operand traffic of a step by 4x:
+// flag-ordered structure, with three changes:
 //   * operands are E2M1 (4-bit floats, two per byte): sign(x) is +-1 and every integer coupling
 //     with |J| <= 4 is exact, so the products and their FP32 sums are the integers the FP8 and
 //     INT8 forms give (bit-identical fields); the MMA is tcgen05 kind::mxf4 with every block scale
 //     1.0 (UE8M0 0x7F written once into TMEM);
 //   * a unit's J rows (128 spins x Kp/2 bytes, at most ~160 KB) are loaded into shared memory once
-//     per launch, so each SB step streams only the unit's V tile (NR replicas x Kp/2 bytes) from L2.
-// TMEM columns: accumulator [0, NR), x [NR, 2NR), y [2NR, 3NR), A scales [3NR, 3NR + 16),
-// B scales [3NR + 16, 3NR + 32). The nibble order inside a byte (spin 2j in the low half) is the
+//     per launch, so each SB step streams only the unit's V tile (NR replicas x Kp/2 bytes) from L2;
+//   * the replica tile is split in two halves that move through the step one after the other:
+//     half 0's epilogue publishes its part of V(t+1) (a dedicated publisher warp does the TMA store
+//     and the release) while half 1 is still being updated, so the units of the column start the
+//     next contraction on half 0 while this one finishes half 1. Flags are per (unit, half).
+// TMEM columns: accumulators [0, NR) (half h at [h NR/2, (h+1) NR/2)), x [NR, 2NR), y [2NR, 3NR),
+// A scales [3NR, 3NR + 16), B scales [3NR + 16, 3NR + 32). The nibble order inside a byte (spin 2j in the low half) is the
 // same for J and V, so the dot products do not depend on how the tensor core orders the pair.
 #pragma once
 #include "sb_tc_kernel.cuh"
@@ -40,36 +44,51 @@ __host__ __device__ constexpr uint32_t make_idesc_mxf4(int m, int n) {
   return (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | (1u << 23) | ((uint32_t)(m >> 4) << 24);
 }
 
-constexpr int kFp4Stages = 4;  // V chunks in flight
-
+// Replica halves and pipeline depth per replica tile: each epilogue warp takes a multiple of 16
+// columns of a half.
 template <int NR>
-__host__ __device__ constexpr int fp4_btile() { return NR * kChunkBytes; }
+struct Fp4Cfg {
+  static constexpr int kHalves = NR >= 64 ? 2 : 1;
+  static constexpr int kNH = NR / kHalves;           // replicas per half: MMA N, V box rows
+  static constexpr int kBTile = kNH * kChunkBytes;   // one V chunk of one half
+  static constexpr int kStages = 8;
+  static constexpr int kWarpCols = kNH / 2;          // columns of a half per epilogue warp
+};
+constexpr int kFp4Threads = kTcThreads + 32;  // + the publisher warp
+
 constexpr int kFp4ATile = kBM * kChunkBytes;  // one J chunk: 128 spins x 256 spins of K
 // Shared memory of one CTA for k_chunks 128-byte chunks of K (256 spins each).
+// At least enough that no more CTAs share an SM than its 512 TMEM columns hold (a CTA waiting
+// in tcgen05.alloc would stall the flag-ordered grid).
 template <int NR>
 constexpr size_t fp4_smem(int k_chunks) {
-  return 1024 + (size_t)kFp4Stages * fp4_btile<NR>() + (size_t)k_chunks * kFp4ATile + (size_t)NR * (kBM / 2);
+  constexpr int kCols = 3 * NR + 32 <= 128 ? 128 : (3 * NR + 32 <= 256 ? 256 : 512);
+  constexpr size_t kFloor = 233472 / (512 / kCols + 1) + 1024;  // 228 KB of shared memory per SM
+  const size_t need = 1024 + (size_t)Fp4Cfg<NR>::kStages * Fp4Cfg<NR>::kBTile + (size_t)k_chunks * kFp4ATile +
+                      (size_t)NR * (kBM / 2);
+  return need > kFloor ? need : kFloor;
 }
 
-// flags / buffers as in tc_sb_kernel; p.k_chunks = Kp / 256 (Kp a multiple of 256, J and V rows of
-// Kp / 2 bytes); p.tmA / p.tmB load 128-byte x rows boxes, p.tmS stores the unit's 64-byte x NR tile.
+// Buffers as in tc_sb_kernel; p.k_chunks = Kp / 256 (Kp a multiple of 256, J and V rows of Kp / 2
+// bytes); p.tmA loads 128-byte x 128-row J boxes, p.tmB 128-byte x NR/2-row V boxes (NR/2 = the
+// half's replicas; the whole NR when NR = 32), p.tmS stores one half tile (64 bytes x NR/2 rows).
+// p.flags[(rt * halves + h) * n_mtiles + mt] = steps whose half h this unit has published.
 template <int NR, int EMODE>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_constant__ TcArgs p) {
-  constexpr int STAGES = kFp4Stages;
-  constexpr int kBTile = fp4_btile<NR>();
+__global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_constant__ TcArgs p) {
+  using F = Fp4Cfg<NR>;
+  constexpr int H = F::kHalves, NH = F::kNH, STAGES = F::kStages, kBTile = F::kBTile;
   constexpr int kVRow = kBM / 2;  // bytes of one replica row of the unit's V tile
   constexpr uint32_t kSf = 3 * NR;
   constexpr uint32_t kCols = kSf + 32 <= 128 ? 128 : (kSf + 32 <= 256 ? 256 : 512);
-  constexpr uint32_t kIdesc = make_idesc_mxf4(kBM, NR);
-  constexpr int kHalf = NR / 2;
-  static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
+  constexpr uint32_t kIdesc = make_idesc_mxf4(kBM, NH);
+  static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128 && F::kWarpCols % 16 == 0, "replica tile");
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t *ring = smem;                                   // [STAGES][NR][128] V chunks
+  uint8_t *ring = smem;                                   // [STAGES][NH][128] V chunks
   uint8_t *jres = smem + STAGES * kBTile;                  // [k_chunks][128][128] resident J
-  uint8_t *vtile = jres + (size_t)p.k_chunks * kFp4ATile;  // [NR][64] next V tile of this unit
-  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], a_bar, accf_bar, acce_bar;
+  uint8_t *vtile = jres + (size_t)p.k_chunks * kFp4ATile;  // [NR][64] next V tile (half h: rows h NH ..)
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], a_bar, accf_bar[H], acce_bar[H], pub_bar[H];
   __shared__ uint32_t tmem_base_sh;
   __shared__ float ered[4][NR];
 
@@ -79,7 +98,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_cons
   constexpr bool kEOnly = EMODE == kEmodeEnergy;
   constexpr bool want_e = EMODE != kEmodeStep;
   const int nsteps = kEOnly ? 1 : p.steps;
-  uint32_t *col_flags = p.flags + (size_t)rt * p.n_mtiles;
   bool ok = true;
 
   if (threadIdx.x == 0) {
@@ -88,8 +106,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_cons
       ptx::mbar_init(&empty_bar[s], 1);
     }
     ptx::mbar_init(&a_bar, 1);
-    ptx::mbar_init(&accf_bar, 1);
-    ptx::mbar_init(&acce_bar, kEpiWarps);
+    for (int h = 0; h < H; ++h) {
+      ptx::mbar_init(&accf_bar[h], 1);
+      ptx::mbar_init(&acce_bar[h], kEpiWarps);
+      ptx::mbar_init(&pub_bar[h], kEpiWarps);
+    }
     ptx::fence_mbar_init();
     ptx::prefetch_tmap(&p.tmA[0]);
     ptx::prefetch_tmap(&p.tmB[0][0]);
@@ -103,8 +124,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_cons
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
-  const uint32_t t_acc = tmem, t_x = tmem + NR, t_y = tmem + 2 * NR;
-  if (warp >= 2) {
+  const uint32_t t_x = tmem + NR, t_y = tmem + 2 * NR;
+  if (warp >= 2 && warp < 2 + kEpiWarps) {
     // every block scale = 2^0: UE8M0 0x7F in all bytes of the scale columns, all 128 lanes
     uint32_t ones[16];
 #pragma unroll
@@ -127,28 +148,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_cons
     uint32_t g = 0;
     for (int ls = 0; ls < nsteps && ok; ++ls) {
       const int buf = (p.buf0 + ls) & 1;
-      int ready = ls == 0 ? p.n_mtiles : 0;  // units of this column known to have published V(ls)
-      for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++g) {
-        // chunk kc holds the spins of units 2 kc and 2 kc + 1
-        const int need = 2 * kc + 2 < p.n_mtiles ? 2 * kc + 2 : p.n_mtiles;
-        if (need > ready) {
-          const int u = ready + lane;
-          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls) : true;
-          if (!__all_sync(0xffffffffu, fl)) ok = false;
-          ready = ready + 32 < p.n_mtiles ? ready + 32 : p.n_mtiles;
+      for (int h = 0; h < H && ok; ++h) {
+        if (ls > 0) {
+          // half h of V(ls) complete: every unit of the replica column has published it (the warp
+          // polls 32 units per L2 round trip)
+          const uint32_t *hf = p.flags + (size_t)(rt * H + h) * p.n_mtiles;
+          for (int u0 = 0; u0 < p.n_mtiles && ok; u0 += 32) {
+            const int u = u0 + lane;
+            const bool fl = u < p.n_mtiles ? wait_flag(hf + u, (uint32_t)ls) : true;
+            if (!__all_sync(0xffffffffu, fl)) ok = false;
+          }
           ptx::fence_proxy_async_global();
         }
-        if (lane == 0 && ok) {
-          const int s = g % STAGES;
-          const uint32_t use = g / STAGES;
-          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
-            ok = false;
-          } else {
-            ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)kBTile);
-            ptx::tma_load_2d(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes, r0, &full_bar[s]);
+        for (int kc = 0; kc < p.k_chunks && ok; ++kc, ++g) {
+          if (lane == 0) {
+            const int s = g % STAGES;
+            const uint32_t use = g / STAGES;
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+              ok = false;
+            } else {
+              ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)kBTile);
+              ptx::tma_load_2d(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes, r0 + h * NH, &full_bar[s]);
+            }
           }
+          ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
         }
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       }
     }
   } else if (warp == 1) {
@@ -157,166 +181,182 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_fp4_kernel(const __grid_cons
       ok = ptx::mbar_wait(&a_bar, 0);
       uint32_t g = 0;
       for (int ls = 0; ls < nsteps && ok; ++ls) {
-        if (ls >= 1 && !ptx::mbar_wait(&acce_bar, (uint32_t)(ls - 1) & 1)) { ok = false; break; }
-        ptx::tc_fence_after();
-        for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
-          const int s = g % STAGES;
-          const uint32_t use = g / STAGES;
-          if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+        for (int h = 0; h < H && ok; ++h) {
+          if (ls >= 1 && !ptx::mbar_wait(&acce_bar[h], (uint32_t)(ls - 1) & 1)) { ok = false; break; }
           ptx::tc_fence_after();
-          const uint32_t sa = ptx::smem_u32(jres + (size_t)kc * kFp4ATile);
-          const uint32_t sb = ptx::smem_u32(ring + s * kBTile);
+          const uint32_t t_acc = tmem + h * NH;
+          for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+            const int s = g % STAGES;
+            const uint32_t use = g / STAGES;
+            if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+            ptx::tc_fence_after();
+            const uint32_t sa = ptx::smem_u32(jres + (size_t)kc * kFp4ATile);
+            const uint32_t sb = ptx::smem_u32(ring + s * kBTile);
 #pragma unroll
-          for (int k = 0; k < kChunkBytes / 32; ++k)
-            ptx::mma_mxf4(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
-                          tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
-          ptx::mma_commit(&empty_bar[s]);
+            for (int k = 0; k < kChunkBytes / 32; ++k)
+              ptx::mma_mxf4(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
+                            tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
+            ptx::mma_commit(&empty_bar[s]);
+          }
+          if (!ok) break;
+          ptx::mma_commit(&accf_bar[h]);
         }
-        if (!ok) break;
-        ptx::mma_commit(&accf_bar);
+      }
+    }
+  } else if (warp == 2 + kEpiWarps) {
+    // ---------------- publisher: half tile -> global (TMA store), then the flag ----------------
+    if (!kEOnly && lane == 0) {
+      for (int ls = 0; ls < nsteps && ok; ++ls) {
+        const int buf = (p.buf0 + ls) & 1;
+        for (int h = 0; h < H; ++h) {
+          if (!ptx::mbar_wait(&pub_bar[h], (uint32_t)ls & 1)) { ok = false; break; }
+          ptx::tma_store_2d(&p.tmS[buf ^ 1], vtile + (size_t)h * NH * kVRow, m0 / 2, r0 + h * NH);
+          ptx::bulk_commit();
+          ptx::bulk_wait_all();             // the half tile is in global memory
+          ptx::fence_proxy_async_global();  // the bulk store's writes, then the flag (release)
+          st_release(p.flags + (size_t)(rt * H + h) * p.n_mtiles + mt, (uint32_t)(ls + 1));
+        }
       }
     }
   } else {
     // ---------------- epilogue: 8 warps, two per TMEM lane quadrant ----------------
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
-    const int c_lo = half * kHalf;
+    const int sub = (warp - 2) >> 2;  // which kWarpCols columns of each half
     const int row = m0 + 32 * q + lane;
     const uint32_t lane_off = (uint32_t)(32 * q) << 16;
     const float hv = (p.h && row < p.n) ? p.h[row] : 0.0f;
     const bool odd = (lane & 1) != 0;
     if constexpr (!kEOnly) {
-      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
-        uint32_t vx[16], vy[16];
+      for (int h = 0; h < H; ++h)
+        for (int c = h * NH + sub * F::kWarpCols; c < h * NH + (sub + 1) * F::kWarpCols; c += 16) {
+          uint32_t vx[16], vy[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = r0 + c + j;
-          const bool in = row < p.n && r < p.R;
-          vx[j] = __float_as_uint(in ? p.x[(size_t)r * p.xp + row] : 0.0f);
-          vy[j] = __float_as_uint(in ? p.y[(size_t)r * p.xp + row] : 0.0f);
+          for (int j = 0; j < 16; ++j) {
+            const int r = r0 + c + j;
+            const bool in = row < p.n && r < p.R;
+            vx[j] = __float_as_uint(in ? p.x[(size_t)r * p.xp + row] : 0.0f);
+            vy[j] = __float_as_uint(in ? p.y[(size_t)r * p.xp + row] : 0.0f);
+          }
+          ptx::tmem_st16(t_x + lane_off + c, vx);
+          ptx::tmem_st16(t_y + lane_off + c, vy);
         }
-        ptx::tmem_st16(t_x + lane_off + c, vx);
-        ptx::tmem_st16(t_y + lane_off + c, vy);
-      }
       ptx::tmem_st_wait();
     }
     float pump_next = (!kEOnly && nsteps > 0) ? p.pumps[p.t0] : 0.0f;
-    for (int ls = 0; ls < nsteps; ++ls) {
+    for (int ls = 0; ls < nsteps && ok; ++ls) {
       const int t = p.t0 + ls;
-      const int buf = (p.buf0 + ls) & 1;
-      const bool got = ptx::mbar_wait(&accf_bar, (uint32_t)ls & 1);
-      if (!epi_all(got)) { ok = false; break; }
-      ptx::tc_fence_after();
       const float pump = pump_next;
       if (!kEOnly && ls + 1 < nsteps) pump_next = p.pumps[t + 1];
-      constexpr int kChunks = kHalf / 16;
+      for (int h = 0; h < H; ++h) {
+        const bool got = ptx::mbar_wait(&accf_bar[h], (uint32_t)ls & 1);
+        if (!epi_all(got)) { ok = false; break; }
+        ptx::tc_fence_after();
+        const int c_lo = h * NH + sub * F::kWarpCols;
 #pragma unroll 1
-      for (int i = 0; i < kChunks; ++i) {
-        const int c = c_lo + 16 * i;
-        uint32_t va[16], vx[16], vy[16];
-        ptx::tmem_ld16(t_acc + lane_off + c, va);
-        if constexpr (!kEOnly) {
-          ptx::tmem_ld16(t_x + lane_off + c, vx);
-          ptx::tmem_ld16(t_y + lane_off + c, vy);
-        }
-        ptx::tmem_ld_wait();
-        float e2[16];
-        uint32_t nib_lo = 0, nib_hi = 0;  // this spin's next-operand nibbles for replicas c..c+7, c+8..c+15
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = r0 + c + j;
-          const bool in = row < p.n && r < p.R;
-          const float f = __uint_as_float(va[j]);
-          float x, y;
-          if constexpr (kEOnly) {
-            x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
-            y = 0.0f;
-          } else {
-            x = __uint_as_float(vx[j]);
-            y = __uint_as_float(vy[j]);
-          }
-          if constexpr (want_e) {
-            const float sg = sgnf(x);
-            e2[j] = in ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
-          }
+        for (int c = c_lo; c < c_lo + F::kWarpCols; c += 16) {
+          uint32_t va[16], vx[16], vy[16];
+          ptx::tmem_ld16(tmem + lane_off + c, va);
           if constexpr (!kEOnly) {
-            if (in) sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
-            const uint32_t nib = in ? (x > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
-            if (j < 8) nib_lo |= nib << (4 * j);
-            else nib_hi |= nib << (4 * (j - 8));
+            ptx::tmem_ld16(t_x + lane_off + c, vx);
+            ptx::tmem_ld16(t_y + lane_off + c, vy);
           }
-          vx[j] = __float_as_uint(x);
-          vy[j] = __float_as_uint(y);
-        }
-        if constexpr (!kEOnly) {
-          ptx::tmem_st16(t_x + lane_off + c, vx);
-          ptx::tmem_st16(t_y + lane_off + c, vy);
-          // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte: the
-          // even lane writes replicas c..c+7, the odd lane c+8..c+15
-          const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
-          const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
-          const uint32_t lo_n = odd ? o_hi : nib_lo;  // even spin's nibbles for this lane's 8 replicas
-          const uint32_t hi_n = odd ? nib_hi : o_lo;  // odd spin's nibbles
-          uint8_t *dst = vtile + (size_t)(c + (odd ? 8 : 0)) * kVRow + ((32 * q + lane) >> 1);
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            dst[j * kVRow] = (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
-        }
-        if constexpr (want_e) {
+          ptx::tmem_ld_wait();
+          float e2[16];
+          uint32_t nib_lo = 0, nib_hi = 0;  // this spin's next-operand nibbles for replicas c..c+7, c+8..c+15
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            float v = e2[j];
+            const int r = r0 + c + j;
+            const bool in = row < p.n && r < p.R;
+            const float f = __uint_as_float(va[j]);
+            float x, y;
+            if constexpr (kEOnly) {
+              x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
+              y = 0.0f;
+            } else {
+              x = __uint_as_float(vx[j]);
+              y = __uint_as_float(vy[j]);
+            }
+            if constexpr (want_e) {
+              const float sg = sgnf(x);
+              e2[j] = in ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
+            }
+            if constexpr (!kEOnly) {
+              // padded spins and replicas hold x = y = 0 and see f = h = 0, so they stay +0: the
+              // update runs unpredicated and only the operand is masked
+              sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
+              const uint32_t nib = in ? (x > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+              if (j < 8) nib_lo |= nib << (4 * j);
+              else nib_hi |= nib << (4 * (j - 8));
+            }
+            vx[j] = __float_as_uint(x);
+            vy[j] = __float_as_uint(y);
+          }
+          if constexpr (!kEOnly) {
+            ptx::tmem_st16(t_x + lane_off + c, vx);
+            ptx::tmem_st16(t_y + lane_off + c, vy);
+            // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte:
+            // the even lane writes replicas c..c+7, the odd lane c+8..c+15
+            const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
+            const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
+            const uint32_t lo_n = odd ? o_hi : nib_lo;  // even spin's nibbles for this lane's 8 replicas
+            const uint32_t hi_n = odd ? nib_hi : o_lo;  // odd spin's nibbles
+            uint8_t *dst = vtile + (size_t)(c + (odd ? 8 : 0)) * kVRow + ((32 * q + lane) >> 1);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) ered[q][c + j] = v;
+            for (int j = 0; j < 8; ++j)
+              dst[j * kVRow] = (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
+          }
+          if constexpr (want_e) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float v = e2[j];
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+              if (lane == 0) ered[q][c + j] = v;
+            }
           }
         }
-      }
-      if constexpr (!kEOnly) ptx::tmem_st_wait();
-      // the accumulator may be overwritten from here on
-      ptx::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(&acce_bar);
-      if constexpr (!kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> TMA store
-      epi_sync();
-      if (!kEOnly && threadIdx.x == kEpiFirstThread) {
-        ptx::tma_store_2d(&p.tmS[buf ^ 1], vtile, m0 / 2, r0);
-        ptx::bulk_commit();
-        ptx::bulk_wait_all();  // the tile is in global memory (and may be rewritten next step)
-        ptx::fence_proxy_async_global();
-        __threadfence();
-        st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
-      }
-      if constexpr (want_e) {
-        for (int c = threadIdx.x - kEpiFirstThread; c < NR; c += kEpiThreads) {
-          const int r = r0 + c;
-          if (r < p.R) {
-            double *slot = kEOnly ? p.energy : p.energy + (size_t)t * p.R;
-            const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
-            atomicAdd(slot + r, 0.5 * sum);
-          }
+        if constexpr (!kEOnly) ptx::tmem_st_wait();
+        // the accumulator half may be overwritten from here on
+        ptx::tc_fence_before();
+        if constexpr (!kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> the publisher's TMA store
+        __syncwarp();
+        if (lane == 0) {
+          ptx::mbar_arrive(&acce_bar[h]);
+          if constexpr (!kEOnly) ptx::mbar_arrive(&pub_bar[h]);
         }
-        epi_sync();  // ered is rewritten by the next step
+        // the next step rewrites this half tile only after its accumulator, which needs this
+        // unit's own published half, i.e. after the publisher's store has completed
+        if constexpr (want_e) {
+          epi_sync();
+          for (int c = h * NH + threadIdx.x - kEpiFirstThread; c < (h + 1) * NH; c += kEpiThreads) {
+            const int r = r0 + c;
+            if (r < p.R) {
+              double *slot = kEOnly ? p.energy : p.energy + (size_t)t * p.R;
+              const double sum = ((double)ered[0][c] + (double)ered[1][c]) + ((double)ered[2][c] + (double)ered[3][c]);
+              atomicAdd(slot + r, 0.5 * sum);
+            }
+          }
+          epi_sync();  // ered is rewritten by the next half
+        }
       }
-      // vtile is rewritten only in the next step's epilogue, whose accumulator needs this unit's
-      // own published chunk, i.e. the store above has completed
     }
     // write the state back
     if (!kEOnly && ok) {
-      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
-        uint32_t vx[16], vy[16];
-        ptx::tmem_ld16(t_x + lane_off + c, vx);
-        ptx::tmem_ld16(t_y + lane_off + c, vy);
-        ptx::tmem_ld_wait();
+      for (int h = 0; h < H; ++h)
+        for (int c = h * NH + sub * F::kWarpCols; c < h * NH + (sub + 1) * F::kWarpCols; c += 16) {
+          uint32_t vx[16], vy[16];
+          ptx::tmem_ld16(t_x + lane_off + c, vx);
+          ptx::tmem_ld16(t_y + lane_off + c, vy);
+          ptx::tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = r0 + c + j;
-          if (row < p.n && r < p.R) {
-            p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
-            p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
+          for (int j = 0; j < 16; ++j) {
+            const int r = r0 + c + j;
+            if (row < p.n && r < p.R) {
+              p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
+              p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
+            }
           }
         }
-      }
     }
   }
   if (!ok) atomicOr(p.status, kErrWaitTimeout);
