@@ -14,8 +14,9 @@
 //     and the release) while half 1 is still being updated, so the units of the column start the
 //     next contraction on half 0 while this one finishes half 1. Flags are per (unit, half).
 // TMEM columns: accumulators [0, NR) (half h at [h NR/2, (h+1) NR/2)), x [NR, 2NR), y [2NR, 3NR),
-// A scales [3NR, 3NR + 16), B scales [3NR + 16, 3NR + 32). The nibble order inside a byte (spin 2j in the low half) is the
-// same for J and V, so the dot products do not depend on how the tensor core orders the pair.
+// A scales [3NR, 3NR + 16), B scales [3NR + 16, 3NR + 32). The nibble order inside a byte (spin 2j
+// in the low half) is the same for J and V, so the dot products do not depend on how the tensor
+// core orders the pair.
 #pragma once
 #include "sb_tc_kernel.cuh"
 

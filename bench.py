@@ -56,6 +56,9 @@ WORKLOADS = {
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu capture of
 # each dominant kernel; the summaries, with the commands, are the files named here.
 NCU_TRAFFIC = {
+    # batched dSB, N=2000, R=1024, E2M1 kernel: bytes per launch, the same for 30 and 240 steps
+    # (everything after the first step is L2-resident)
+    "batched-dsb": (19.58e6, "profiles/tc_fp4_kernel_batched_dsb_n2000_r1024.md"),
     # plain dSB, N=2000, R=1: bytes per launch (ncu runs the launch with cold caches)
     "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
     # uneven batch: measured bytes per algorithmic byte on a 48-instance batch (441.2 MB of
@@ -275,8 +278,9 @@ def run_ours(args, rank, world, local_rank):
                         "fp8e4m3": (2.0, "2 x {} dense BF16 burst (FP8 E4M3 rate)")}.get(fdt, (1.0, "{} dense BF16 burst"))
         tc_peak = scale * bf16
         achieved = flops_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e12
+        traffic = NCU_TRAFFIC["batched-dsb"] if (fdt == "fp4e2m1" and n == 2000 and R == 1024) else (None, None)
         roof = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
-                "frac": achieved / tc_peak, "traffic": None,
+                "frac": achieved / tc_peak, "traffic": traffic[0], "traffic_source": traffic[1],
                 "kernel": ("tc_fp4_kernel" if fdt == "fp4e2m1" else "tc_sb_kernel") + " (persistent, one launch per solve)",
                 "launch_ms": rp.kernel_ms_avg, "sb_steps_per_launch": rp.steps_per_launch,
                 "flops_per_launch": flops_per_launch, "peak_source": label.format(src),
