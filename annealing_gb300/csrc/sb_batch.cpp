@@ -116,12 +116,26 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
       return SB_ERR_UNSUPPORTED;
     }
   }
+  // operands: packed E2M1 when every instance's couplings allow it (|J| <= 4), else FP8 E4M3
+  bool fp4 = true;
+  for (int k = 0; k < count; ++k) fp4 = fp4 && sbk::grouped_fp4_exact(&problems[k]);
+  if (prm->operand_dtype == SB_OPERAND_FP8) {
+    fp4 = false;
+  } else if (prm->operand_dtype == SB_OPERAND_FP4) {
+    if (!fp4) {
+      err = "E2M1 operands need integer couplings |J| <= 4 in every problem of the batch";
+      return SB_ERR_UNSUPPORTED;
+    }
+  } else if (prm->operand_dtype != SB_OPERAND_AUTO) {
+    err = "the grouped path runs E2M1 or FP8 operands";
+    return SB_ERR_UNSUPPORTED;
+  }
   sb_batch *b = new sb_batch();
   b->ctx = ctx;
   b->prm = *prm;
   b->probs.resize(count);
   const int R = prm->replicas;
-  b->g = new sbk::Grouped(ctx->stream, R <= 32 ? 32 : (R <= 64 ? 64 : 128), 0);
+  b->g = new sbk::Grouped(ctx->stream, R <= 32 ? 32 : (R <= 64 ? 64 : 128), 0, fp4);
   if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
     destroy(b);
     err = "cudaEventCreate";
@@ -251,7 +265,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
     r.best_energy_i64 = e64[k];
     r.best_replica = best[k];
     r.field_mode_used = SB_FIELD_TC;
-    r.field_dtype_used = 1;
+    r.field_dtype_used = g.fp4 ? SB_OPERAND_FP4 : SB_OPERAND_FP8;
     r.energy_check_ok = okv[k];
     r.device_ms = dev_ms;
     r.kernel_ms_avg = kernel_ms;

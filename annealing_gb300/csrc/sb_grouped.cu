@@ -40,6 +40,18 @@ __global__ void g_signs_kernel(const float *x, int n, int R, int xp, uint8_t *v,
   }
 }
 
+// packed E2M1 signs: byte b of replica r holds spins 2b (low nibble) and 2b + 1 (high nibble)
+__global__ void g_signs_fp4_kernel(const float *x, int n, int R, int xp, uint8_t *v, int kb) {
+  const int nb = (n + 1) / 2;
+  const size_t total = (size_t)nb * R;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / nb, b = k % nb, i = 2 * b;
+    const uint32_t c0 = x[r * xp + i] > 0.0f ? kE2m1Plus : kE2m1Minus;
+    const uint32_t c1 = i + 1 < (size_t)n ? (x[r * xp + i + 1] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+    v[r * kb + b] = (uint8_t)(c0 | (c1 << 4));
+  }
+}
+
 int grid1(size_t total) {
   size_t g = (total + 255) / 256;
   return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
@@ -70,16 +82,17 @@ bool encode_fp8(CUtensorMap *m, void *base, uint64_t inner, uint64_t outer, uint
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NR, int EMODE>
-const void *gk() {
-  return reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), EMODE>);
+template <int NR, bool FP4>
+const void *gk(int emode) {
+  return emode == kEmodeEnergy ? reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeEnergy, FP4>)
+                               : reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeStep, FP4>);
 }
 
-bool grouped_kernel_for(int nr, int emode, const void **k, size_t *smem) {
+bool grouped_kernel_for(int nr, int emode, bool fp4, const void **k, size_t *smem) {
   switch (nr) {
-    case 32: *k = emode == kEmodeEnergy ? gk<32, kEmodeEnergy>() : gk<32, kEmodeStep>(); *smem = grouped_smem<32>(); return true;
-    case 64: *k = emode == kEmodeEnergy ? gk<64, kEmodeEnergy>() : gk<64, kEmodeStep>(); *smem = grouped_smem<64>(); return true;
-    case 128: *k = emode == kEmodeEnergy ? gk<128, kEmodeEnergy>() : gk<128, kEmodeStep>(); *smem = grouped_smem<128>(); return true;
+    case 32: *k = fp4 ? gk<32, true>(emode) : gk<32, false>(emode); *smem = grouped_smem<32>(); return true;
+    case 64: *k = fp4 ? gk<64, true>(emode) : gk<64, false>(emode); *smem = grouped_smem<64>(); return true;
+    case 128: *k = fp4 ? gk<128, true>(emode) : gk<128, false>(emode); *smem = grouped_smem<128>(); return true;
   }
   return false;
 }
@@ -121,6 +134,30 @@ void pack_fp8(const float *J, int n, uint8_t *dst, int Np, int Kp) {
   for (auto &t : th) t.join();
 }
 
+// Couplings as packed E2M1 (integers |J| <= 4; e2m1_code), rows of kb bytes, zero padded.
+void pack_fp4(const float *J, int n, uint8_t *dst, int Np, int kb) {
+  uint8_t lut[9];
+  for (int v = -4; v <= 4; ++v) lut[v + 4] = (uint8_t)(e2m1_code((float)v) & 0xF);
+  const unsigned want = (unsigned)std::max<int64_t>(1, (int64_t)Np * kb / (1 << 20));
+  const unsigned nt = std::max(1u, std::min({std::thread::hardware_concurrency() / 2, want, 16u}));
+  const int rows_per = (Np + (int)nt - 1) / (int)nt;
+  std::vector<std::thread> th;
+  for (unsigned w = 0; w < nt; ++w)
+    th.emplace_back([=, &lut] {
+      const int r0 = (int)w * rows_per, r1 = std::min(Np, r0 + rows_per);
+      for (int i = r0; i < r1; ++i) {
+        uint8_t *d = dst + (size_t)i * kb;
+        memset(d, 0, kb);
+        if (i >= n) continue;
+        const float *Ji = J + (size_t)i * n;
+        for (int j = 0; j + 1 < n; j += 2)
+          d[j >> 1] = (uint8_t)(lut[(int)Ji[j] + 4] | (lut[(int)Ji[j + 1] + 4] << 4));
+        if (n & 1) d[n >> 1] = lut[(int)Ji[n - 1] + 4];
+      }
+    });
+  for (auto &t : th) t.join();
+}
+
 int device_sms() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -137,9 +174,12 @@ bool grouped_supports(const sb_problem *p, const sb_params *prm) {
          prm->replicas <= 4096 && (int64_t)p->n * 16 < (1 << 24);
 }
 
-int64_t grouped_instance_bytes(int n, int R, int steps, int nr) {
-  const int64_t Np = (n + 127) / 128 * 128, Kp = Np, Rp = (R + nr - 1) / nr * nr, xp = (n + 3) / 4 * 4;
-  return Np * Kp + 2 * Rp * Kp + 2 * (int64_t)R * xp * 4 + (int64_t)n * 4 + (int64_t)R * 8 + (int64_t)steps * 4 + 4096;
+bool grouped_fp4_exact(const sb_problem *p) { return p->integer_valued && p->max_abs_j <= 4; }
+
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr, bool fp4) {
+  const int64_t Np = (n + 127) / 128 * 128, Rp = (R + nr - 1) / nr * nr, xp = (n + 3) / 4 * 4;
+  const int64_t kb = fp4 ? (n + 255) / 256 * 128 : Np;
+  return Np * kb + 2 * Rp * kb + 2 * (int64_t)R * xp * 4 + (int64_t)n * 4 + (int64_t)R * 8 + (int64_t)steps * 4 + 4096;
 }
 
 Grouped::~Grouped() { clear(); }
@@ -182,7 +222,7 @@ void Grouped::release(GHost &g, cudaStream_t s) {
 }
 
 sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
-                           cudaStream_t st, Staging &stg, std::string &err) {
+                           cudaStream_t st, Staging &stg, std::string &err, bool fp4) {
   g.tag = tag;
   g.prob = p;
   g.n = p->n;
@@ -190,7 +230,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   g.steps = prm->steps;
   g.t0 = 0;
   g.Np = (g.n + 127) / 128 * 128;
-  g.Kp = g.Np;
+  g.fp4 = fp4;
+  g.Kp = fp4 ? (g.n + 255) / 256 * 256 : g.Np;  // K extent in spins: whole 128-byte chunks
+  g.kbytes = fp4 ? g.Kp / 2 : g.Kp;
   g.Rp = (g.R + nr - 1) / nr * nr;
   g.xp = (g.n + 3) / 4 * 4;
   g.c0 = prm->c0 > 0.0f ? prm->c0 : sb_default_c0(p);
@@ -202,8 +244,8 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     release(g, st);
     return e == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
   };
-  const size_t xs = (size_t)g.R * g.xp * sizeof(float), vb = (size_t)g.Rp * g.Kp;
-  if ((e = cudaMallocAsync(&g.a, (size_t)g.Np * g.Kp, st)) != cudaSuccess) return fail("cudaMalloc(J operand)");
+  const size_t xs = (size_t)g.R * g.xp * sizeof(float), vb = (size_t)g.Rp * g.kbytes;
+  if ((e = cudaMallocAsync(&g.a, (size_t)g.Np * g.kbytes, st)) != cudaSuccess) return fail("cudaMalloc(J operand)");
   if ((e = cudaMallocAsync(&g.v[0], vb, st)) != cudaSuccess) return fail("cudaMalloc(V)");
   if ((e = cudaMallocAsync(&g.v[1], vb, st)) != cudaSuccess) return fail("cudaMalloc(V)");
   if ((e = cudaMallocAsync(&g.x, xs, st)) != cudaSuccess) return fail("cudaMalloc(x)");
@@ -216,10 +258,10 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     if ((e = cudaMemcpyAsync(g.h, p->h, (size_t)g.n * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return fail("upload h");
   }
-  // couplings: packed to FP8 E4M3 on the host threads (integers |J| <= 16 are exact, see
-  // fp8_code) into a pinned staging buffer, then one copy into the padded operand layout: a
-  // quarter of the bytes of an FP32 upload.
-  const size_t ab = (size_t)g.Np * g.Kp;
+  // couplings: packed to FP8 E4M3 (integers |J| <= 16 are exact, see fp8_code) or to E2M1 pairs
+  // (|J| <= 4) on the host threads into a pinned staging buffer, then one copy into the padded
+  // operand layout: a quarter (an eighth) of the bytes of an FP32 upload.
+  const size_t ab = (size_t)g.Np * g.kbytes;
   if (ab > stg.bytes) {
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("synchronize");
     cudaFreeHost(stg.pin);
@@ -228,7 +270,10 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     if ((e = cudaMallocHost(&stg.pin, ab)) != cudaSuccess) return fail("cudaMallocHost(staging)");
     stg.bytes = ab;
   }
-  pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
+  if (fp4)
+    pack_fp4(p->J, g.n, stg.pin, g.Np, g.kbytes);
+  else
+    pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
   if ((e = cudaMemcpyAsync(g.a, stg.pin, ab, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
   std::vector<float> pumps((size_t)(g.steps > 0 ? g.steps : 1), 0.0f);
   for (int t = 0; t < g.steps; ++t) pumps[t] = sb_pump(prm->a0, t, g.steps);
@@ -241,9 +286,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   if ((e = cudaMemsetAsync(g.v[1], 0, vb, st)) != cudaSuccess) return fail("memset");
   if ((e = cudaMemsetAsync(g.x, 0, xs, st)) != cudaSuccess) return fail("memset");
   if ((e = cudaMemsetAsync(g.y, 0, xs, st)) != cudaSuccess) return fail("memset");
-  if (!encode_fp8(&g.desc.tmA, g.a, (uint64_t)g.Kp, (uint64_t)g.Np, kBM) ||
-      !encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr) ||
-      !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr)) {
+  if (!encode_fp8(&g.desc.tmA, g.a, (uint64_t)g.kbytes, (uint64_t)g.Np, kBM) ||
+      !encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
+      !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
     e = cudaErrorInvalidValue;
     return fail("cuTensorMapEncodeTiled");
   }
@@ -256,6 +301,7 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   g.desc.pumps = g.pumps;
   g.desc.n = g.n;
   g.desc.Kp = g.Kp;
+  g.desc.kbytes = g.kbytes;
   g.desc.R = g.R;
   g.desc.Rp = g.Rp;
   g.desc.xp = g.xp;
@@ -283,7 +329,7 @@ void Grouped::attach(GHost &g, int t0) {
 
 sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err) {
   GHost g;
-  sb_status s = prepare(g, p, prm, seed, tag, nr, st, stg_, err);
+  sb_status s = prepare(g, p, prm, seed, tag, nr, st, stg_, err, fp4);
   if (s != SB_OK) return s;
   attach(g, t0);
   return SB_OK;
@@ -295,7 +341,10 @@ sb_status Grouped::init_state(GHost &g, uint64_t seed, std::string &err) { retur
 sb_status Grouped::init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err) {
   cudaError_t e = launch_init_uniform(g.x, g.y, g.n, g.R, g.xp, seed, st);
   if (e == cudaSuccess) {
-    g_signs_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.Kp);
+    if (g.fp4)
+      g_signs_fp4_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.kbytes);
+    else
+      g_signs_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.Kp);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
@@ -314,7 +363,7 @@ sb_status Grouped::retile(int new_nr, std::string &err) {
     cudaFreeAsync(g.v[1], st);
     g.v[0] = g.v[1] = nullptr;
     g.Rp = (g.R + nr - 1) / nr * nr;
-    const size_t vb = (size_t)g.Rp * g.Kp;
+    const size_t vb = (size_t)g.Rp * g.kbytes;
     cudaError_t e;
     if ((e = cudaMallocAsync(&g.v[0], vb, st)) != cudaSuccess || (e = cudaMallocAsync(&g.v[1], vb, st)) != cudaSuccess) {
       err = "cudaMalloc(V)";
@@ -322,8 +371,8 @@ sb_status Grouped::retile(int new_nr, std::string &err) {
     }
     cudaMemsetAsync(g.v[0], 0, vb, st);
     cudaMemsetAsync(g.v[1], 0, vb, st);
-    if (!encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr) ||
-        !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.Kp, (uint64_t)g.Rp, (uint32_t)nr)) {
+    if (!encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
+        !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
       err = "cuTensorMapEncodeTiled";
       return SB_ERR_CUDA;
     }
@@ -359,7 +408,7 @@ sb_status Grouped::sync_tables(std::string &err) {
     descs[i] = insts[i].desc;
     const GHost &g = insts[i];
     for (int m0 = 0; m0 < g.Np; m0 += kBM)
-      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{(int)i, m0, r0, g.Kp / kChunkBytes});
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{(int)i, m0, r0, g.kbytes / kChunkBytes});
   }
   if (order == 0) {
     // longest first, dealt round-robin to the persistent CTAs
@@ -407,7 +456,7 @@ cudaError_t Grouped::launch(int tick, int emode) { return launch_items(d_items, 
 cudaError_t Grouped::launch_items(const GItem *items_ptr, int count, int tick, int emode) {
   const void *k = nullptr;
   size_t smem = 0;
-  if (!grouped_kernel_for(nr, emode, &k, &smem)) return cudaErrorInvalidValue;
+  if (!grouped_kernel_for(nr, emode, fp4, &k, &smem)) return cudaErrorInvalidValue;
   static std::mutex mu;
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -444,7 +493,7 @@ cudaError_t Grouped::run_steps(int tick0, int count, bool use_graph) {
     // kernel attributes are set before the capture starts
     const void *k = nullptr;
     size_t smem = 0;
-    grouped_kernel_for(nr, kEmodeStep, &k, &smem);
+    grouped_kernel_for(nr, kEmodeStep, fp4, &k, &smem);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -485,7 +534,7 @@ cudaError_t Grouped::energy_pass_for(const std::vector<int> &idx, int tick) {
     cudaError_t e = cudaMemsetAsync(g.energy, 0, (size_t)g.R * sizeof(double), st);
     if (e != cudaSuccess) return e;
     for (int m0 = 0; m0 < g.Np; m0 += kBM)
-      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{i, m0, r0, g.Kp / kChunkBytes});
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{i, m0, r0, g.kbytes / kChunkBytes});
   }
   if (items.empty()) return cudaSuccess;
   if ((int)items.size() > cap_sub) {
@@ -515,13 +564,14 @@ std::string Grouped::tune_key() const {
   int64_t chunks = 0;
   int rmax = 0;
   for (const auto &g : insts) {
-    chunks += (int64_t)(g.Np / kBM) * (g.Kp / kChunkBytes);
+    chunks += (int64_t)(g.Np / kBM) * (g.kbytes / kChunkBytes);
     rmax = std::max(rmax, g.R);
   }
   // bucket by total work (log2) and replica count
   int b = 0;
   while ((int64_t(1) << b) < chunks) ++b;
-  return std::to_string(rmax) + ":" + std::to_string(b) + ":" + std::to_string(insts.size() > 64 ? 2 : insts.size() > 8 ? 1 : 0);
+  return std::to_string(rmax) + ":" + std::to_string(b) + ":" + std::to_string(insts.size() > 64 ? 2 : insts.size() > 8 ? 1 : 0) +
+         (fp4 ? ":e2m1" : ":e4m3");
 }
 
 std::vector<std::pair<int, int>> Grouped::candidates(int R) {

@@ -17,13 +17,16 @@
 // different times advance side by side (continuous batching). Every wait is bounded.
 #pragma once
 #include "sb_grouped.h"
+#include "sb_tc_fp4.cuh"
 #include "sb_tc_kernel.cuh"
 
 namespace sbk {
 
 namespace tck {
 
-template <int NR, int STAGES, int EMODE>
+// FP4: packed E2M1 operands (kind::mxf4, every block scale 1.0 in TMEM columns [2NR, 2NR + 32)),
+// a 128-byte chunk holding 256 spins of K; V written as nibble pairs (spin 2s low, 2s + 1 high).
+template <int NR, int STAGES, int EMODE, bool FP4>
 __global__ void __launch_bounds__(kTcThreads, 1)
     grouped_kernel(const GInst *__restrict__ insts, const GItem *__restrict__ items, int n_items, int tick,
                    uint32_t *status) {
@@ -32,8 +35,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr int kBTile = NR * kChunkBytes;
   constexpr int kStage = kATile + kBTile;
   constexpr uint32_t kTx = (uint32_t)kStage;
-  constexpr uint32_t kCols = 2 * NR <= 32 ? 32 : (2 * NR <= 64 ? 64 : (2 * NR <= 128 ? 128 : 256));
-  constexpr uint32_t kIdesc = make_idesc(kTcFp8, kBM, NR);
+  constexpr uint32_t kSf = 2 * NR;
+  constexpr uint32_t kNeed = FP4 ? 2 * NR + 32 : 2 * NR;
+  constexpr uint32_t kCols = kNeed <= 32 ? 32 : (kNeed <= 64 ? 64 : (kNeed <= 128 ? 128 : (kNeed <= 256 ? 256 : 512)));
+  constexpr uint32_t kIdesc = FP4 ? make_idesc_mxf4(kBM, NR) : make_idesc(kTcFp8, kBM, NR);
   constexpr int kHalf = NR / 2;
   constexpr bool kEOnly = EMODE == kEmodeEnergy;
   static_assert(NR == 32 || NR == 64 || NR == 128, "replica tile");
@@ -66,6 +71,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
+  if constexpr (FP4) {
+    if (warp >= 2) {
+      // every block scale = 2^0: UE8M0 0x7F in all bytes of the 32 scale columns, all 128 lanes
+      uint32_t ones[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) ones[j] = 0x7F7F7F7Fu;
+      ptx::tmem_st16(tmem + kSf + 16 * ((warp - 2) >> 2) + ((uint32_t)(32 * (warp & 3)) << 16), ones);
+      ptx::tmem_st_wait();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+  }
 
   if (warp == 0) {
     if (lane == 0) {
@@ -113,9 +131,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           ptx::tc_fence_after();
           const uint32_t sa = ptx::smem_u32(smem + s * kStage);
 #pragma unroll
-          for (int k = 0; k < C::kMmaPerChunk; ++k)
-            ptx::mma_f8(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sa + kATile + k * 32), kIdesc,
-                        (kc > 0 || k > 0) ? 1u : 0u);
+          for (int k = 0; k < C::kMmaPerChunk; ++k) {
+            const uint64_t ad = ptx::smem_desc_sw128(sa + k * 32), bd = ptx::smem_desc_sw128(sa + kATile + k * 32);
+            if constexpr (FP4)
+              ptx::mma_mxf4(t_acc, ad, bd, kIdesc, tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
+            else
+              ptx::mma_f8(t_acc, ad, bd, kIdesc, (kc > 0 || k > 0) ? 1u : 0u);
+          }
           ptx::mma_commit(&empty_bar[s]);
         }
         ptx::mma_commit(&accf_bar[ab]);
@@ -140,7 +162,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       ptx::tc_fence_after();
       const int t = tick - in->t0;
-      const int n = in->n, R = in->R, xp = in->xp, Kp = in->Kp;
+      const int n = in->n, R = in->R, xp = in->xp, kb = in->kbytes;
       const int row = w.m0 + 32 * q + lane;
       const float hv = (in->h && row < n) ? in->h[row] : 0.0f;
       const float pump = kEOnly ? 0.0f : in->pumps[t];
@@ -188,7 +210,31 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const size_t k = (size_t)r * xp + row;
               xs[k] = xv[j];
               ys[k] = yv[j];
-              vn[(size_t)r * Kp + row] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+              if constexpr (!FP4) vn[(size_t)r * kb + row] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+            }
+          }
+          if constexpr (FP4) {
+            // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte: the
+            // even lane writes replicas c..c+7, the odd lane c+8..c+15
+            uint32_t nib_lo = 0, nib_hi = 0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const bool ins = row < n && w.r0 + c + j < R;
+              const uint32_t nib = ins ? (xv[j] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+              if (j < 8) nib_lo |= nib << (4 * j);
+              else nib_hi |= nib << (4 * (j - 8));
+            }
+            const bool odd = (lane & 1) != 0;
+            const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
+            const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
+            const uint32_t lo_n = odd ? o_hi : nib_lo, hi_n = odd ? nib_hi : o_lo;
+            const int row_e = row & ~1;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int r = w.r0 + c + (odd ? 8 : 0) + j;
+              if (row_e < n && r < R)
+                vn[(size_t)r * kb + (row_e >> 1)] =
+                    (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
             }
           }
         }

@@ -25,7 +25,7 @@ struct alignas(64) GInst {
   int n, Kp, R, Rp, xp;
   int t0;                // the instance's step t = tick - t0
   float c0, dt, dta0;
-  int pad_;
+  int kbytes;            // bytes of one operand row: Kp (FP8) or Kp / 2 (packed E2M1)
 };
 
 // One work item: a 128-spin x NR-replica tile of one instance.
@@ -35,13 +35,17 @@ struct GItem {
 
 // dSB with integer |J| <= 16 (exact FP8 operands) and n * 16 < 2^24 (exact FP32 accumulation).
 bool grouped_supports(const sb_problem *p, const sb_params *prm);
+// ... and integer |J| <= 4: exact as packed E2M1 operands (half the bytes of FP8)
+bool grouped_fp4_exact(const sb_problem *p);
 // device bytes one instance holds while resident
-int64_t grouped_instance_bytes(int n, int R, int steps, int nr);
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr, bool fp4 = false);
 
 struct GHost {
   int tag = 0;                  // caller's index / ticket
   const sb_problem *prob = nullptr;
   int n = 0, R = 0, steps = 0, t0 = 0, Np = 0, Kp = 0, Rp = 0, xp = 0;
+  int kbytes = 0;  // operand row bytes (Kp, or Kp / 2 for packed E2M1)
+  bool fp4 = false;
   float c0 = 0, dt = 0, dta0 = 0;
   uint64_t seed = 0;
   uint8_t *a = nullptr, *v[2] = {nullptr, nullptr};
@@ -61,14 +65,16 @@ struct Staging {
 
 class Grouped {
  public:
-  explicit Grouped(cudaStream_t s, int replica_tile, int item_order) : st(s), nr(replica_tile), order(item_order) {}
+  // fp4: every instance's couplings are integers |J| <= 4, held as packed E2M1 (else FP8 E4M3)
+  explicit Grouped(cudaStream_t s, int replica_tile, int item_order, bool fp4_operands = false)
+      : st(s), nr(replica_tile), order(item_order), fp4(fp4_operands) {}
   ~Grouped();
   // Uploads p (host), converts J to FP8, seeds the state. t0: the tick at which its step 0 runs.
   sb_status add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err);
   // The two halves of add: prepare builds a complete instance on stream `st` (any thread; memory
   // from the stream-ordered pool), attach makes it resident from tick t0 (the engine's thread).
   static sb_status prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
-                           cudaStream_t st, Staging &stg, std::string &err);
+                           cudaStream_t st, Staging &stg, std::string &err, bool fp4 = false);
   void attach(GHost &g, int t0);
   static void release(GHost &g, cudaStream_t s);
   static sb_status init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err);
@@ -102,6 +108,7 @@ class Grouped {
 
   cudaStream_t st;
   int nr, order;
+  bool fp4;
   std::vector<GHost> insts;
   int64_t launches = 0;
   int n_items = 0;

@@ -375,7 +375,9 @@ def run_batch(args, rank, world, local_rank):
     n_sum = sum(p.n for p in probs)
     stream = torch.cuda.current_stream(dev)
     ctx = sb.Context(local_rank, stream=stream.cuda_stream)
-    prm = sb.Params.default(sb.DSB, steps=sb_steps, replicas=R, seed=1234 + 1000 * rank, field_mode=sb.FIELD_TC)
+    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16}[args.operand]
+    prm = sb.Params.default(sb.DSB, steps=sb_steps, replicas=R, seed=1234 + 1000 * rank, field_mode=sb.FIELD_TC,
+                            operand_dtype=odt)
     t0 = time.perf_counter()
     batch = ctx.batch(probs, prm)
     setup_s = time.perf_counter() - t0
@@ -407,18 +409,24 @@ def run_batch(args, rank, world, local_rank):
     updates = float(n_sum) * R * sb_steps
     value = weak_scaling_value(updates, world, args.steps, total_ms)
     # roofline: one profiled run, event pair around every grouped step launch
-    prm_p = sb.Params.default(sb.DSB, steps=24, replicas=R, seed=7, field_mode=sb.FIELD_TC, profile=1)
+    prm_p = sb.Params.default(sb.DSB, steps=24, replicas=R, seed=7, field_mode=sb.FIELD_TC, profile=1,
+                              operand_dtype=odt)
     bp = ctx.batch(probs, prm_p)
     bp.run()
     rp = bp.run(seed=8)
     bp.close()
     hbm, bf16, src = peaks()
-    np_kp = sum(((p.n + 127) // 128 * 128) ** 2 for p in probs)
-    bytes_per_launch = np_kp + sum(p.n for p in probs) * R * 17.0  # FP8 J + (x, y in/out, next operand)
+    fp4 = rp[0].field_dtype == "fp4e2m1"
+    # couplings as stored on the device: FP8 [Np][Np], or E2M1 pairs [Np][Kp / 2] with Kp = N rounded to 256
+    np_kp = sum(((p.n + 127) // 128 * 128) * (((p.n + 255) // 256 * 128) if fp4 else ((p.n + 127) // 128 * 128))
+                for p in probs)
+    # J + per spin-replica: x, y read and written (16 B) and the next sign operand (1 B, or 1/2)
+    bytes_per_launch = np_kp + sum(p.n for p in probs) * R * (16.5 if fp4 else 17.0)
     achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": NCU_TRAFFIC["uneven-batch"][0] * bytes_per_launch,
-            "traffic_source": NCU_TRAFFIC["uneven-batch"][1] + " (48-instance capture, scaled by algorithmic bytes)",
+            "traffic": NCU_TRAFFIC["uneven-batch"][0] * bytes_per_launch if not fp4 else None,
+            "traffic_source": NCU_TRAFFIC["uneven-batch"][1] + " (48-instance capture, scaled by algorithmic bytes)"
+            if not fp4 else None,
             "kernel": "grouped_kernel (one launch per SB step)",
             "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
             "peak_source": f"{src} HBM copy"}
@@ -436,13 +444,14 @@ def run_batch(args, rank, world, local_rank):
         "metric": "SB spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp8e4m3 field (f32 accumulate), f32 state", "data": "synthetic (seeded)",
+        "dtype": ("e2m1 x e2m1 field (f32 accumulate, exact for |J| <= 4), f32 state" if fp4
+                  else "fp8e4m3 field (f32 accumulate), f32 state"), "data": "synthetic (seeded)",
         "config": {"workload": desc, "instances": len(probs), "sum_n": n_sum, "replicas": R,
                    "sb_steps": sb_steps, "parallelism": f"replicas-only x{world}",
-                   "l2": f"inputs ({np_kp / 1e9:.2f} GB of FP8 J) "
+                   "l2": f"inputs ({np_kp / 1e9:.2f} GB of {'E2M1' if fp4 else 'FP8'} J) "
                    + ("larger than L2" if np_kp > 129e6 else "smaller than L2") + "; 256 MB flush between runs"},
         "e2e": {"value": world * updates * args.steps / (e2e_total * 1e-3), "unit": "spin-updates/s",
-                "h2d_bytes_per_step": int(sum(p.n * p.n * 4 for p in probs)),
+                "h2d_bytes_per_step": int(np_kp),  # couplings packed on the host, then copied
                 "d2h_bytes_per_step": int(sum(p.n + 8 * R for p in probs)),
                 "ms_per_step": e2e_total / args.steps},
         "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary(),
@@ -521,7 +530,8 @@ def run_serving(args, rank, world, local_rank):
         "quality": {"energy_check_ok": all(r.energy_check_ok for r in results)},
         "clocks": clk.summary(),
         "e2e": {"value": updates / makespan, "unit": "spin-updates/s",
-                "h2d_bytes_per_step": int(np.mean([p.n * p.n * 4 for _, p, _ in reqs])),
+                # couplings packed to FP8 on the host before the copy
+                "h2d_bytes_per_step": int(np.mean([((p.n + 127) // 128 * 128) ** 2 for _, p, _ in reqs])),
                 "d2h_bytes_per_step": int(np.mean([p.n + 8 * R for _, p, _ in reqs]))},
     }
     print(json.dumps(line), flush=True)

@@ -1,4 +1,7 @@
-"""Grouped tensor-core batches (sb_batch_*): every instance bit-exact against the CPU oracle."""
+"""Grouped tensor-core batches (sb_batch_*): every instance bit-exact against the CPU oracle.
+
+Batches whose couplings are all integers |J| <= 4 run packed E2M1 operands; others FP8 E4M3.
+"""
 import numpy as np
 import pytest
 
@@ -18,15 +21,19 @@ def make_instances(ns, jmax=4, with_h=(2,)):
     return out
 
 
-@pytest.mark.parametrize("R", [64, 32, 100])
-def test_batch_matches_oracle(ctx, R):
-    ns = [64, 100, 129, 300, 513, 1000]
-    insts = make_instances(ns)
+@pytest.mark.parametrize("R,jmax,dtype", [(64, 4, "fp4e2m1"), (32, 4, "fp4e2m1"), (100, 4, "fp4e2m1"),
+                                          (64, 4, "fp8e4m3"), (100, 16, "fp8e4m3"), (32, 1, "fp4e2m1")])
+def test_batch_matches_oracle(ctx, R, jmax, dtype):
+    # odd sizes: a last E2M1 byte with one spin, padded K chunks, partial spin and replica tiles
+    ns = [64, 100, 129, 301, 513, 1000]
+    insts = make_instances(ns, jmax=jmax)
     probs = [sb.Problem.from_dense(J, h) for J, h in insts]
     steps, seed = 30, 100
-    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
+    odt = sb.OPERAND_FP8 if (dtype == "fp8e4m3" and jmax <= 4) else sb.OPERAND_AUTO
+    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC, operand_dtype=odt)
     batch = ctx.batch(probs, prm, want_state=True)
     res = batch.run()
+    assert all(r.field_dtype == dtype for r in res)
     for k, ((J, h), p, r) in enumerate(zip(insts, probs, res)):
         x, y = orc.init_uniform(J.shape[0], R, seed + k)
         orc.sb_run_f32(2, J, h, x, y, steps, 1.0, p.default_c0(), 1.25)
