@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <map>
 #include <mutex>
@@ -141,13 +142,62 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     err = "cudaEventCreate";
     return SB_ERR_CUDA;
   }
+  // Instances are prepared (packed on the host, uploaded, seeded) by several threads, each with its
+  // own stream and pinned staging buffer, then made resident in order.
+  std::vector<sbk::GHost> hosts(count);
+  std::vector<sb_status> sts(count, SB_OK);
+  const int nw = std::min(count, 8);
+  std::vector<std::string> errs(nw);
+  std::atomic<int> next{0};
+  std::atomic<bool> failed{false};
+  const int nr = b->g->nr;
+  auto worker = [&](int w) {
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+      errs[w] = "cudaSetDevice";
+      failed = true;
+      return;
+    }
+    cudaStream_t ps = nullptr;
+    if (cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) != cudaSuccess) {
+      errs[w] = "cudaStreamCreate";
+      failed = true;
+      return;
+    }
+    {
+      sbk::Staging stg;
+      for (int k; !failed.load() && (k = next.fetch_add(1)) < count;) {
+        const sb_status st = sbk::Grouped::prepare(hosts[k], &problems[k], prm, prm->seed + k, k, nr, ps, stg, errs[w], fp4);
+        if (st != SB_OK) {
+          sts[k] = st;
+          failed = true;
+        }
+      }
+      cudaStreamSynchronize(ps);  // before the staging buffer is freed
+    }
+    cudaStreamDestroy(ps);
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < nw; ++w) th.emplace_back(worker, w);
+  for (auto &t : th) t.join();
+  if (failed.load()) {
+    sb_status first = SB_ERR_CUDA;
+    for (int k = 0; k < count; ++k)
+      if (sts[k] != SB_OK) {
+        first = sts[k];
+        break;
+      }
+    for (int w = 0; w < nw; ++w)
+      if (!errs[w].empty()) {
+        err = errs[w];
+        break;
+      }
+    for (auto &h : hosts) sbk::Grouped::release(h, ctx->stream);
+    destroy(b);
+    return first;
+  }
   for (int k = 0; k < count; ++k) {
     b->probs[k] = &problems[k];
-    sb_status s = b->g->add(&problems[k], prm, prm->seed + k, 0, k, err);
-    if (s != SB_OK) {
-      destroy(b);
-      return s;
-    }
+    b->g->attach(hosts[k], 0);
   }
   sb_status s = autotune(b, err);
   if (s == SB_OK) s = b->g->sync_tables(err);
