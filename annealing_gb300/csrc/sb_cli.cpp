@@ -4,7 +4,10 @@
 // With no options it runs what m2_opt.cu runs: aSB, STEP = 100, one trial (TIMES = 1), the
 // reference's xorshift initial state, xi = 0.01565, and writes output.txt with one energy per trial
 // (m2_opt.cu:206-210). Options select bSB / dSB, replicas, schedule and field precision, and add
-// best_spins.txt (one +1/-1 per line) and a JSON summary on stdout.
+// best_spins.txt (one +1/-1 per line) and a JSON summary on stdout. --target E adds the
+// time-to-target summary of the run's replica traces (plot_energy_decrease/plot.r:88-240,
+// SA_naive/CUDA_GPU/tests/test.sh:26-32).
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -22,6 +25,7 @@ static void usage() {
       "             [--field auto|fp32|tc] [--init uniform|reference]\n"
       "             [--n N] [--index-base 0|1] [--strict] [--trace] [--device D]\n"
       "             [--out output.txt] [--spins best_spins.txt] [--json]\n"
+      "             [--target E [--p-target P]]\n"
       "Graph file: N [E] then lines 'i j J_ij' (i != j) and optional 'i i h_i'.\n");
 }
 
@@ -32,7 +36,8 @@ int main(int argc, char **argv) {
   }
   const char *path = nullptr;
   std::string out_path = "output.txt", spins_path = "best_spins.txt";
-  bool json = false;
+  bool json = false, have_target = false;
+  double target = 0.0, p_target = 0.99;
   int device = 0;
   sb_graph_opts go;
   sb_graph_opts_default(&go);
@@ -76,6 +81,10 @@ int main(int argc, char **argv) {
     else if (!strcmp(a, "--out")) out_path = next();
     else if (!strcmp(a, "--spins")) spins_path = next();
     else if (!strcmp(a, "--json")) json = true;
+    else if (!strcmp(a, "--target")) {
+      target = atof(next());
+      have_target = true;
+    } else if (!strcmp(a, "--p-target")) p_target = atof(next());
     else if (!strcmp(a, "-h") || !strcmp(a, "--help")) {
       usage();
       return 0;
@@ -107,11 +116,14 @@ int main(int argc, char **argv) {
   std::vector<int8_t> spins((size_t)prob.n);
   std::vector<double> energies((size_t)p.replicas);
   std::vector<double> trace(p.trace ? (size_t)p.steps + 1 : 0);
+  if (have_target) p.trace_all = 1;
+  std::vector<double> trace_all(have_target ? ((size_t)p.steps + 1) * (size_t)p.replicas : 0);
   sb_result r;
   memset(&r, 0, sizeof(r));
   r.best_spins = spins.data();
   r.replica_energies = energies.data();
   r.energy_trace = p.trace ? trace.data() : nullptr;
+  r.energy_trace_all = have_target ? trace_all.data() : nullptr;
   s = sb_solve(ctx, &prob, &p, &r);
   if (s != SB_OK) {
     fprintf(stderr, "sb: solve failed: %s (%s)\n", sb_status_string(s), sb_last_error(ctx));
@@ -135,6 +147,35 @@ int main(int argc, char **argv) {
   if (f) {
     for (int i = 0; i < prob.n; ++i) fprintf(f, "%d\n", (int)spins[i]);
     fclose(f);
+  }
+  // every replica is one run; row t of its trace is reached at t / steps of the device time
+  sb_tts tts;
+  memset(&tts, 0, sizeof(tts));
+  if (have_target) {
+    std::vector<double> times((size_t)p.steps + 1);
+    for (int t = 0; t <= p.steps; ++t) times[t] = p.steps > 0 ? r.device_ms * t / p.steps : 0.0;
+    s = sb_time_to_target(trace_all.data(), times.data(), p.steps + 1, p.replicas, 0, target, r.device_ms,
+                          p_target, &tts);
+    if (s != SB_OK) {
+      fprintf(stderr, "sb: time to target: %s (%s)\n", sb_status_string(s), sb_last_error(nullptr));
+      have_target = false;
+    }
+  }
+  auto num = [](double v) -> std::string {
+    char b[64];
+    if (isnan(v)) return "null";
+    if (isinf(v)) return v > 0 ? "\"inf\"" : "\"-inf\"";
+    snprintf(b, sizeof(b), "%.9g", v);
+    return b;
+  };
+  if (have_target) {
+    const std::string line =
+        "{\"target\": " + num(target) + ", \"p_target\": " + num(p_target) + ", \"trials\": " +
+        std::to_string(tts.trials) + ", \"reached\": " + std::to_string(tts.reached) + ", \"best_ms\": " +
+        num(tts.best_ms) + ", \"mean_ms\": " + num(tts.mean_ms) + ", \"worst_ms\": " + num(tts.worst_ms) +
+        ", \"succeeded\": " + std::to_string(tts.succeeded) + ", \"success_rate\": " + num(tts.success_rate) +
+        ", \"tts_ms\": " + num(tts.tts_ms) + "}";
+    printf("time_to_target %s\n", line.c_str());
   }
   if (json) {
     printf(

@@ -96,20 +96,59 @@ float sb_default_c0(const sb_problem *p) {
 sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out) {
   if (!p || !p->J || !spins || !out || p->n <= 0) return SB_ERR_INVALID_ARG;
   const int n = p->n;
+  if (p->h)
+    for (int i = 0; i < n; ++i)
+      if (p->h[i] != floorf(p->h[i]) || !(fabsf(p->h[i]) < 9.0e18f)) return SB_ERR_UNSUPPORTED;
+  // A problem scanned on creation (sb_problem_init / wrap / load / random) carries its
+  // integrality and max |J|: the couplings need no per-element test, and when n * max|J| stays
+  // below 2^31 every row sum is exact in int32, which the compiler vectorises. Otherwise each
+  // coupling is tested and the products are summed in int64.
+  const bool scanned = p->integer_valued != 0;
+  const bool row32 = scanned && p->max_abs_j < 2000000000 && (double)p->max_abs_j * (double)n < 2147483647.0;
+  // rows [i0, i1) step `stride` of the upper triangle; false on a non-integral coupling
+  auto rows = [&](int i0, int stride, int64_t &sum) -> bool {
+    int64_t e = 0;
+    for (int i = i0; i < n; i += stride) {
+      const float *Ji = p->J + (size_t)i * n;
+      int64_t row = 0;
+      if (row32) {
+        int32_t acc = 0;
+        for (int j = i + 1; j < n; ++j) {
+          const int32_t w = (int32_t)Ji[j];
+          const int32_t m = (int32_t)spins[j] >> 1;  // 0 for +1, -1 for -1
+          acc += (w ^ m) - m;
+        }
+        row = acc;
+      } else {
+        for (int j = i + 1; j < n; ++j) {
+          const float w = Ji[j];
+          if (w != floorf(w) || !(fabsf(w) < 9.0e18f)) return false;
+          row += (int64_t)w * (int64_t)spins[j];
+        }
+      }
+      e -= row * (int64_t)spins[i];
+      if (p->h) e -= (int64_t)p->h[i] * (int64_t)spins[i];
+    }
+    sum = e;
+    return true;
+  };
+  // large problems: rows dealt round-robin to host threads (the triangle stays balanced); the
+  // integer sum does not depend on the split
+  const int nt = n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+  std::vector<int64_t> part((size_t)nt, 0);
+  std::vector<char> ok((size_t)nt, 1);
+  if (nt == 1) {
+    ok[0] = rows(0, 1, part[0]);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back([&, t] { ok[t] = rows(t, nt, part[t]); });
+    ok[0] = rows(0, nt, part[0]);
+    for (auto &x : th) x.join();
+  }
   int64_t e = 0;
-  for (int i = 0; i < n; ++i) {
-    const float *Ji = p->J + (size_t)i * n;
-    int64_t row = 0;
-    for (int j = i + 1; j < n; ++j) {
-      const float w = Ji[j];
-      if (w != floorf(w)) return SB_ERR_UNSUPPORTED;
-      row += (int64_t)w * (int64_t)spins[j];
-    }
-    e -= row * (int64_t)spins[i];
-    if (p->h) {
-      if (p->h[i] != floorf(p->h[i])) return SB_ERR_UNSUPPORTED;
-      e -= (int64_t)p->h[i] * (int64_t)spins[i];
-    }
+  for (int t = 0; t < nt; ++t) {
+    if (!ok[t]) return SB_ERR_UNSUPPORTED;
+    e += part[t];
   }
   *out = e;
   return SB_OK;

@@ -124,6 +124,19 @@ class ServingStats(C.Structure):
     ]
 
 
+class TtsStruct(C.Structure):
+    _fields_ = [
+        ("trials", C.c_int32),
+        ("reached", C.c_int32),
+        ("succeeded", C.c_int32),
+        ("best_ms", C.c_double),
+        ("mean_ms", C.c_double),
+        ("worst_ms", C.c_double),
+        ("success_rate", C.c_double),
+        ("tts_ms", C.c_double),
+    ]
+
+
 # Every symbol include/sb.h declares, with its ctypes signature.
 _SIGS = {
     "sb_status_string": (C.c_char_p, [C.c_int]),
@@ -144,6 +157,8 @@ _SIGS = {
     "sb_energy_i64": (C.c_int, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8),
                                 C.POINTER(C.c_int64)]),
     "sb_energy_f64": (C.c_double, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8)]),
+    "sb_time_to_target": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_double, C.c_double, C.c_double, C.POINTER(TtsStruct)]),
     "sb_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(DeviceOpts)]),
     "sb_destroy": (C.c_int, [C.c_void_p]),
     "sb_last_error": (C.c_char_p, [C.c_void_p]),
@@ -456,3 +471,47 @@ class Context:
 
 def pump(a0: float, t: int, steps: int) -> float:
     return lib().sb_pump(a0, t, steps)
+
+
+def time_to_target(energies: np.ndarray, times_ms: np.ndarray, threshold: float, run_ms: float,
+                   p_target: float = 0.99) -> dict:
+    """Time-to-target summary of an energy trace (sb_time_to_target).
+
+    energies: [rows, trials] (a Result's energy_trace_all, row = step). times_ms: [rows] (time at
+    which each row was reached, shared by replicas that run together) or [rows, trials]. run_ms:
+    the time of one run, used for the success-probability time.
+    """
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+    if e.ndim != 2:
+        raise ValueError("energies must be [rows, trials]")
+    t = np.ascontiguousarray(times_ms, dtype=np.float64)
+    per_trial = 1 if t.ndim == 2 else 0
+    if t.shape != (e.shape if per_trial else (e.shape[0],)):
+        raise ValueError("times_ms must be [rows] or [rows, trials]")
+    out = TtsStruct()
+    dp = C.POINTER(C.c_double)
+    _check(lib().sb_time_to_target(e.ctypes.data_as(dp), t.ctypes.data_as(dp), e.shape[0], e.shape[1],
+                                   per_trial, threshold, run_ms, p_target, C.byref(out)))
+    return {k: getattr(out, k) for k, _ in TtsStruct._fields_}
+
+
+def success_threshold(final_energies: np.ndarray, divisor: int = 5) -> float:
+    """Success cut of SA_naive/CUDA_GPU/tests/test.sh:26-28: the best energy plus 1/divisor of
+    the spread between the worst and the best (divisor 5: "80% --> success"). Integer energies use
+    the script's integer division."""
+    e = np.asarray(final_energies, dtype=np.float64)
+    small, big = float(e.min()), float(e.max())
+    if np.all(e == np.round(e)):
+        return small + float(int(big - small) // divisor)
+    return small + (big - small) / divisor
+
+
+def result_time_to_target(res: "Result", threshold: float, p_target: float = 0.99) -> dict:
+    """time_to_target of a solve's energy_trace_all: row t is reached at t / steps of the solve's
+    device time, every replica is a run and the run time is the solve's device time."""
+    if res.energy_trace_all is None:
+        raise ValueError("solve with trace_all=1 to get per-replica traces")
+    rows = res.energy_trace_all.shape[0]
+    steps = max(rows - 1, 1)
+    times = np.arange(rows, dtype=np.float64) * (res.device_ms / steps)
+    return time_to_target(res.energy_trace_all, times, threshold, res.device_ms, p_target)

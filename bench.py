@@ -38,7 +38,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (variant, n, replicas, sb_steps, field, description)
     "batched-dsb": ("dsb", 2000, 1024, 2000, "tc",
-                    "batched dSB: complete N=2000, J iid +-1, R=1024, 2000 steps, FP8 tensor-core field"),
+                    "batched dSB: complete N=2000, J iid +-1, R=1024, 2000 steps, tensor-core field "
+                    "(packed E2M1 operands; FP8 with --operand fp8)"),
     "plain-dsb": ("dsb", 2000, 1, 1000, "fp32",
                   "plain dSB: complete N=2000, J iid +-1, R=1, 1000 steps, fused FP32 kernel"),
     "batched-bsb": ("bsb", 8192, 256, 3000, "tc",

@@ -13,6 +13,9 @@
  *                   <- the host energy loop                  SB/CUDA_GPU/m2_opt.cu:192-202
  *   sb_params.trace <- print_energy (per-step energy trace)  SB/CUDA_GPU/m2_opt.cu:77-91
  *                      (filled into sb_result.energy_trace)
+ *   sb_time_to_target
+ *                   <- the trace analysis of plot_energy_decrease/plot.r:88-240 and the
+ *                      success-probability time of SA_naive/CUDA_GPU/tests/test.sh:26-32
  *   sb_create / sb_destroy
  *                   <- cublasCreate + the cudaMalloc block   SB/CUDA_GPU/m2_opt.cu:106-145
  *
@@ -212,6 +215,30 @@ float sb_pump(float a0, int32_t t, int32_t steps);
 /* exact energies: int64 when every J, h is integral (else SB_ERR_UNSUPPORTED), double otherwise */
 sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out);
 double sb_energy_f64(const sb_problem *p, const int8_t *spins);
+
+/* ---- time to target (host only, no GPU needed) ----
+ * Replaces the reference's trace analysis: per trial, the first time its energy trace goes below
+ * a target, summarised over the trials that reach it (SB/CUDA_GPU/plot_figure/
+ * plot_energy_decrease/plot.r:88-240), and the time to reach the target with probability P from
+ * the success rate p_s of single runs, run_ms * ln(1 - P) / ln(1 - p_s)
+ * (SA_naive/CUDA_GPU/tests/test.sh:26-32). energies is laid out as sb_result.energy_trace_all:
+ * [rows * trials], row-major (row = step 0..steps); times_ms holds the time at which each row was
+ * reached, [rows] shared by all trials (times_per_trial = 0, replicas run together) or
+ * [rows * trials] (1, trials run one after another). "Below" is strict, as in both scripts. */
+typedef struct sb_tts {
+  int32_t trials;
+  int32_t reached;      /* trials whose trace went below the target at some row */
+  int32_t succeeded;    /* trials whose final row is below the target (the success test) */
+  double best_ms;       /* first-passage time: least, mean and greatest over the trials that */
+  double mean_ms;       /* reached the target; NaN when none did */
+  double worst_ms;
+  double success_rate;  /* succeeded / trials */
+  double tts_ms;        /* run_ms * ln(1 - p_target) / ln(1 - success_rate); run_ms when the
+                           success rate is >= p_target; +inf when no trial succeeded */
+} sb_tts;
+sb_status sb_time_to_target(const double *energies, const double *times_ms, int32_t rows,
+                            int32_t trials, int32_t times_per_trial, double threshold,
+                            double run_ms, double p_target, sb_tts *out);
 
 /* ---- contexts ---- */
 sb_status sb_create(sb_ctx **out, const sb_device_opts *opts);

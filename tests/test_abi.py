@@ -1,6 +1,7 @@
 """C-ABI library: loads, exports what include/sb.h declares, host-side entry points (CPU only)."""
 import os
 import re
+import ctypes as C
 import subprocess
 
 import numpy as np
@@ -67,6 +68,29 @@ def test_energy_evaluators_match_oracle():
     pg = sb.Problem.from_dense(Jg, hg)
     assert not pg.integer_valued
     assert pg.energy(s[:80]) == orc.energy_f64(Jg, hg, s[:80])
+
+
+def test_exact_energy_paths():
+    """sb_energy_i64: the scanned int32-row path (threaded from n = 1024 on), the per-element
+    checked int64 path of a problem whose struct carries no scan, and its refusal of a real J."""
+    rng = np.random.default_rng(4)
+    for n, jmax in ((1500, 1), (1100, 16)):
+        J = instances.erdos_renyi(n, 0.7, n, jmax=jmax, allow_zero=True)
+        h = rng.integers(-3, 4, n).astype(np.float32)
+        s = (rng.integers(0, 2, n) * 2 - 1).astype(np.int8)
+        p = sb.Problem.from_dense(J, h)
+        ref = orc.energy_i64(J, h, s)
+        assert p.energy(s) == ref
+        p.s.integer_valued = 0  # as if the caller filled the struct by hand
+        out = C.c_int64()
+        assert lib().sb_energy_i64(C.byref(p.s), s.ctypes.data_as(C.POINTER(C.c_int8)), C.byref(out)) == 0
+        assert out.value == ref
+    J = instances.complete_pm1(1200, seed=2)
+    J[3, 700] = J[700, 3] = 0.5
+    p = sb.Problem.from_dense(J)
+    s = np.ones(1200, np.int8)
+    out = C.c_int64()
+    assert lib().sb_energy_i64(C.byref(p.s), s.ctypes.data_as(C.POINTER(C.c_int8)), C.byref(out)) == 6
 
 
 def test_graph_reader_reference_format(tmp_path):
