@@ -6,9 +6,10 @@ build (_build.py) and the synthetic instance generators (instances.py).
 """
 from .sb import (ASB, BSB, DSB, Batch, FIELD_AUTO, FIELD_FP32, FIELD_TC, INIT_REFERENCE, INIT_UNIFORM,
                  OPERAND_AUTO, OPERAND_BF16, OPERAND_BF16X2, OPERAND_FP4, OPERAND_FP8, Context, Params, Plan,
-                 Problem, Result, SBError, lib, pump, result_time_to_target, success_threshold,
-                 time_to_target)
+                 Problem, Result, SBError, SQA_RNG_HASH, SQA_RNG_REFERENCE, SqaParams, SqaResult, lib, pump,
+                 result_time_to_target, sqa_schedule, success_threshold, time_to_target)
 
 __all__ = ["ASB", "BSB", "DSB", "Batch", "FIELD_AUTO", "FIELD_FP32", "FIELD_TC", "INIT_REFERENCE",
            "INIT_UNIFORM", "OPERAND_AUTO", "OPERAND_BF16", "OPERAND_BF16X2", "OPERAND_FP4", "OPERAND_FP8", "Context", "Params", "Plan", "Problem", "Result", "SBError", "lib",
-           "pump", "result_time_to_target", "success_threshold", "time_to_target"]
+           "pump", "result_time_to_target", "SQA_RNG_HASH", "SQA_RNG_REFERENCE", "SqaParams", "SqaResult",
+           "sqa_schedule", "success_threshold", "time_to_target"]

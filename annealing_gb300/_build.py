@@ -21,7 +21,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["sb_plain.cu", "sb_tc.cu", "sb_tc_fp8.cu", "sb_tc_bf16.cu", "sb_tc_split.cu", "sb_tc_fp4.cu", "sb_grouped.cu", "sb_noalloc.cu",
-               "sb_api.cpp", "sb_batch.cpp", "sb_problem.cpp", "sb_serve.cpp", "sb_analysis.cpp"]
+               "sb_api.cpp", "sb_batch.cpp", "sb_problem.cpp", "sb_serve.cpp", "sb_analysis.cpp", "sb_sqa.cu"]
 
 
 def _nvcc() -> str:
@@ -85,8 +85,10 @@ def build_oracle(force: bool = False) -> str:
     os.makedirs(out_dir, exist_ok=True)
     exact = os.path.join(ORACLE, "sb_oracle.c")
     base = os.path.join(ORACLE, "sb_cpu_baseline.c")
+    sqa = os.path.join(ORACLE, "sqa_oracle.c")
     o1 = os.path.join(out_dir, "sb_oracle.o")
     o2 = os.path.join(out_dir, "sb_cpu_baseline.o")
+    o3 = os.path.join(out_dir, "sqa_oracle.o")
     lib = os.path.join(ORACLE, "libsboracle.so")
     jobs = []
     if force or not _newer(o1, [exact]):
@@ -95,11 +97,14 @@ def build_oracle(force: bool = False) -> str:
     if force or not _newer(o2, [base]):
         jobs.append(["gcc", "-O3", "-std=gnu11", "-fPIC", "-ffp-contract=fast", "-pthread",
                      "-c", base, "-o", o2])
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    if force or not _newer(o3, [sqa]):
+        jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                     "-c", sqa, "-o", o3])
+    with ThreadPoolExecutor(max_workers=3) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
     if force or jobs or not os.path.exists(lib):
-        _run(["gcc", "-shared", "-o", lib, o1, o2, "-lm", "-pthread"])
+        _run(["gcc", "-shared", "-o", lib, o1, o2, o3, "-lm", "-pthread"])
     return lib
 
 

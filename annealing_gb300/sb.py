@@ -124,6 +124,63 @@ class ServingStats(C.Structure):
     ]
 
 
+SQA_RNG_REFERENCE, SQA_RNG_HASH = 0, 1
+
+
+class SqaParams(C.Structure):
+    _fields_ = [
+        ("trotter", C.c_int32),
+        ("steps", C.c_int32),
+        ("replicas", C.c_int32),
+        ("rng_mode", C.c_int32),
+        ("seed", C.c_uint64),
+        ("trace", C.c_int32),
+    ]
+
+    @classmethod
+    def default(cls, **kw) -> "SqaParams":
+        p = cls()
+        lib().sb_sqa_params_default(C.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+
+class SqaResultStruct(C.Structure):
+    _fields_ = [
+        ("best_spins", C.POINTER(C.c_int8)),
+        ("replica_energies", C.POINTER(C.c_double)),
+        ("energy_trace", C.POINTER(C.c_double)),
+        ("final_spins", C.POINTER(C.c_int8)),
+        ("best_energy", C.c_double),
+        ("best_energy_i64", C.c_int64),
+        ("best_replica", C.c_int32),
+        ("energy_check_ok", C.c_int32),
+        ("device_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("spin_updates_per_s", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+
+@dataclass
+class SqaResult:
+    best_spins: np.ndarray
+    replica_energies: np.ndarray
+    best_energy: float
+    best_energy_i64: int
+    best_replica: int
+    energy_check_ok: bool
+    device_ms: float
+    total_ms: float
+    spin_updates_per_s: float
+    kernel_launches: int
+    energy_trace: Optional[np.ndarray] = None   # [replicas, steps]
+    final_spins: Optional[np.ndarray] = None    # [replicas, trotter, n]
+
+
 class TtsStruct(C.Structure):
     _fields_ = [
         ("trials", C.c_int32),
@@ -157,6 +214,10 @@ _SIGS = {
     "sb_energy_i64": (C.c_int, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8),
                                 C.POINTER(C.c_int64)]),
     "sb_energy_f64": (C.c_double, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8)]),
+    "sb_sqa_params_default": (None, [C.POINTER(SqaParams)]),
+    "sb_sqa_schedule": (None, [C.c_int32, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "sb_sqa_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(SqaParams),
+                               C.POINTER(SqaResultStruct)]),
     "sb_time_to_target": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32, C.c_int32,
                                     C.c_int32, C.c_double, C.c_double, C.c_double, C.POINTER(TtsStruct)]),
     "sb_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(DeviceOpts)]),
@@ -429,6 +490,27 @@ class Context:
         _check(lib().sb_solve(self.h, C.byref(problem.s), C.byref(params), C.byref(buf.r)), self.h)
         return buf.result()
 
+    def sqa_solve(self, problem: Problem, params: SqaParams, want_spins: bool = False) -> SqaResult:
+        """Simulated quantum annealing (sb_sqa_solve)."""
+        n, R, M, T = problem.n, params.replicas, params.trotter, params.steps
+        spins = np.zeros(n, np.int8)
+        energies = np.zeros(R, np.float64)
+        trace = np.zeros((R, T), np.float64) if params.trace else None
+        allsp = np.zeros((R, M, n), np.int8) if want_spins else None
+        r = SqaResultStruct()
+        r.best_spins = spins.ctypes.data_as(C.POINTER(C.c_int8))
+        r.replica_energies = energies.ctypes.data_as(C.POINTER(C.c_double))
+        if trace is not None:
+            r.energy_trace = trace.ctypes.data_as(C.POINTER(C.c_double))
+        if allsp is not None:
+            r.final_spins = allsp.ctypes.data_as(C.POINTER(C.c_int8))
+        _check(lib().sb_sqa_solve(self.h, C.byref(problem.s), C.byref(params), C.byref(r)), self.h)
+        return SqaResult(best_spins=spins, replica_energies=energies, best_energy=r.best_energy,
+                         best_energy_i64=r.best_energy_i64, best_replica=r.best_replica,
+                         energy_check_ok=bool(r.energy_check_ok), device_ms=r.device_ms,
+                         total_ms=r.total_ms, spin_updates_per_s=r.spin_updates_per_s,
+                         kernel_launches=r.kernel_launches, energy_trace=trace, final_spins=allsp)
+
     def plan(self, problem: Problem, params: Params, want_state: bool = False) -> Plan:
         return Plan(self, problem, params, want_state)
 
@@ -471,6 +553,14 @@ class Context:
 
 def pump(a0: float, t: int, steps: int) -> float:
     return lib().sb_pump(a0, t, steps)
+
+
+def sqa_schedule(steps: int, trotter: int):
+    """beta[p], J_perp[p] of the SQA schedule (sb_sqa_schedule)."""
+    b = np.zeros(steps, np.float32)
+    j = np.zeros(steps, np.float32)
+    lib().sb_sqa_schedule(steps, trotter, b.ctypes.data_as(C.POINTER(C.c_float)), j.ctypes.data_as(C.POINTER(C.c_float)))
+    return b, j
 
 
 def time_to_target(energies: np.ndarray, times_ms: np.ndarray, threshold: float, run_ms: float,

@@ -13,6 +13,8 @@
  *                   <- the host energy loop                  SB/CUDA_GPU/m2_opt.cu:192-202
  *   sb_params.trace <- print_energy (per-step energy trace)  SB/CUDA_GPU/m2_opt.cu:77-91
  *                      (filled into sb_result.energy_trace)
+ *   sb_sqa_solve    <- the SQA program SQA_fully/fully_test/pre_calculate.cu (main :158-257;
+ *                      preapare_spins :38-51, reduce :99-149, update_spins :53-84)
  *   sb_time_to_target
  *                   <- the trace analysis of plot_energy_decrease/plot.r:88-240 and the
  *                      success-probability time of SA_naive/CUDA_GPU/tests/test.sh:26-32
@@ -300,6 +302,50 @@ typedef struct sb_serving_stats {
   double admit_ms;              /* summed time spent preparing requests (several threads) */
 } sb_serving_stats;
 sb_status sb_serving_stats_get(sb_ctx *ctx, sb_serving_stats *out);
+
+/* ---- simulated quantum annealing (SQA), fully connected ----
+ * Replaces the reference's GPU SQA program SQA_fully/fully_test/pre_calculate.cu (its main,
+ * :158-257): M Trotter slices of the N spins, a diagonal wavefront of M + N - 1 Metropolis updates
+ * per slice and annealing step (slice m updates spin (a - m) mod N at iteration a, :63, :221-224),
+ * the energy change 2 M s (f - M J_perp (s[m-1] + s[m+1])) with f the exact integer local field
+ * (:68-77), acceptance when -log(u) / beta > delta (:79-81), and the schedule
+ * Gamma = 8 (1 - p / steps), J_perp = -0.5 log(tanh(Gamma / M * beta)) / beta, beta from 1/16
+ * rising by (8 - 1/16) / steps per step (:206-225; sb_sqa_schedule returns it). Couplings: integers
+ * with |J| <= 127 (the reference stores char, :164-179), no fields (:176). Replicas are the
+ * reference's TIMES trials, run side by side. Energies are those of slice 0, as the reference
+ * reports (:230-236), exact (int64). */
+enum { SB_SQA_RNG_REFERENCE = 0, /* the reference's random numbers: per-spin xorshift32 seeded with
+                                    the spin index, M calls per trial for the initial slices
+                                    (:38-51, :186-191), and one fixed random word per spin for every
+                                    acceptance test of the run (update_spins never advances it, :71) */
+       SB_SQA_RNG_HASH = 1 };     /* initial slices and one uniform per (replica, step, iteration,
+                                    slice) from counter hashes of the seed */
+typedef struct sb_sqa_params {
+  int32_t trotter;    /* M, Trotter slices: 1 <= M <= min(n, 128) (reference: pre_calculate.cu:16) */
+  int32_t steps;      /* annealing steps (:15) */
+  int32_t replicas;   /* independent runs (:12 TIMES) */
+  int32_t rng_mode;   /* SB_SQA_RNG_REFERENCE or SB_SQA_RNG_HASH */
+  uint64_t seed;      /* hash mode */
+  int32_t trace;      /* 1: every replica's slice-0 energy after every step */
+} sb_sqa_params;
+typedef struct sb_sqa_result {
+  int8_t *best_spins;         /* [n] slice 0 of the lowest-energy replica */
+  double *replica_energies;   /* [replicas] final slice-0 energy of each replica */
+  double *energy_trace;       /* [replicas * steps] replica-major (trace) */
+  int8_t *final_spins;        /* [replicas * trotter * n] every slice of every replica, or NULL */
+  double best_energy;
+  int64_t best_energy_i64;    /* host re-check of best_spins */
+  int32_t best_replica;
+  int32_t energy_check_ok;
+  double device_ms;           /* CUDA-event time of set-up kernels + the anneal + energies */
+  double total_ms;            /* host wall time of the call, copies included */
+  double spin_updates_per_s;  /* replicas * trotter * (n + trotter - 1) * steps / device time */
+  int64_t kernel_launches;
+} sb_sqa_result;
+void sb_sqa_params_default(sb_sqa_params *p);
+/* beta[p] and J_perp[p] for p = 0 .. steps - 1 (host only) */
+void sb_sqa_schedule(int32_t steps, int32_t trotter, float *beta, float *jperp);
+sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *p, const sb_sqa_params *params, sb_sqa_result *res);
 
 /* ---- dSB without any device allocation ----
  * No counterpart in the reference (its program allocates everything itself, m2_opt.cu:106-145).

@@ -17,6 +17,7 @@ _lib = None
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 
 
 def lib():
@@ -57,6 +58,13 @@ def lib():
                                          C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
                                          C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                          C.c_int]),
+            "oracle_sqa_log": (C.c_float, [C.c_float]),
+            "oracle_sqa_schedule": (None, [C.c_int, C.c_int, f32p, f32p]),
+            "oracle_sqa_init_reference": (None, [C.c_int, C.c_int, C.c_int, i8p, u32p]),
+            "oracle_sqa_init_hash": (None, [C.c_int, C.c_int, C.c_int, C.c_uint64, i8p]),
+            "oracle_sqa_energy": (C.c_int64, [C.c_int, i8p, i8p]),
+            "oracle_sqa_run": (C.c_int, [C.c_int, i8p, C.c_int, C.c_int, f32p, f32p, C.c_int, C.c_int,
+                                         C.c_void_p, C.c_uint64, i8p, C.c_void_p]),
         }
         for k, (r, a) in sig.items():
             fn = getattr(L, k)
@@ -182,3 +190,48 @@ def cpu_run(variant, J, h, x, y, steps, a0=1.0, c0=0.0, dt=1.25, m=2, mts_dt=0.5
     if rc != 0:
         raise RuntimeError(f"oracle_cpu_run failed: {rc}")
     return threads
+
+
+# ---- SQA (oracle/sqa_oracle.c) ----
+
+def sqa_log(u):
+    return lib().oracle_sqa_log(u)
+
+
+def sqa_schedule(steps, M):
+    beta = np.zeros(steps, np.float32)
+    jp = np.zeros(steps, np.float32)
+    lib().oracle_sqa_schedule(steps, M, beta, jp)
+    return beta, jp
+
+
+def sqa_init(n, M, R, rng, seed=0):
+    """Initial slices [R, M, n] int8 and (reference mode) the per-spin random words [R, n]."""
+    s = np.zeros((R, M, n), np.int8)
+    rnd = np.zeros((R, n), np.uint32)
+    if rng == 0:
+        lib().oracle_sqa_init_reference(n, M, R, s, rnd)
+    else:
+        lib().oracle_sqa_init_hash(n, M, R, seed, s)
+    return s, (rnd if rng == 0 else None)
+
+
+def sqa_run(J, spins, steps, rng, rnd=None, seed=0, beta=None, jperp=None):
+    """SQA on spins [R, M, n] int8 (updated in place); returns the slice-0 energy trace [R, steps]."""
+    J8 = np.ascontiguousarray(J, np.float32).astype(np.int8)
+    R, M, n = spins.shape
+    if beta is None:
+        beta, jperp = sqa_schedule(steps, M)
+    trace = np.zeros((R, steps), np.int64)
+    rc = lib().oracle_sqa_run(n, J8, M, steps, np.ascontiguousarray(beta, np.float32),
+                              np.ascontiguousarray(jperp, np.float32), R, rng,
+                              _vp(None if rnd is None else np.ascontiguousarray(rnd, np.uint32)), seed,
+                              spins, _vp(trace))
+    if rc != 0:
+        raise ValueError("bad SQA sizes")
+    return trace
+
+
+def sqa_energy(J, s):
+    J8 = np.ascontiguousarray(J, np.float32).astype(np.int8)
+    return int(lib().oracle_sqa_energy(J8.shape[0], J8, np.ascontiguousarray(s, np.int8)))
