@@ -6,7 +6,9 @@
 // (m2_opt.cu:206-210). Options select bSB / dSB, replicas, schedule and field precision, and add
 // best_spins.txt (one +1/-1 per line) and a JSON summary on stdout. --target E adds the
 // time-to-target summary of the run's replica traces (plot_energy_decrease/plot.r:88-240,
-// SA_naive/CUDA_GPU/tests/test.sh:26-32).
+// SA_naive/CUDA_GPU/tests/test.sh:26-32). --variant sqa runs simulated quantum annealing, the
+// drop-in for the reference's SQA program (SQA_fully/fully_test/pre_calculate.cu: output.txt holds
+// each trial's final slice-0 energy, :242-246; --trace prints each step's energy, :236).
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -20,13 +22,54 @@
 static void usage() {
   printf(
       "Usage:\n"
-      "  sb <graph> [--variant asb|bsb|dsb] [--steps S] [--replicas R] [--seed X]\n"
+      "  sb <graph> [--variant asb|bsb|dsb|sqa] [--steps S] [--replicas R] [--seed X]\n"
       "             [--dt DT] [--a0 A0] [--c0 C0] [--xi XI] [--mts-m M]\n"
       "             [--field auto|fp32|tc] [--init uniform|reference]\n"
       "             [--n N] [--index-base 0|1] [--strict] [--trace] [--device D]\n"
       "             [--out output.txt] [--spins best_spins.txt] [--json]\n"
-      "             [--target E [--p-target P]]\n"
+      "             [--target E [--p-target P]] [--trotter M]\n"
       "Graph file: N [E] then lines 'i j J_ij' (i != j) and optional 'i i h_i'.\n");
+}
+
+// --variant sqa: one sb_sqa_solve; output.txt gets each trial's final energy
+static int run_sqa(sb_ctx *ctx, const sb_problem *prob, const sb_sqa_params &q, const std::string &out_path,
+                   const std::string &spins_path, bool json) {
+  std::vector<int8_t> spins((size_t)prob->n);
+  std::vector<double> energies((size_t)q.replicas);
+  std::vector<double> trace(q.trace ? (size_t)q.replicas * q.steps : 0);
+  sb_sqa_result r;
+  memset(&r, 0, sizeof(r));
+  r.best_spins = spins.data();
+  r.replica_energies = energies.data();
+  r.energy_trace = q.trace ? trace.data() : nullptr;
+  const sb_status s = sb_sqa_solve(ctx, prob, &q, &r);
+  if (s != SB_OK) {
+    fprintf(stderr, "sb: sqa failed: %s (%s)\n", sb_status_string(s), sb_last_error(ctx));
+    return 1;
+  }
+  if (q.trace)
+    for (int k = 0; k < q.replicas; ++k)
+      for (int t = 0; t < q.steps; ++t)
+        printf("trial %d step %d energy %lld\n", k, t, (long long)trace[(size_t)k * q.steps + t]);
+  FILE *f = fopen(out_path.c_str(), "w");
+  if (f) {
+    for (int k = 0; k < q.replicas; ++k) fprintf(f, "%lld\n", (long long)energies[k]);
+    fclose(f);
+  }
+  f = fopen(spins_path.c_str(), "w");
+  if (f) {
+    for (int i = 0; i < prob->n; ++i) fprintf(f, "%d\n", (int)spins[i]);
+    fclose(f);
+  }
+  if (json)
+    printf("{\"n\": %d, \"trotter\": %d, \"replicas\": %d, \"steps\": %d, \"best_energy\": %lld, "
+           "\"energy_check_ok\": %d, \"device_ms\": %.6f, \"total_ms\": %.6f, \"spin_updates_per_s\": %.6e}\n",
+           prob->n, q.trotter, q.replicas, q.steps, (long long)r.best_energy, r.energy_check_ok, r.device_ms,
+           r.total_ms, r.spin_updates_per_s);
+  else
+    printf("best energy %lld (replica %d), %.3f ms on device, %.4e spin-updates/s\n", (long long)r.best_energy,
+           r.best_replica, r.device_ms, r.spin_updates_per_s);
+  return 0;
 }
 
 int main(int argc, char **argv) {
@@ -42,14 +85,19 @@ int main(int argc, char **argv) {
   sb_graph_opts go;
   sb_graph_opts_default(&go);
   int variant = SB_ASB;
+  bool sqa = false;
   // first pass: variant (it sets the defaults)
   for (int i = 1; i < argc; ++i)
     if (!strcmp(argv[i], "--variant") && i + 1 < argc) {
       const char *v = argv[i + 1];
       variant = !strcmp(v, "bsb") ? SB_BSB : !strcmp(v, "dsb") ? SB_DSB : SB_ASB;
+      sqa = !strcmp(v, "sqa");
     }
   sb_params p;
   sb_params_default(&p, variant);
+  sb_sqa_params q;
+  sb_sqa_params_default(&q);
+  if (sqa) p.steps = q.steps;
   for (int i = 1; i < argc; ++i) {
     const char *a = argv[i];
     auto next = [&](void) -> const char * {
@@ -85,6 +133,7 @@ int main(int argc, char **argv) {
       target = atof(next());
       have_target = true;
     } else if (!strcmp(a, "--p-target")) p_target = atof(next());
+    else if (!strcmp(a, "--trotter")) q.trotter = atoi(next());
     else if (!strcmp(a, "-h") || !strcmp(a, "--help")) {
       usage();
       return 0;
@@ -112,6 +161,17 @@ int main(int argc, char **argv) {
     fprintf(stderr, "sb: %s (%s)\n", sb_status_string(s), sb_last_error(nullptr));
     sb_problem_free(&prob);
     return 1;
+  }
+  if (sqa) {
+    q.steps = p.steps;
+    q.replicas = p.replicas;
+    q.seed = p.seed;
+    q.rng_mode = p.init_mode == SB_INIT_REFERENCE ? SB_SQA_RNG_REFERENCE : SB_SQA_RNG_HASH;
+    q.trace = p.trace;
+    const int rc = run_sqa(ctx, &prob, q, out_path, spins_path, json);
+    sb_destroy(ctx);
+    sb_problem_free(&prob);
+    return rc;
   }
   std::vector<int8_t> spins((size_t)prob.n);
   std::vector<double> energies((size_t)p.replicas);

@@ -48,6 +48,9 @@ WORKLOADS = {
     "uneven-batch": ("dsb", 0, 64, 1500, "grouped",
                      "uneven batch: 512 instances, N ~ U[64,4096], Erdos-Renyi density ~ U[0.05,1], "
                      "J = +-1, R=64, 1500 steps, one grouped tensor-core launch per step"),
+    "sqa": ("sqa", 4096, 152, 100, "sqa",
+            "SQA: complete N=4096, J iid +-1, M=64 Trotter slices, 100 annealing steps (the sizes of "
+            "SQA_fully/fully_test/pre_calculate.cu), one replica per SM"),
     "serving": ("dsb", 0, 32, 0, "serving",
                 "serving stream: Poisson arrivals at 200/s, N log-uniform in [128,16384], density "
                 "~ U[0.01,1], J ~ U{-8..8}, R=32, step budget ~ U[500,4000]"),
@@ -187,6 +190,8 @@ def run_reference(args, rank, world):
     """The CPU port of the reference step loop, timed per bench step on a bounded sample."""
     if rank != 0:
         return
+    if args.workload == "sqa":
+        return run_reference_sqa(args, world)
     J, h = make_problem(args.workload)
     variant, n, R, steps, field, desc = WORKLOADS[args.workload]
     budget = args.cpu_budget or max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
@@ -539,6 +544,124 @@ def run_serving(args, rank, world, local_rank):
     ctx.close()
 
 
+SQA_TROTTER = 64
+
+
+def sqa_cpu_sample(J, M, budget_s=10.0):
+    """The SQA oracle (single-threaded C restatement of pre_calculate.cu) on whole annealing steps
+    of one replica, as many as fit ~budget_s (at least one)."""
+    from oracle import binding as orc
+
+    n = J.shape[0]
+    s, _ = orc.sqa_init(n, M, 1, 1, 1234)
+    b, jp = orc.sqa_schedule(100, M)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        orc.sqa_run(J, s, 1, 1, seed=1234, beta=b[k % 100:k % 100 + 1], jperp=jp[k % 100:k % 100 + 1])
+        k += 1
+        if time.perf_counter() - t0 >= budget_s or k >= 100:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": M * (n + M - 1) * k / dt, "unit": "spin-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{k} annealing steps x 1 replica (N={n}, M={M}), single thread", "seconds": dt}
+
+
+def run_reference_sqa(args, world):
+    from annealing_gb300 import instances
+
+    _, n, R, steps, _, desc = WORKLOADS["sqa"]
+    J = instances.complete_pm1(n, seed=1234)
+    budget = args.cpu_budget or max(2.0, min(10.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        sqa_cpu_sample(J, SQA_TROTTER, budget_s=budget / 4)
+    samples = [sqa_cpu_sample(J, SQA_TROTTER, budget_s=budget) for _ in range(args.steps)]
+    value = float(statistics.median(s["value"] for s in samples))
+    updates = float(R) * SQA_TROTTER * (n + SQA_TROTTER - 1) * steps
+    line = {
+        "impl": "reference", "metric": "SQA spin-updates/s", "value": value, "unit": "spin-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * updates / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int",
+        "data": "synthetic", "config": {"workload": desc, "n": n, "trotter": SQA_TROTTER, "replicas": R,
+                                        "anneal_steps": steps},
+        "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": 1, "kind": "port",
+                         "sample": samples[0]["sample"]},
+        "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the C restatement of pre_calculate.cu's wavefront (oracle/sqa_oracle.c), one thread",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_sqa(args, rank, world, local_rank):
+    import torch
+
+    import annealing_gb300 as sb
+    from annealing_gb300 import instances
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    _, n, R, steps, _, desc = WORKLOADS["sqa"]
+    M = SQA_TROTTER
+    J = instances.complete_pm1(n, seed=1234)
+    prob = sb.Problem.from_dense(J)
+    stream = torch.cuda.current_stream(dev)
+    ctx = sb.Context(local_rank, stream=stream.cuda_stream)
+    prm = sb.SqaParams.default(trotter=M, steps=steps, replicas=R, seed=1234 + rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for k in range(args.warmup):
+        ctx.sqa_solve(prob, prm)
+    barrier()
+    dev_ms, tot_ms, results = [], [], []
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize(dev)
+            prm.seed = 5000 + k
+            t0 = time.perf_counter()
+            r = ctx.sqa_solve(prob, prm)  # H2D of J, anneal, D2H of energies and spins
+            tot_ms.append(1e3 * (time.perf_counter() - t0))
+            dev_ms.append(r.device_ms)
+            results.append(r)
+        barrier()
+    updates = float(R) * M * (n + M - 1) * steps
+    total_dev = reduce_max(float(sum(dev_ms)), world)
+    total_e2e = reduce_max(float(sum(tot_ms)), world)
+    value = weak_scaling_value(updates, world, args.steps, total_dev)
+    e2e = weak_scaling_value(updates, world, args.steps, total_e2e)
+    if rank != 0:
+        ctx.close()
+        return
+    # couplings evaluated per second: every update's field covers N couplings of one row
+    coupling_evals = updates * n / (total_dev / args.steps * 1e-3)
+    line = {
+        "metric": "SQA spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int (bit-plane couplings, popcount fields), f32 acceptance test",
+        "data": "synthetic (seeded +-1 complete graph)",
+        "config": {"workload": desc, "n": n, "trotter": M, "replicas": R, "anneal_steps": steps,
+                   "rng": "hash", "parallelism": f"replicas-only x{world}",
+                   "l2": "flushed between timed solves (256 MB write outside the timed region)"},
+        "e2e": {"value": e2e, "unit": "spin-updates/s", "h2d_bytes_per_step": int(J.nbytes),
+                "d2h_bytes_per_step": int(R * 8 + n)},
+        "gpu_launches": int(sum(r.kernel_launches for r in results)),
+        "throughput": {"coupling_evals_per_s": coupling_evals,
+                       "note": "each Metropolis update evaluates its spin's N couplings against its slice"},
+        "clocks": clk.summary(),
+        "quality": {"best_energy": min(r.best_energy for r in results),
+                    "energy_check_ok": all(r.energy_check_ok for r in results)},
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = sqa_cpu_sample(J, M)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -575,6 +698,8 @@ def main():
         run_batch(args, rank, world, local_rank)
     elif args.workload == "serving":
         run_serving(args, rank, world, local_rank)
+    elif args.workload == "sqa":
+        run_sqa(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1 and args.impl == "ours":

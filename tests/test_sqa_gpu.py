@@ -83,3 +83,22 @@ def test_rejects_what_it_cannot_run(ctx):
     with pytest.raises(sb.SBError) as e:
         ctx.sqa_solve(sb.Problem.from_dense(J, np.ones(16, np.float32)), sb.SqaParams.default(trotter=4))
     assert e.value.status == 6
+
+
+def test_cli_drop_in_reproduces_the_reference_program(tmp_path):
+    """`sb <graph> --variant sqa --init reference` on the pinned instance writes the final slice-0
+    energy of each trial to output.txt, as pre_calculate.cu:242-246 does, equal to the run of the
+    reference's own kernels."""
+    import subprocess
+
+    d = np.load(os.path.join(GOLDEN, "ref_sqa_n256_m8.npz"))
+    trials, steps = d["energy"].shape
+    g = str(tmp_path / "k256.txt")
+    instances.write_graph(g, d["J"].astype(np.float32))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [os.path.join(root, "annealing_gb300", "sb"), g, "--variant", "sqa", "--trotter", "8", "--trials",
+           str(trials), "--steps", str(steps), "--init", "reference"]
+    out = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    got = np.array(open(tmp_path / "output.txt").read().split(), dtype=np.int64)
+    np.testing.assert_array_equal(got, d["energy"][:, -1])
