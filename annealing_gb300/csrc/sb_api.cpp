@@ -756,7 +756,13 @@ sb_status sb_submit(sb_ctx *ctx, const sb_problem *p, const sb_params *params, u
 sb_status sb_poll(sb_ctx *ctx, uint64_t ticket, sb_result *res, int32_t wait_ms) {
   if (!ctx || !res) return SB_ERR_INVALID_ARG;
   if (!ctx->server) return SB_ERR_NOT_FOUND;
-  return sbs::server_poll(ctx->server, ticket, res, wait_ms);
+  std::string err;
+  const sb_status s = sbs::server_poll(ctx->server, ticket, res, wait_ms, err);
+  if (s != SB_OK && s != SB_ERR_PENDING) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error = err;
+  }
+  return s;
 }
 
 sb_status sb_cancel(sb_ctx *ctx, uint64_t ticket) {

@@ -234,7 +234,10 @@ void Server::retire(int at_tick) {
     cudaError_t e = groups[kv.first]->energy_pass_for(kv.second, at_tick);
     if (e != cudaSuccess)
       for (Req *r : fin)
-        if (r->nr == kv.first) r->status = SB_ERR_CUDA;
+        if (r->nr == kv.first) {
+          r->status = SB_ERR_CUDA;
+          r->err = std::string("energy pass: ") + cudaGetErrorString(e);
+        }
   }
   uint32_t status = 0;
   for (auto &kv : groups)
@@ -346,7 +349,7 @@ void Server::check_loop() {
     Req *r = job.first;
     if (job.second == SB_OK && sb_energy_i64(r->prob, r->spins.data(), &r->e64) == SB_OK)
       r->ok = (double)r->e64 == r->best ? 1 : 0;
-    finish(r, job.second, job.second == SB_OK ? "" : "device error");
+    finish(r, job.second, job.second == SB_OK ? "" : (r->err.empty() ? std::string("device error") : r->err));
   }
 }
 
@@ -428,7 +431,7 @@ sb_status server_submit(Server *s, const sb_problem *p, const sb_params *prm, ui
   return SB_OK;
 }
 
-sb_status server_poll(Server *s, uint64_t ticket, sb_result *res, int32_t wait_ms) {
+sb_status server_poll(Server *s, uint64_t ticket, sb_result *res, int32_t wait_ms, std::string &err) {
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return SB_ERR_NOT_FOUND;
@@ -442,6 +445,7 @@ sb_status server_poll(Server *s, uint64_t ticket, sb_result *res, int32_t wait_m
       return SB_ERR_PENDING;
   }
   const sb_status st = r->status;
+  if (st != SB_OK) err = r->err;
   if (st == SB_OK) {
     if (res->best_spins) memcpy(res->best_spins, r->spins.data(), r->spins.size());
     if (res->replica_energies) memcpy(res->replica_energies, r->energies.data(), r->energies.size() * sizeof(double));

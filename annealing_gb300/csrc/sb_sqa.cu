@@ -122,39 +122,54 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
   for (int k = tid; k < M * W; k += blockDim.x) sp[k] = p.spins[(size_t)r * M * W + k];
   __syncthreads();
 
-  // stream index q -> row ((q mod per_step) - (M - 1)) mod n, slot q mod S
+  // Stream index q -> row ((q mod per_step) - (M - 1)) mod n, slot q mod S, slot use (lap) q / S.
+  // Every index below is kept by increments (no division in the loop): the issuer's position, and
+  // per iteration the newest row's slot / lap (slice 0) and a mod n.
   long long issued = 0;
+  int iss_slot = 0, iss_pos = 0;
+  const int row_first = (n - (M - 1) % n) % n;  // row of stream position 0 within a step
+  int iss_row = row_first;
   auto issue_upto = [&](long long last) {  // thread 0 only
     if (last >= total) last = total - 1;
     if (issued <= last) sbk::ptx::fence_proxy_async_shared();  // earlier generic reads of the slots
     for (; issued <= last; ++issued) {
-      const long long it = issued % per_step - (M - 1);
-      const int row = (int)(((it % n) + n) % n);
-      const int slot = (int)(issued % S);
-      sbk::ptx::mbar_arrive_expect_tx(&bar[slot], row_bytes);
-      sbk::ptx::bulk_g2s(ring + (size_t)slot * RW, p.rows + (size_t)row * RW, row_bytes, &bar[slot]);
+      sbk::ptx::mbar_arrive_expect_tx(&bar[iss_slot], row_bytes);
+      sbk::ptx::bulk_g2s(ring + (size_t)iss_slot * RW, p.rows + (size_t)iss_row * RW, row_bytes, &bar[iss_slot]);
+      if (++iss_slot == S) iss_slot = 0;
+      if (++iss_pos == per_step) {
+        iss_pos = 0;
+        iss_row = row_first;
+      } else if (++iss_row == n) {
+        iss_row = 0;
+      }
     }
   };
   const int D = S - M;
   if (tid == 0) issue_upto((long long)M - 1 + D);
 
   bool ok = true;
+  long long q0 = M - 1;     // stream index of slice 0's row in the current iteration
+  int slot0 = M - 1, lap0 = 0;  // q0 mod S, q0 / S (M - 1 < S)
   for (int st = 0; st < p.steps && ok; ++st) {
     const float beta = p.beta[st], jp = p.jperp[st];
     const float mj = __fmul_rn((float)M, jp);
-    const long long base = (long long)st * per_step;
+    uint64_t e_it = ((uint64_t)r * p.steps + st) * (uint64_t)iters * (uint64_t)M;  // hash index of (a, m = 0)
+    int t0 = 0;  // a mod n
     for (int a = 0; a < iters; ++a) {
-      if (tid == 0 && a + st > 0) issue_upto(base + a + M - 1 + D);
+      if (tid == 0 && a + st > 0) issue_upto(q0 + D);
       // fields of this warp's slices (at most 4 per warp: M <= 128), kept in registers
       int f0 = 0, f1 = 0, f2 = 0, f3 = 0, ns = 0;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int m = warp + j * nw;
         if (m < M && ok) {
-          const long long q = base + a - m + (M - 1);
-          const int slot = (int)(q % S);
+          int slot = slot0 - m, lap = lap0;  // stream index q0 - m
+          if (slot < 0) {
+            slot += S;
+            lap -= 1;
+          }
           // one verdict per warp: the field's shuffles need every lane
-          if (!__all_sync(0xffffffffu, sbk::ptx::mbar_wait(&bar[slot], (uint32_t)((q / S) & 1)))) {
+          if (!__all_sync(0xffffffffu, sbk::ptx::mbar_wait(&bar[slot], (uint32_t)(lap & 1)))) {
             ok = false;
           } else {
             const int f = sqa_field(ring + (size_t)slot * RW, sp + (size_t)m * W, W, p.P, lane);
@@ -173,20 +188,23 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
         // lane j decides slice warp + j * nw
         const int m = warp + lane * nw;
         const int f = lane == 0 ? f0 : lane == 1 ? f1 : lane == 2 ? f2 : f3;
-        const int target = ((a - m) % n + n) % n;
+        const int target = t0 - m < 0 ? t0 - m + n : t0 - m;  // (a - m) mod n, m < n
         const uint32_t wi = (uint32_t)target >> 5, bi = 1u << (target & 31);
         const int up = m == 0 ? M - 1 : m - 1, lo = m == M - 1 ? 0 : m + 1;
         const int s = (sp[(size_t)m * W + wi] & bi) ? -1 : 1;
         const int nb = ((sp[(size_t)up * W + wi] & bi) ? -1 : 1) + ((sp[(size_t)lo * W + wi] & bi) ? -1 : 1);
         const float inner = __fsub_rn((float)f, __fmul_rn(mj, (float)nb));
-        const float delta = __double2float_rn(__dmul_rn((double)(2 * M * s), (double)inner));
+        // the reference forms 2 M s * inner in double (pre_calculate.cu:76-77); that product is exact
+        // (|2 M s| <= 256 times a 24-bit significand), so rounding it to float is one correctly
+        // rounded float multiply: the same value without the (slow) FP64 pipe
+        const float delta = __fmul_rn((float)(2 * M * s), inner);
         float u;
         if (p.rnd) {
           u = __fdiv_rn(__uint2float_rn(p.rnd[(size_t)r * n + target]), 4294967296.0f);
         } else {
-          const uint64_t e = ((((uint64_t)r * p.steps + st) * iters + a) * M) + m;
+          const uint64_t e = e_it + (uint64_t)m;
           const uint64_t z = sqa_mix64((p.seed ^ 0xD1B54A32D192ED03ULL) + 0x9E3779B97F4A7C15ULL * (e + 1));
-          u = __fmul_rn((float)(z >> 40), 0x1p-24f);
+          u = __fmul_rn((float)(uint32_t)(z >> 40), 0x1p-24f);
         }
         const float thr = __fdiv_rn(-sqa_log(u), beta);
         if (thr > delta) sp[(size_t)m * W + wi] ^= bi;
@@ -196,6 +214,21 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
         ok = false;
         break;
       }
+      // next iteration: q0 + 1, a + 1
+      ++q0;
+      if (++slot0 == S) {
+        slot0 = 0;
+        ++lap0;
+      }
+      if (++t0 == n) t0 = 0;
+      e_it += (uint64_t)M;
+    }
+    // the next step starts at stream index base + per_step + M - 1: M - 1 past where the loop ended
+    q0 += M - 1;
+    slot0 += M - 1;
+    if (slot0 >= S) {
+      slot0 -= S;
+      ++lap0;
     }
     if (!ok) break;
     // slice-0 energy: E = -1/2 sum_i s_i f_i, rows read from global memory
