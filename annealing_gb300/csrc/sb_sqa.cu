@@ -10,16 +10,20 @@
 //
 // Here one CTA runs one replica (one of the reference's TIMES trials) for the whole anneal:
 //   * the M x N spins live in shared memory as bits (bit 1 = spin -1), slice-major;
-//   * J lives in global memory (L2-resident) as bit-planes per row: a sign plane (1 where
-//     J_ij < 0) and P magnitude planes (bit k-1 of |J_ij|), plus the row's sum of |J_ij|. A field is
-//     then sum_i J_i s_i = rowabs - 2 sum_k 2^(k-1) popc(mag_k & (sign ^ spin)): 32 couplings per
-//     XOR / AND / POPC, exact integers;
+//   * J lives in global memory (L2-resident) as bit-planes per row: per 32-coupling word a sign
+//     word (1 where J_ij < 0) and P magnitude words (bit k-1 of |J_ij|), then the row's sum of
+//     |J_ij|. A field is sum_i J_i s_i = rowabs - 2 sum_k 2^(k-1) popc(mag_k & (sign ^ spin)):
+//     32 couplings per XOR / AND / POPC, exact integers (P templated: one 8-byte load per word for
+//     +-1 couplings);
 //   * the wavefront needs rows a - M + 1 .. a at iteration a; they stream through a ring of
 //     M + D row slots in shared memory by 1-D bulk copies (cp.async.bulk + mbarrier), D rows ahead,
 //     so a row is read from L2 once per use window instead of M times;
-//   * warp w takes slices w, w + warps, ...: its lanes split the row's words, a shuffle reduction
-//     gives the field, and one lane per slice makes the slice's decision; one __syncthreads per
-//     iteration orders the flips before the next iteration's fields.
+//   * a group of 8 lanes sums one slice's field (4 slices per warp); the group's first lane makes
+//     the slice's decision against a threshold -log(u) / beta made ahead of time (per step and
+//     spin in reference mode, whose random word per spin is fixed; per chunk of iterations in hash
+//     mode); one __syncthreads per iteration orders the flips before the next iteration's fields;
+//   * slot and slice strides are padded (16 and 8 words mod 32) so the four groups of a warp read
+//     different banks, and a ring shallow enough for two CTAs per SM is preferred.
 // No two slices of one iteration touch the same spin, and a slice's Trotter neighbours read other
 // spins than the ones it flips (M <= N), so the CTA reproduces the reference's iteration semantics
 // exactly. The acceptance log is this library's own (sqa_log below; the oracle carries the same
@@ -46,6 +50,7 @@ namespace {
 constexpr int kSqaMaxWarps = 32;
 constexpr int kSqaAhead = 8;                 // rows the ring streams ahead of the wavefront
 constexpr size_t kSqaSmemBudget = 220 * 1024;
+constexpr size_t kSqaSmemHalf = 112 * 1024;  // two CTAs per SM (228 KB, less static and reserved)
 
 struct SqaArgs {
   const uint32_t *rows;   // [n][RW]: sign plane [W], P magnitude planes [W] each, rowabs, 3 pad words
@@ -57,6 +62,7 @@ struct SqaArgs {
   uint32_t *status;
   uint64_t seed;
   int n, W, P, RW, M, steps, S, trace;
+  int RS, SPS;            // shared-memory strides of a ring slot and of a slice (bank-spread padding)
 };
 
 // log(u) for u in [0, 1] (the oracle's sqa_log, operation for operation): u = 2^e m with m in
@@ -86,24 +92,93 @@ __device__ __forceinline__ uint64_t sqa_mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-// Field of `row` against slice bits `sm`, summed over the warp (every lane gets it).
-__device__ __forceinline__ int sqa_field(const uint32_t *row, const uint32_t *sm, int W, int P, int lane) {
+// Field of `row` against slice bits `sm`, summed over the warp (every lane gets it). A row stores,
+// per 32-coupling word w, the sign word then the P magnitude words (row[w (P + 1) + k]), and the
+// row's sum of |J| after the W groups.
+template <int P>
+__device__ __forceinline__ int sqa_field(const uint32_t *row, const uint32_t *sm, int W, int lane) {
   int acc = 0;
+#pragma unroll 4
   for (int w = lane; w < W; w += 32) {
-    const uint32_t x = row[w] ^ sm[w];
-    for (int k = 1; k <= P; ++k) acc += __popc(row[k * W + w] & x) << (k - 1);
+    const uint32_t *g = row + (size_t)w * (P + 1);
+    uint32_t v[P + 1];
+    if constexpr (P == 1) {
+      const uint2 t = *reinterpret_cast<const uint2 *>(g);
+      v[0] = t.x;
+      v[1] = t.y;
+    } else if constexpr (P == 3) {
+      const uint4 t = *reinterpret_cast<const uint4 *>(g);
+      v[0] = t.x;
+      v[1] = t.y;
+      v[2] = t.z;
+      v[3] = t.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k <= P; ++k) v[k] = g[k];
+    }
+    const uint32_t x = v[0] ^ sm[w];
+#pragma unroll
+    for (int k = 1; k <= P; ++k) acc += __popc(v[k] & x) << (k - 1);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  return (int)row[(P + 1) * W] - 2 * acc;
+  return (int)row[(size_t)W * (P + 1)] - 2 * acc;
 }
 
+// The same field computed by a group of G lanes (G a power of two dividing 32): lane gl of the
+// group takes words gl, gl + G, ...; a group that has no slice (row == nullptr) contributes 0 and
+// still joins the shuffles. Every lane of the group gets the group's field.
+template <int P, int G>
+__device__ __forceinline__ int sqa_field_group(const uint32_t *row, const uint32_t *sm, int W, int gl) {
+  int acc = 0;
+  if (row) {
+#pragma unroll 4
+    for (int w = gl; w < W; w += G) {
+      const uint32_t *g = row + (size_t)w * (P + 1);
+      uint32_t v[P + 1];
+      if constexpr (P == 1) {
+        const uint2 t = *reinterpret_cast<const uint2 *>(g);
+        v[0] = t.x;
+        v[1] = t.y;
+      } else if constexpr (P == 3) {
+        const uint4 t = *reinterpret_cast<const uint4 *>(g);
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+      } else {
+#pragma unroll
+        for (int k = 0; k <= P; ++k) v[k] = g[k];
+      }
+      const uint32_t x = v[0] ^ sm[w];
+#pragma unroll
+      for (int k = 1; k <= P; ++k) acc += __popc(v[k] & x) << (k - 1);
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return row ? (int)row[(size_t)W * (P + 1)] - 2 * acc : 0;
+}
+
+// Acceptance threshold -log(u) / beta of the reference's test (pre_calculate.cu:79), with this
+// library's log.
+__device__ __forceinline__ float sqa_threshold(float u, float beta) { return __fdiv_rn(-sqa_log(u), beta); }
+
+constexpr int kSqaChunk = 16;  // wavefront iterations whose hash-mode thresholds are made at once
+constexpr int kSqaGroup = 8;   // lanes per slice in the field sums
+constexpr int kSqaSlicesPerWarp = 32 / kSqaGroup;
+
+template <int P>
 __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_constant__ SqaArgs p) {
   extern __shared__ __align__(128) uint8_t smem[];
-  const int RW = p.RW, W = p.W, M = p.M, n = p.n, S = p.S;
-  uint32_t *ring = reinterpret_cast<uint32_t *>(smem);      // [S][RW]
-  uint32_t *sp = ring + (size_t)S * RW;                      // [M][W]
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sp + (size_t)M * W + (((size_t)M * W) & 1));  // [S]
+  const int RW = p.RW, W = p.W, M = p.M, n = p.n, S = p.S, RS = p.RS, SPS = p.SPS;
+  // slot stride RS = 16 (mod 32) words and slice stride SPS = 8 (mod 32): the four lane groups of a
+  // warp read four slots / slices whose words fall in different banks
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem);      // [S][RS] (RW words used)
+  uint32_t *sp = ring + (size_t)S * RS;                      // [M][SPS] (W words used)
+  float *thr = reinterpret_cast<float *>(sp + (size_t)M * SPS);  // [n] (reference) or [kSqaChunk][M] (hash)
+  const size_t thr_words = p.rnd ? (size_t)n : (size_t)kSqaChunk * M;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(thr + ((thr_words + 3) & ~(size_t)3));  // [S]
   __shared__ long long ered[kSqaMaxWarps];
   __shared__ int abort_sh;
 
@@ -119,7 +194,7 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
     sbk::ptx::fence_mbar_init();
     abort_sh = 0;
   }
-  for (int k = tid; k < M * W; k += blockDim.x) sp[k] = p.spins[(size_t)r * M * W + k];
+  for (int k = tid; k < M * W; k += blockDim.x) sp[(k / W) * SPS + k % W] = p.spins[(size_t)r * M * W + k];
   __syncthreads();
 
   // Stream index q -> row ((q mod per_step) - (M - 1)) mod n, slot q mod S, slot use (lap) q / S.
@@ -131,10 +206,11 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
   int iss_row = row_first;
   auto issue_upto = [&](long long last) {  // thread 0 only
     if (last >= total) last = total - 1;
-    if (issued <= last) sbk::ptx::fence_proxy_async_shared();  // earlier generic reads of the slots
+    // a slot is rewritten only after the __syncthreads that ended the last iteration reading it
+    // (a write after reads: the barrier orders them, no proxy fence)
     for (; issued <= last; ++issued) {
       sbk::ptx::mbar_arrive_expect_tx(&bar[iss_slot], row_bytes);
-      sbk::ptx::bulk_g2s(ring + (size_t)iss_slot * RW, p.rows + (size_t)iss_row * RW, row_bytes, &bar[iss_slot]);
+      sbk::ptx::bulk_g2s(ring + (size_t)iss_slot * RS, p.rows + (size_t)iss_row * RW, row_bytes, &bar[iss_slot]);
       if (++iss_slot == S) iss_slot = 0;
       if (++iss_pos == per_step) {
         iss_pos = 0;
@@ -148,66 +224,65 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
   if (tid == 0) issue_upto((long long)M - 1 + D);
 
   bool ok = true;
-  long long q0 = M - 1;     // stream index of slice 0's row in the current iteration
+  long long q0 = M - 1;         // stream index of slice 0's row in the current iteration
   int slot0 = M - 1, lap0 = 0;  // q0 mod S, q0 / S (M - 1 < S)
   for (int st = 0; st < p.steps && ok; ++st) {
     const float beta = p.beta[st], jp = p.jperp[st];
     const float mj = __fmul_rn((float)M, jp);
-    uint64_t e_it = ((uint64_t)r * p.steps + st) * (uint64_t)iters * (uint64_t)M;  // hash index of (a, m = 0)
-    int t0 = 0;  // a mod n
+    const uint64_t e_step = ((uint64_t)r * p.steps + st) * (uint64_t)iters * (uint64_t)M;  // hash index of (a = 0, m = 0)
+    if (p.rnd) {
+      // reference mode: every spin keeps one random word, so a step's thresholds are one per spin
+      for (int i = tid; i < n; i += blockDim.x)
+        thr[i] = sqa_threshold(__fdiv_rn(__uint2float_rn(p.rnd[(size_t)r * n + i]), 4294967296.0f), beta);
+      __syncthreads();
+    }
+    int t0 = 0, ci = 0;  // a mod n, a mod kSqaChunk
     for (int a = 0; a < iters; ++a) {
-      if (tid == 0 && a + st > 0) issue_upto(q0 + D);
-      // fields of this warp's slices (at most 4 per warp: M <= 128), kept in registers
-      int f0 = 0, f1 = 0, f2 = 0, f3 = 0, ns = 0;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int m = warp + j * nw;
-        if (m < M && ok) {
-          int slot = slot0 - m, lap = lap0;  // stream index q0 - m
-          if (slot < 0) {
-            slot += S;
-            lap -= 1;
-          }
-          // one verdict per warp: the field's shuffles need every lane
-          if (!__all_sync(0xffffffffu, sbk::ptx::mbar_wait(&bar[slot], (uint32_t)(lap & 1)))) {
-            ok = false;
-          } else {
-            const int f = sqa_field(ring + (size_t)slot * RW, sp + (size_t)m * W, W, p.P, lane);
-            if (j == 0) f0 = f;
-            else if (j == 1) f1 = f;
-            else if (j == 2) f2 = f;
-            else f3 = f;
-            ns = j + 1;
-          }
-        }
-      }
-      if (!ok) {
-        atomicOr(p.status, sbk::kErrWaitTimeout);
-        abort_sh = 1;
-      } else if (lane < ns) {
-        // lane j decides slice warp + j * nw
-        const int m = warp + lane * nw;
-        const int f = lane == 0 ? f0 : lane == 1 ? f1 : lane == 2 ? f2 : f3;
-        const int target = t0 - m < 0 ? t0 - m + n : t0 - m;  // (a - m) mod n, m < n
-        const uint32_t wi = (uint32_t)target >> 5, bi = 1u << (target & 31);
-        const int up = m == 0 ? M - 1 : m - 1, lo = m == M - 1 ? 0 : m + 1;
-        const int s = (sp[(size_t)m * W + wi] & bi) ? -1 : 1;
-        const int nb = ((sp[(size_t)up * W + wi] & bi) ? -1 : 1) + ((sp[(size_t)lo * W + wi] & bi) ? -1 : 1);
-        const float inner = __fsub_rn((float)f, __fmul_rn(mj, (float)nb));
-        // the reference forms 2 M s * inner in double (pre_calculate.cu:76-77); that product is exact
-        // (|2 M s| <= 256 times a 24-bit significand), so rounding it to float is one correctly
-        // rounded float multiply: the same value without the (slow) FP64 pipe
-        const float delta = __fmul_rn((float)(2 * M * s), inner);
-        float u;
-        if (p.rnd) {
-          u = __fdiv_rn(__uint2float_rn(p.rnd[(size_t)r * n + target]), 4294967296.0f);
-        } else {
-          const uint64_t e = e_it + (uint64_t)m;
+      if (!p.rnd && ci == 0) {
+        // hash mode: thresholds of iterations a .. a + kSqaChunk - 1 (every slice) at once; the
+        // previous chunk's last readers finished before the barrier that ended its iteration
+        const int cnt = min(kSqaChunk, iters - a) * M;
+        for (int k = tid; k < cnt; k += blockDim.x) {
+          const uint64_t e = e_step + (uint64_t)a * M + (uint64_t)k;  // (a + k / M) M + k % M
           const uint64_t z = sqa_mix64((p.seed ^ 0xD1B54A32D192ED03ULL) + 0x9E3779B97F4A7C15ULL * (e + 1));
-          u = __fmul_rn((float)(uint32_t)(z >> 40), 0x1p-24f);
+          thr[k] = sqa_threshold(__fmul_rn((float)(uint32_t)(z >> 40), 0x1p-24f), beta);
         }
-        const float thr = __fdiv_rn(-sqa_log(u), beta);
-        if (thr > delta) sp[(size_t)m * W + wi] ^= bi;
+        __syncthreads();
+      }
+      if (tid == 0 && a + st > 0) issue_upto(q0 + D);
+      // fields: lane group lane / kSqaGroup of warp w takes slice w * kSqaSlicesPerWarp + group
+      {
+        const int m = warp * kSqaSlicesPerWarp + lane / kSqaGroup, gl = lane % kSqaGroup;
+        const bool have = m < M;
+        int slot = slot0 - m, lap = lap0;  // stream index q0 - m
+        if (slot < 0) {
+          slot += S;
+          lap -= 1;
+        }
+        // one verdict per warp: the field's shuffles need every lane
+        const bool got = have ? sbk::ptx::mbar_wait(&bar[slot], (uint32_t)(lap & 1)) : true;
+        if (!__all_sync(0xffffffffu, got)) {
+          atomicOr(p.status, sbk::kErrWaitTimeout);
+          abort_sh = 1;
+        } else {
+          const int f = sqa_field_group<P, kSqaGroup>(have ? ring + (size_t)slot * RS : nullptr,
+                                                      sp + (size_t)(have ? m : 0) * SPS, W, gl);
+          if (have && gl == 0) {
+            // the group's first lane decides slice m (pre_calculate.cu:73-81)
+            const int target = t0 - m < 0 ? t0 - m + n : t0 - m;  // (a - m) mod n, m < n
+            const uint32_t wi = (uint32_t)target >> 5, bi = 1u << (target & 31);
+            const int up = m == 0 ? M - 1 : m - 1, lo = m == M - 1 ? 0 : m + 1;
+            const int s = (sp[(size_t)m * SPS + wi] & bi) ? -1 : 1;
+            const int nb = ((sp[(size_t)up * SPS + wi] & bi) ? -1 : 1) + ((sp[(size_t)lo * SPS + wi] & bi) ? -1 : 1);
+            const float inner = __fsub_rn((float)f, __fmul_rn(mj, (float)nb));
+            // the reference forms 2 M s * inner in double (pre_calculate.cu:76-77); that product is
+            // exact (|2 M s| <= 256 times a 24-bit significand), so rounding it to float is one
+            // correctly rounded float multiply: the same value without the (slow) FP64 pipe
+            const float delta = __fmul_rn((float)(2 * M * s), inner);
+            const float th = p.rnd ? thr[target] : thr[ci * M + m];
+            if (th > delta) sp[(size_t)m * SPS + wi] ^= bi;
+          }
+        }
       }
       __syncthreads();
       if (abort_sh) {
@@ -221,7 +296,7 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
         ++lap0;
       }
       if (++t0 == n) t0 = 0;
-      e_it += (uint64_t)M;
+      if (++ci == kSqaChunk) ci = 0;
     }
     // the next step starts at stream index base + per_step + M - 1: M - 1 past where the loop ended
     q0 += M - 1;
@@ -235,7 +310,7 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
     if (p.trace || st == p.steps - 1) {
       long long acc = 0;
       for (int i = warp; i < n; i += nw) {
-        const int f = sqa_field(p.rows + (size_t)i * RW, sp, W, p.P, lane);
+        const int f = sqa_field<P>(p.rows + (size_t)i * RW, sp, W, lane);
         acc += ((sp[i >> 5] >> (i & 31)) & 1u) ? -(long long)f : (long long)f;
       }
       if (lane == 0) ered[warp] = acc;
@@ -245,8 +320,9 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
         for (int w = 0; w < nw; ++w) t += ered[w];
         p.energy[p.trace ? (size_t)r * p.steps + st : (size_t)r] = -t / 2;
       }
-      __syncthreads();
     }
+    // the next step's reference thresholds overwrite thr only after every decision of this one
+    __syncthreads();
   }
   if (!ok && tid == 0) {
     // every issued copy completes before the CTA's shared memory goes away
@@ -255,7 +331,7 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
   }
   __syncthreads();
   if (ok)
-    for (int k = tid; k < M * W; k += blockDim.x) p.spins[(size_t)r * M * W + k] = sp[k];
+    for (int k = tid; k < M * W; k += blockDim.x) p.spins[(size_t)r * M * W + k] = sp[(k / W) * SPS + k % W];
 }
 
 // Initial slices as bits [R][M][W]. Reference mode (pre_calculate.cu:38-51, :186-191, :213): spin i
@@ -288,7 +364,8 @@ __global__ void sqa_init_kernel(uint32_t *spins, uint32_t *rnd, int n, int W, in
   }
 }
 
-// Bit-plane rows of J ([n][n] FP32 integers, |J| < 2^P) into [n][RW]: one thread per 32 couplings.
+// Bit-plane rows of J ([n][n] FP32 integers, |J| < 2^P) into [n][RW]: per 32-coupling word the sign
+// word then the P magnitude words, the row's sum of |J| after them; one thread per word.
 __global__ void sqa_rows_kernel(const float *J, int n, int W, int P, int RW, uint32_t *rows) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)n * W) return;
@@ -306,10 +383,30 @@ __global__ void sqa_rows_kernel(const float *J, int n, int W, int P, int RW, uin
     abs_sum += a;
   }
   uint32_t *row = rows + (size_t)i * RW;
-  row[w] = sign;
-  for (int k = 0; k < P; ++k) row[(k + 1) * W + w] = mag[k];
+  row[(size_t)w * (P + 1)] = sign;
+  for (int k = 0; k < P; ++k) row[(size_t)w * (P + 1) + k + 1] = mag[k];
   // the row's sum of |J| (warps of one row reduce through an atomic; the word starts at 0)
   atomicAdd(&row[(P + 1) * W], (uint32_t)abs_sum);
+}
+
+// The kernel for P magnitude planes (|J| < 2^P, P <= 7).
+const void *sqa_kernel_for(int P) {
+  switch (P) {
+    case 1: return reinterpret_cast<const void *>(&sqa_kernel<1>);
+    case 2: return reinterpret_cast<const void *>(&sqa_kernel<2>);
+    case 3: return reinterpret_cast<const void *>(&sqa_kernel<3>);
+    case 4: return reinterpret_cast<const void *>(&sqa_kernel<4>);
+    case 5: return reinterpret_cast<const void *>(&sqa_kernel<5>);
+    case 6: return reinterpret_cast<const void *>(&sqa_kernel<6>);
+    default: return reinterpret_cast<const void *>(&sqa_kernel<7>);
+  }
+}
+
+// cudaLaunchKernel argument array for a kernel taking one SqaArgs by value
+void **args_of(SqaArgs &a) {
+  static thread_local void *ptr[1];
+  ptr[0] = &a;
+  return ptr;
 }
 
 sb_status fail(sb_ctx *ctx, sb_status s, const std::string &msg) {
@@ -367,15 +464,22 @@ extern "C" sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *prob, const sb_
   const int W = (((n + 31) / 32) + 3) / 4 * 4;
   const int RW = (P + 1) * W + 4;
   const size_t spin_words = (size_t)M * W;
-  // ring slots: the M rows of one iteration plus up to kSqaAhead rows ahead
+  // thresholds: one per spin (reference mode) or per (iteration, slice) of a chunk (hash mode)
+  const size_t thr_words = ((prm->rng_mode == SB_SQA_RNG_REFERENCE ? (size_t)n : (size_t)kSqaChunk * M) + 3) & ~(size_t)3;
+  // shared-memory strides: a slot of RS = 16 (mod 32) words, a slice of SPS = 8 (mod 32) words
+  const int RS = RW + ((16 - RW % 32) + 32) % 32, SPS = W + ((8 - W % 32) + 32) % 32;
+  const size_t sp_words = (size_t)M * SPS;
+  // ring slots: the M rows of one iteration plus up to kSqaAhead rows ahead; the deepest ring that
+  // lets two CTAs (two replicas) share an SM, else the deepest that fits one
   int S = 0;
-  for (int d = kSqaAhead; d >= 1 && S == 0; --d) {
-    const size_t bytes = (size_t)(M + d) * RW * 4 + spin_words * 4 + 8 + (size_t)(M + d) * 8;
-    if (bytes <= kSqaSmemBudget) S = M + d;
-  }
+  for (size_t budget : {kSqaSmemHalf, kSqaSmemBudget})
+    for (int d = kSqaAhead; d >= 2 && S == 0; --d) {
+      const size_t bytes = (size_t)(M + d) * RS * 4 + sp_words * 4 + thr_words * 4 + (size_t)(M + d) * 8;
+      if (bytes <= budget) S = M + d;
+    }
   if (S == 0) return fail(ctx, SB_ERR_UNSUPPORTED, "sb_sqa_solve: trotter x n too large for one CTA's shared memory");
-  const size_t smem = (size_t)S * RW * 4 + spin_words * 4 + 8 + (size_t)S * 8;
-  const int threads = 32 * std::min(M, kSqaMaxWarps);
+  const size_t smem = (size_t)S * RS * 4 + sp_words * 4 + thr_words * 4 + (size_t)S * 8;
+  const int threads = 32 * ((M + kSqaSlicesPerWarp - 1) / kSqaSlicesPerWarp);
   cudaStream_t st = ctx->stream;
   cudaError_t e;
   float *dJ = nullptr, *dbeta = nullptr, *djp = nullptr;
@@ -396,7 +500,7 @@ extern "C" sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *prob, const sb_
     where = #call;                    \
     goto cleanup;                     \
   }
-  SQ_CUDA(cudaFuncSetAttribute(sqa_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SQ_CUDA(cudaFuncSetAttribute(sqa_kernel_for(P), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SQ_CUDA(cudaEventCreate(&ev0));
   SQ_CUDA(cudaEventCreate(&ev1));
   SQ_CUDA(cudaMallocAsync((void **)&dJ, (size_t)n * n * sizeof(float), st));
@@ -436,8 +540,10 @@ extern "C" sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *prob, const sb_
     a.M = M;
     a.steps = steps;
     a.S = S;
+    a.RS = RS;
+    a.SPS = SPS;
     a.trace = prm->trace ? 1 : 0;
-    sqa_kernel<<<R, threads, smem, st>>>(a);
+    SQ_CUDA(cudaLaunchKernel(sqa_kernel_for(P), dim3((unsigned)R), dim3((unsigned)threads), args_of(a), smem, st));
     SQ_CUDA(cudaGetLastError());
   }
   SQ_CUDA(cudaEventRecord(ev1, st));

@@ -48,9 +48,9 @@ WORKLOADS = {
     "uneven-batch": ("dsb", 0, 64, 1500, "grouped",
                      "uneven batch: 512 instances, N ~ U[64,4096], Erdos-Renyi density ~ U[0.05,1], "
                      "J = +-1, R=64, 1500 steps, one grouped tensor-core launch per step"),
-    "sqa": ("sqa", 4096, 152, 100, "sqa",
+    "sqa": ("sqa", 4096, 304, 100, "sqa",
             "SQA: complete N=4096, J iid +-1, M=64 Trotter slices, 100 annealing steps (the sizes of "
-            "SQA_fully/fully_test/pre_calculate.cu), one replica per SM"),
+            "SQA_fully/fully_test/pre_calculate.cu), 304 replicas (two per SM)"),
     "serving": ("dsb", 0, 32, 0, "serving",
                 "serving stream: Poisson arrivals at 200/s, N log-uniform in [128,16384], density "
                 "~ U[0.01,1], J ~ U{-8..8}, R=32, step budget ~ U[500,4000]"),
