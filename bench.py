@@ -80,7 +80,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -96,7 +96,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -665,7 +665,9 @@ def run_sqa(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed bench steps (one step = one solve); default per workload, about half a "
+                         "second to a few seconds of timed work (40 solves of the default workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched-dsb")
@@ -681,6 +683,9 @@ def main():
     ap.add_argument("--instances", type=int, default=512,
                     help="uneven-batch workload: instance count (smaller cases for profiling)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"batched-dsb": 40, "plain-dsb": 40, "batched-bsb": 10, "uneven-batch": 5, "serving": 1,
+                      "sqa": 5}[args.workload] if args.impl == "ours" else 5
     if args.sb_steps > 0 and args.workload != "serving":
         v, n, R, _, field, desc = WORKLOADS[args.workload]
         WORKLOADS[args.workload] = (v, n, R, args.sb_steps, field,
