@@ -220,6 +220,32 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def plain_fp32_comparison(sb, ctx, prob, plan, vcode, n, R, sb_steps, value, stream):
+    """The plain FP32 fused kernel (one launch per SB step) on the same instance, replicas and steps:
+    its spin-updates/s, the tensor-core path's ratio to it, and whether both return the same
+    replica energies for the same seed (equal mean best energy: integer fields are exact on both)."""
+    import torch
+
+    prm_f = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=sb.FIELD_FP32, seed=4242)
+    plan_f = ctx.plan(prob, prm_f)
+    plan_f.run(seed=4242)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rf = plan_f.run(seed=4243)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    plan_f.close()
+    rt = plan.run(seed=4243)
+    plain = float(n) * R * sb_steps / (ms * 1e-3)
+    return {"plain_fp32_value": plain, "unit": "spin-updates/s", "ratio": value / plain, "plain_ms_per_solve": ms,
+            "replica_energies_identical": bool(np.array_equal(rf.replica_energies, rt.replica_energies)),
+            "mean_best_energy": {"tensor_core": float(rt.best_energy), "plain_fp32": float(rf.best_energy)},
+            "mean_replica_energy": {"tensor_core": float(np.mean(rt.replica_energies)),
+                                    "plain_fp32": float(np.mean(rf.replica_energies))},
+            "note": "same instance, replicas, SB steps and seed; one solve each"}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -350,6 +376,8 @@ def run_ours(args, rank, world, local_rank):
                     "energy_check_ok": all(r.energy_check_ok for r in results)},
         "wall_s": wall,
     }
+    if field == "tc" and variant == "dsb" and world == 1:
+        line["vs_plain_fp32"] = plain_fp32_comparison(sb, ctx, prob, plan, vcode, n, R, sb_steps, value, stream)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(args.workload, J, h).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
