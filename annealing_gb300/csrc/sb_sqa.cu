@@ -22,8 +22,8 @@
 //     the slice's decision against a threshold -log(u) / beta made ahead of time (per step and
 //     spin in reference mode, whose random word per spin is fixed; per chunk of iterations in hash
 //     mode); one __syncthreads per iteration orders the flips before the next iteration's fields;
-//   * slot and slice strides are padded (16 and 8 words mod 32) so the four groups of a warp read
-//     different banks, and a ring shallow enough for two CTAs per SM is preferred.
+//   * slot and slice strides are padded (16 and 8 or 16 words mod 32) so the four groups of a warp
+//     read different banks, and a ring shallow enough for two CTAs per SM is preferred.
 // No two slices of one iteration touch the same spin, and a slice's Trotter neighbours read other
 // spins than the ones it flips (M <= N), so the CTA reproduces the reference's iteration semantics
 // exactly. The acceptance log is this library's own (sqa_log below; the oracle carries the same
@@ -131,7 +131,16 @@ __device__ __forceinline__ int sqa_field(const uint32_t *row, const uint32_t *sm
 template <int P, int G>
 __device__ __forceinline__ int sqa_field_group(const uint32_t *row, const uint32_t *sm, int W, int gl) {
   int acc = 0;
-  if (row) {
+  if (row && P == 1) {
+    // +-1 couplings: word pairs, one 16-byte load of (sign, magnitude) x 2 and one 8-byte load of
+    // the two spin words (W is a multiple of 4)
+#pragma unroll 4
+    for (int w = 2 * gl; w < W; w += 2 * G) {
+      const uint4 t = *reinterpret_cast<const uint4 *>(row + (size_t)w * 2);
+      const uint2 sv = *reinterpret_cast<const uint2 *>(sm + w);
+      acc += __popc(t.y & (t.x ^ sv.x)) + __popc(t.w & (t.z ^ sv.y));
+    }
+  } else if (row) {
 #pragma unroll 4
     for (int w = gl; w < W; w += G) {
       const uint32_t *g = row + (size_t)w * (P + 1);
@@ -172,8 +181,8 @@ template <int P>
 __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_constant__ SqaArgs p) {
   extern __shared__ __align__(128) uint8_t smem[];
   const int RW = p.RW, W = p.W, M = p.M, n = p.n, S = p.S, RS = p.RS, SPS = p.SPS;
-  // slot stride RS = 16 (mod 32) words and slice stride SPS = 8 (mod 32): the four lane groups of a
-  // warp read four slots / slices whose words fall in different banks
+  // slot stride RS = 16 (mod 32) words and slice stride SPS = 8 or 16 (mod 32): the four lane groups
+  // of a warp read four slots / slices whose words fall in different banks
   uint32_t *ring = reinterpret_cast<uint32_t *>(smem);      // [S][RS] (RW words used)
   uint32_t *sp = ring + (size_t)S * RS;                      // [M][SPS] (W words used)
   float *thr = reinterpret_cast<float *>(sp + (size_t)M * SPS);  // [n] (reference) or [kSqaChunk][M] (hash)
@@ -466,8 +475,10 @@ extern "C" sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *prob, const sb_
   const size_t spin_words = (size_t)M * W;
   // thresholds: one per spin (reference mode) or per (iteration, slice) of a chunk (hash mode)
   const size_t thr_words = ((prm->rng_mode == SB_SQA_RNG_REFERENCE ? (size_t)n : (size_t)kSqaChunk * M) + 3) & ~(size_t)3;
-  // shared-memory strides: a slot of RS = 16 (mod 32) words, a slice of SPS = 8 (mod 32) words
-  const int RS = RW + ((16 - RW % 32) + 32) % 32, SPS = W + ((8 - W % 32) + 32) % 32;
+  // shared-memory strides: a slot of RS = 16 (mod 32) words; a slice of SPS = 16 (mod 32) words for
+  // the word-pair loads of +-1 couplings, 8 (mod 32) otherwise
+  const int RS = RW + ((16 - RW % 32) + 32) % 32;
+  const int SPS = W + (((P == 1 ? 16 : 8) - W % 32) + 32) % 32;
   const size_t sp_words = (size_t)M * SPS;
   // ring slots: the M rows of one iteration plus up to kSqaAhead rows ahead; the deepest ring that
   // lets two CTAs (two replicas) share an SM, else the deepest that fits one

@@ -33,10 +33,12 @@ def _oracle(J, M, R, steps, rng, seed):
     (40, 40, 1, 3, "pm1"),       # as many slices as spins
     (129, 1, 3, 5, "er3"),       # one slice (its own Trotter neighbour)
     (520, 128, 1, 1, "pm1"),     # the most slices: four per warp
+    (96, 12, 2, 3, "er9"),       # |J| <= 9: four magnitude planes
+    (80, 6, 2, 3, "er127"),      # |J| <= 127, the reference's char range: seven planes
 ])
 def test_hash_mode_bit_exact(ctx, n, M, R, steps, kind):
     J = instances.complete_pm1(n, seed=n) if kind == "pm1" else \
-        instances.erdos_renyi(n, 0.6, n, jmax=int(kind[2:]))
+        instances.erdos_renyi(n, 0.6, n, jmax=int(kind[2:]), allow_zero=True)
     prm = sb.SqaParams.default(trotter=M, steps=steps, replicas=R, rng_mode=sb.SQA_RNG_HASH, seed=77, trace=1)
     res = ctx.sqa_solve(sb.Problem.from_dense(J), prm, want_spins=True)
     s, tr = _oracle(J, M, R, steps, 1, 77)
