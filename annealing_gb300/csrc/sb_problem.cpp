@@ -72,13 +72,53 @@ double sb_coupling_std(const sb_problem *p) {
   if (!p || !p->J || p->n < 2) return 0.0;
   const int n = p->n;
   double s = 0.0, s2 = 0.0;
-  for (int i = 0; i < n; ++i) {
-    const float *Ji = p->J + (size_t)i * n;
-    for (int j = 0; j < n; ++j) {
-      if (i == j) continue;
-      double v = (double)Ji[j];
-      s += v;
-      s2 += v * v;
+  const double maxj = (double)p->max_abs_j;
+  if (p->integer_valued && p->max_abs_j < 2000000000 && (double)n * n * maxj * maxj < 9.0e15) {
+    // Integer couplings whose sums stay below 2^53: the sequential double sums below are exact, so
+    // exact int64 sums (vectorised, rows dealt round-robin to host threads) give the same doubles.
+    const int nt = n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<int64_t> ps((size_t)nt, 0), ps2((size_t)nt, 0);
+    auto rows = [&](int t) {
+      int64_t a = 0, a2 = 0;
+      for (int i = t; i < n; i += nt) {
+        const float *Ji = p->J + (size_t)i * n;
+        int64_t r = 0, r2 = 0;
+        for (int j = 0; j < n; ++j) {
+          const int64_t v = (int64_t)(int32_t)Ji[j];
+          r += v;
+          r2 += v * v;
+        }
+        const int64_t d = (int64_t)(int32_t)Ji[i];  // the diagonal does not count
+        a += r - d;
+        a2 += r2 - d * d;
+      }
+      ps[t] = a;
+      ps2[t] = a2;
+    };
+    if (nt == 1) {
+      rows(0);
+    } else {
+      std::vector<std::thread> th;
+      for (int t = 1; t < nt; ++t) th.emplace_back(rows, t);
+      rows(0);
+      for (auto &x : th) x.join();
+    }
+    int64_t a = 0, a2 = 0;
+    for (int t = 0; t < nt; ++t) {
+      a += ps[t];
+      a2 += ps2[t];
+    }
+    s = (double)a;
+    s2 = (double)a2;
+  } else {
+    for (int i = 0; i < n; ++i) {
+      const float *Ji = p->J + (size_t)i * n;
+      for (int j = 0; j < n; ++j) {
+        if (i == j) continue;
+        double v = (double)Ji[j];
+        s += v;
+        s2 += v * v;
+      }
     }
   }
   double cnt = (double)n * (double)(n - 1);
