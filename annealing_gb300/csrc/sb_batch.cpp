@@ -298,7 +298,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
         const auto &gi = g.insts[k];
         spins[k].resize(gi.n);
         for (int i = 0; i < gi.n; ++i) spins[k][i] = xb[k][i] > 0.0f ? 1 : -1;
-        if (sb_energy_i64(b->probs[k], spins[k].data(), &e64[k]) == SB_OK)
+        if (sbh::energy_i64(b->probs[k], spins[k].data(), &e64[k], 1) == SB_OK)
           okv[k] = (double)e64[k] == energies[k][best[k]] ? 1 : 0;
       }
     });

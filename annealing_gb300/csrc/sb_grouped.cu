@@ -235,7 +235,7 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   g.kbytes = fp4 ? g.Kp / 2 : g.Kp;
   g.Rp = (g.R + nr - 1) / nr * nr;
   g.xp = (g.n + 3) / 4 * 4;
-  g.c0 = prm->c0 > 0.0f ? prm->c0 : sb_default_c0(p);
+  g.c0 = prm->c0 > 0.0f ? prm->c0 : sbh::default_c0(p, 1);  // prepared one instance per thread
   g.dt = prm->dt;
   g.dta0 = prm->dt * prm->a0;
   cudaError_t e;

@@ -13,6 +13,11 @@ sb_status load_graph(const char *path, const sb_graph_opts *opts, sb_problem *ou
                      std::string &err);
 void set_thread_error(const std::string &e);
 const char *thread_error();
+// sb_energy_i64 / sb_coupling_std / sb_default_c0 on a given number of host threads (0: as many as
+// pay for the size, up to 8); callers that already run one instance per thread pass 1.
+sb_status energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out, int threads);
+double coupling_std(const sb_problem *p, int threads);
+float default_c0(const sb_problem *p, int threads);
 }  // namespace sbh
 
 namespace sbk {

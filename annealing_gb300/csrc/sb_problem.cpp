@@ -68,7 +68,26 @@ float sb_pump(float a0, int32_t t, int32_t steps) {
   return a0 - a;
 }
 
-double sb_coupling_std(const sb_problem *p) {
+double sb_coupling_std(const sb_problem *p) { return sbh::coupling_std(p, 0); }
+
+float sb_default_c0(const sb_problem *p) { return sbh::default_c0(p, 0); }
+
+}  // extern "C"
+
+namespace {
+int auto_threads(int n, int threads) {
+  if (threads > 0) return threads;
+  return n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+}
+}  // namespace
+
+float sbh::default_c0(const sb_problem *p, int threads) {
+  double sd = sbh::coupling_std(p, threads);
+  if (!(sd > 0.0)) sd = 1.0;
+  return (float)(0.5 / (sqrt((double)(p ? p->n : 1)) * sd));
+}
+
+double sbh::coupling_std(const sb_problem *p, int threads) {
   if (!p || !p->J || p->n < 2) return 0.0;
   const int n = p->n;
   double s = 0.0, s2 = 0.0;
@@ -76,7 +95,7 @@ double sb_coupling_std(const sb_problem *p) {
   if (p->integer_valued && p->max_abs_j < 2000000000 && (double)n * n * maxj * maxj < 9.0e15) {
     // Integer couplings whose sums stay below 2^53: the sequential double sums below are exact, so
     // exact int64 sums (vectorised, rows dealt round-robin to host threads) give the same doubles.
-    const int nt = n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    const int nt = auto_threads(n, threads);
     std::vector<int64_t> ps((size_t)nt, 0), ps2((size_t)nt, 0);
     auto rows = [&](int t) {
       int64_t a = 0, a2 = 0;
@@ -127,13 +146,15 @@ double sb_coupling_std(const sb_problem *p) {
   return var > 0.0 ? sqrt(var) : 0.0;
 }
 
-float sb_default_c0(const sb_problem *p) {
-  double sd = sb_coupling_std(p);
-  if (!(sd > 0.0)) sd = 1.0;
-  return (float)(0.5 / (sqrt((double)(p ? p->n : 1)) * sd));
-}
+extern "C" {
 
 sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out) {
+  return sbh::energy_i64(p, spins, out, 0);
+}
+
+}  // extern "C"
+
+sb_status sbh::energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out, int threads) {
   if (!p || !p->J || !spins || !out || p->n <= 0) return SB_ERR_INVALID_ARG;
   const int n = p->n;
   if (p->h)
@@ -174,7 +195,7 @@ sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out) 
   };
   // large problems: rows dealt round-robin to host threads (the triangle stays balanced); the
   // integer sum does not depend on the split
-  const int nt = n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
+  const int nt = auto_threads(n, threads);
   std::vector<int64_t> part((size_t)nt, 0);
   std::vector<char> ok((size_t)nt, 1);
   if (nt == 1) {
@@ -194,7 +215,7 @@ sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out) 
   return SB_OK;
 }
 
-double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
+extern "C" double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
   if (!p || !p->J || !spins || p->n <= 0) return 0.0;
   const int n = p->n;
   double e = 0.0;
@@ -207,8 +228,6 @@ double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
   }
   return e;
 }
-
-}  // extern "C"
 
 // ---------------------------------------------------------------------------------------------
 // Problem bookkeeping.

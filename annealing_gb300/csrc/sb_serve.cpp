@@ -347,7 +347,7 @@ void Server::check_loop() {
       check_q.pop_front();
     }
     Req *r = job.first;
-    if (job.second == SB_OK && sb_energy_i64(r->prob, r->spins.data(), &r->e64) == SB_OK)
+    if (job.second == SB_OK && sbh::energy_i64(r->prob, r->spins.data(), &r->e64, 1) == SB_OK)
       r->ok = (double)r->e64 == r->best ? 1 : 0;
     finish(r, job.second, job.second == SB_OK ? "" : (r->err.empty() ? std::string("device error") : r->err));
   }
