@@ -380,6 +380,9 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
     a.do_local = (t + 1 < p.steps) ? 1 : 0;
     a.energy = eslot;
     a.status = pl->dstatus;
+    // consecutive steps overlap (J is never written inside the loop); profiled runs time each
+    // launch alone between its events
+    a.overlap = evs ? 0 : 1;
     e = sbk::launch_plain_step(a, st);
     if (e != cudaSuccess) return e;
     if (evs) cudaEventRecord((*evs)[2 * t + 1], st);

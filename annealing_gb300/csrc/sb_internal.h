@@ -31,6 +31,10 @@ struct PlainStep {
   int m, do_local;
   double *energy;          // [R] energy of s(x_in) (dSB only; may be null)
   uint32_t *status;
+  // 1: launched with programmatic stream serialization, so the launch overlaps the previous
+  // kernel's tail (J must not be written by that kernel: J copies start before the wait for it)
+  int overlap;
+  int stages;              // set by launch_plain_step
 };
 
 struct PlainEnergy {
@@ -39,6 +43,7 @@ struct PlainEnergy {
   const float *x;
   double *energy;          // [R] += energy of s(x)
   uint32_t *status;
+  int stages;              // set by launch_plain_energy
 };
 
 // Sets kernel attributes (dynamic shared memory limits) once per process; call before any capture.

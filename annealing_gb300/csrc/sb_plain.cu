@@ -3,17 +3,25 @@
 // Replaces, per step, the reference's two launches UpdateTwice<<<N/64,64>>> + cublasSgemv
 // (SB/CUDA_GPU/m2_opt.cu:168-169) with one kernel that computes the field and the update:
 //   * each CTA owns 8 rows of J (one warp per row) and up to 8 replicas;
-//   * the CTA's J rows are staged into shared memory by bulk TMA copies (cp.async.bulk) in
-//     512-float chunks through a two-stage mbarrier ring, the multiplied vector chunk
-//     (x, or sign(x) for dSB) is staged beside it with 128-bit loads;
+//   * up to two replicas per CTA (the latency-bound case: one replica per trial), the CTA's J rows
+//     and its replicas' x are staged into shared memory by bulk copies (cp.async.bulk) in
+//     512-float chunks through an mbarrier ring of up to four stages (all of K in flight at once
+//     for N <= 2048 and one replica); dSB takes sign(x) as it reads x. With more replicas per CTA
+//     (bound by shared-memory loads of the replica vectors) J goes through a two-stage ring and the
+//     replicas' chunk (signs for dSB) is staged once by the CTA's threads;
+//   * consecutive steps overlap through programmatic dependent launch: a step's kernel starts
+//     during the previous one's tail, requests its J rows, and waits for the previous step only
+//     before it touches x;
 //   * each warp forms its row's dot products with float4 shared-memory reads and a shuffle
-//     reduction, then one lane per replica applies the SB update and writes x (ping-pong) and y
-//     (in place: every element has exactly one owner);
+//     reduction; the fields then go through shared memory to consecutive threads, which apply the
+//     SB update (the aSB sub-steps in FP64 on one or two warps per CTA) and write x (ping-pong)
+//     and y (in place: every element has exactly one owner);
 //   * dSB also reduces -1/2 s_i f_i - h_i s_i per replica (block reduction + one atomic per
 //     replica), which is the energy of s(t) and costs nothing extra because f = J s(t).
 // Every wait is bounded: a timeout sets a status bit and the kernel returns.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "sb_internal.h"
 #include "sb_ptx.cuh"
@@ -25,7 +33,13 @@ constexpr int kRows = 8;
 constexpr int kThreads = 256;
 constexpr int kChunk = 512;  // floats per row per stage
 constexpr int kMaxRB = 8;
-constexpr size_t kSmemBytes = (size_t)(2 * kRows * kChunk + kMaxRB * kChunk) * sizeof(float);
+constexpr int kMaxStages = 4;
+// Shared memory: up to two replicas per CTA a ring of up to kStageBudget bytes (all of K for
+// N <= 2048 at one replica, 3 CTAs per SM); with more, the two-stage J ring and one replica
+// chunk buffer (48 KB, 4 CTAs per SM).
+constexpr int kStageBudget = 72 * 1024;
+constexpr size_t kWideSmem = (size_t)(2 * kRows * kChunk + kMaxRB * kChunk) * sizeof(float);
+constexpr size_t kSmemBytes = kStageBudget;
 
 __device__ __forceinline__ float sgn(float v) { return v > 0.0f ? 1.0f : -1.0f; }
 
@@ -62,26 +76,124 @@ struct RowAcc {
   Acc v[kMaxRB];
 };
 
-// Shared machinery: stream the CTA's J rows through shared memory and form dot products with the
-// CTA's replica vectors. MODE 0: v = x; MODE 1: v = sign(x).
+// One chunk of a row's dot products with rb replica vectors in shared memory (row stride `stride`
+// floats); SIGN: use sign(v).
+template <bool SIGN, typename Acc>
+__device__ __forceinline__ void dot_chunk(const float4 *jr, const float *sx, int stride, int len, int rb,
+                                          int lane, Acc (&acc)[kMaxRB]) {
+  for (int q = lane; q < (len >> 2); q += 32) {
+    const float4 jv = jr[q];
+#pragma unroll
+    for (int rr = 0; rr < kMaxRB; ++rr) {
+      if (rr < rb) {
+        float4 vv = reinterpret_cast<const float4 *>(sx + rr * stride)[q];
+        if (SIGN) {
+          vv.x = sgn(vv.x);
+          vv.y = sgn(vv.y);
+          vv.z = sgn(vv.z);
+          vv.w = sgn(vv.w);
+        }
+        if constexpr (sizeof(Acc) == 8) {
+          acc[rr] += (double)jv.x * (double)vv.x + (double)jv.y * (double)vv.y +
+                     (double)jv.z * (double)vv.z + (double)jv.w * (double)vv.w;
+        } else {
+          acc[rr] = __fmaf_rn(jv.x, vv.x, acc[rr]);
+          acc[rr] = __fmaf_rn(jv.y, vv.y, acc[rr]);
+          acc[rr] = __fmaf_rn(jv.z, vv.z, acc[rr]);
+          acc[rr] = __fmaf_rn(jv.w, vv.w, acc[rr]);
+        }
+      }
+    }
+  }
+}
+
+// Butterfly sums: every lane of the row's warp ends with the row's fields.
+template <typename Acc>
+__device__ __forceinline__ void warp_sums(Acc (&acc)[kMaxRB]) {
+#pragma unroll
+  for (int rr = 0; rr < kMaxRB; ++rr) {
+    Acc v = acc[rr];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    acc[rr] = v;
+  }
+}
+
+// Field of the CTA's rows for at most two replicas per CTA, where a step is latency-bound. Stage s
+// of the ring holds J[rows][kChunk] and x[rb][kChunk] of one chunk of K, both copied by
+// cp.async.bulk and counted on full[s]; `stages` chunks are in flight (all of K for N <= 2048 at
+// one replica). dSB takes sign(x) as it reads x. J does not change during a solve, so the first
+// stages' J rows are requested before grid_dep_wait: when this launch overlaps the previous step's
+// kernel, those copies run during its tail and only the x copies wait for it.
 template <int MODE, typename Acc>
-__device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, int n, int row0,
-                                           int rows, const float *__restrict__ xv, int xp, int r0,
-                                           int rb, float *sJ, float *sV, uint64_t *full,
-                                           Acc (&acc)[kMaxRB]) {
+__device__ __forceinline__ bool field_rows_ring(const float *__restrict__ J, int jp, int row0, int rows,
+                                                const float *__restrict__ xv, int xp, int r0, int rb,
+                                                int stages, float *smem, uint64_t *full,
+                                                Acc (&acc)[kMaxRB]) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = (jp + kChunk - 1) / kChunk;
-#pragma unroll
-  for (int q = 0; q < kMaxRB; ++q) acc[q] = Acc(0);
+  const int stage_floats = (kRows + rb) * kChunk;
+  auto len_of = [&](int c) { return min(kChunk, jp - c * kChunk); };
+  auto issue_j = [&](int c) {
+    const int s = c % stages;
+    const uint32_t bytes = (uint32_t)len_of(c) * 4u;
+    ptx::mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)(rows + rb));
+    for (int w = 0; w < rows; ++w)
+      ptx::bulk_g2s(smem + s * stage_floats + w * kChunk, J + (size_t)(row0 + w) * jp + c * kChunk,
+                    bytes, &full[s]);
+  };
+  auto issue_x = [&](int c) {
+    const int s = c % stages;
+    const uint32_t bytes = (uint32_t)len_of(c) * 4u;
+    for (int rr = 0; rr < rb; ++rr)
+      ptx::bulk_g2s(smem + s * stage_floats + (kRows + rr) * kChunk,
+                    xv + (size_t)(r0 + rr) * xp + c * kChunk, bytes, &full[s]);
+  };
+  const int pre = min(nchunks, stages);
+  if (tid == 0)
+    for (int c = 0; c < pre; ++c) issue_j(c);
+  // every thread: x (and, in the caller, y) are the previous step's output
+  ptx::grid_dep_wait();
+  ptx::grid_dep_launch();
+  if (tid == 0)
+    for (int c = 0; c < pre; ++c) issue_x(c);
+  bool ok = true;
+  for (int c = 0; c < nchunks; ++c) {
+    const int s = c % stages;
+    if (!ptx::mbar_wait(&full[s], (uint32_t)((c / stages) & 1))) ok = false;
+    if (warp < rows && ok)
+      dot_chunk<MODE == 1>(reinterpret_cast<const float4 *>(smem + s * stage_floats + warp * kChunk),
+                           smem + s * stage_floats + kRows * kChunk, kChunk, len_of(c), rb, lane, acc);
+    if (c + stages < nchunks) {
+      __syncthreads();  // every warp is done with stage s before it is refilled
+      if (tid == 0 && ok) {
+        issue_j(c + stages);
+        issue_x(c + stages);
+      }
+    }
+  }
+  return ok;
+}
+
+// Field of the CTA's rows for three to eight replicas per CTA, where a step is bound by
+// shared-memory loads of the replica vectors: J rows through a two-stage ring of bulk copies, the
+// replicas' chunk (signs for dSB) staged once by the CTA's threads with 128-bit loads and shared by
+// the eight row warps. Ring: sJ[2][kRows][kChunk], then sV[kMaxRB][kChunk]. These launches do not
+// overlap the previous step's (a wave of many CTAs gains nothing from it), so nothing here waits.
+template <int MODE, typename Acc>
+__device__ __forceinline__ bool field_rows_wide(const float *__restrict__ J, int jp, int row0, int rows,
+                                                const float *__restrict__ xv, int xp, int r0, int rb,
+                                                float *smem, uint64_t *full, Acc (&acc)[kMaxRB]) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nchunks = (jp + kChunk - 1) / kChunk;
+  float *sJ = smem, *sV = smem + 2 * kRows * kChunk;
   auto issue = [&](int c) {
     const int k0 = c * kChunk;
-    const int len = min(kChunk, jp - k0);
-    const uint32_t bytes = (uint32_t)len * 4u;
-    uint64_t *bar = &full[c & 1];
-    ptx::mbar_arrive_expect_tx(bar, bytes * (uint32_t)rows);
+    const uint32_t bytes = (uint32_t)min(kChunk, jp - k0) * 4u;
+    ptx::mbar_arrive_expect_tx(&full[c & 1], bytes * (uint32_t)rows);
     for (int w = 0; w < rows; ++w)
       ptx::bulk_g2s(sJ + ((c & 1) * kRows + w) * kChunk, J + (size_t)(row0 + w) * jp + k0, bytes,
-                    bar);
+                    &full[c & 1]);
   };
   if (tid == 0) {
     issue(0);
@@ -91,7 +203,6 @@ __device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, 
   for (int c = 0; c < nchunks; ++c) {
     const int k0 = c * kChunk;
     const int len = min(kChunk, jp - k0);
-    // stage the vector chunk (len is a multiple of 4)
     for (int rr = 0; rr < rb; ++rr) {
       const float *src = xv + (size_t)(r0 + rr) * xp + k0;
       float *dst = sV + rr * kChunk;
@@ -108,78 +219,78 @@ __device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, 
     }
     if (!ptx::mbar_wait(&full[c & 1], (uint32_t)((c >> 1) & 1))) ok = false;
     __syncthreads();
-    if (warp < rows && ok) {
-      const float4 *jr = reinterpret_cast<const float4 *>(sJ + ((c & 1) * kRows + warp) * kChunk);
-      for (int q = lane; q < (len >> 2); q += 32) {
-        const float4 jv = jr[q];
-#pragma unroll
-        for (int rr = 0; rr < kMaxRB; ++rr) {
-          if (rr < rb) {
-            const float4 vv = reinterpret_cast<const float4 *>(sV + rr * kChunk)[q];
-            if constexpr (sizeof(Acc) == 8) {
-              acc[rr] += (double)jv.x * (double)vv.x + (double)jv.y * (double)vv.y +
-                         (double)jv.z * (double)vv.z + (double)jv.w * (double)vv.w;
-            } else {
-              acc[rr] = __fmaf_rn(jv.x, vv.x, acc[rr]);
-              acc[rr] = __fmaf_rn(jv.y, vv.y, acc[rr]);
-              acc[rr] = __fmaf_rn(jv.z, vv.z, acc[rr]);
-              acc[rr] = __fmaf_rn(jv.w, vv.w, acc[rr]);
-            }
-          }
-        }
-      }
-    }
+    if (warp < rows && ok)
+      dot_chunk<false>(reinterpret_cast<const float4 *>(sJ + ((c & 1) * kRows + warp) * kChunk), sV,
+                       kChunk, len, rb, lane, acc);
     __syncthreads();
     if (tid == 0 && c + 2 < nchunks && ok) issue(c + 2);
-  }
-  // every thread leaves with the same verdict, so no thread skips a later barrier
-  ok = __syncthreads_and(ok ? 1 : 0) != 0;
-#pragma unroll
-  for (int rr = 0; rr < kMaxRB; ++rr) {
-    Acc v = acc[rr];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    acc[rr] = v;
   }
   return ok;
 }
 
-template <int VARIANT>
+// The CTA's fields; WIDE (the launch's replicas per CTA > 2) selects the layout at compile time
+// (one layout per kernel instantiation). Returns the CTA-wide verdict of the bounded waits; every
+// lane of row w's warp holds its fields.
+template <int MODE, bool WIDE, typename Acc>
+__device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, int row0, int rows,
+                                           const float *__restrict__ xv, int xp, int r0, int rb, int stages,
+                                           float *smem, uint64_t *full, Acc (&acc)[kMaxRB]) {
+#pragma unroll
+  for (int q = 0; q < kMaxRB; ++q) acc[q] = Acc(0);
+  bool ok;
+  if constexpr (WIDE)
+    ok = field_rows_wide<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, smem, full, acc);
+  else
+    ok = field_rows_ring<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, stages, smem, full, acc);
+  // every thread leaves with the same verdict, so no thread skips a later barrier
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  warp_sums(acc);
+  return ok;
+}
+
+template <int VARIANT, bool WIDE>
 __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  float *sJ = reinterpret_cast<float *>(smem);
-  float *sV = sJ + 2 * kRows * kChunk;
-  __shared__ __align__(8) uint64_t full[2];
+  __shared__ __align__(8) uint64_t full[kMaxStages];
   __shared__ double red[kRows][kMaxRB];
+  __shared__ float fsh[kRows][kMaxRB];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.x * kRows;
   const int r0 = blockIdx.y * a.rb;
   const int rb = min(a.rb, a.R - r0);
   const int rows = min(kRows, a.n - row0);
-  if (rows <= 0 || rb <= 0 || rb > kMaxRB) {
+  if (rows <= 0 || rb <= 0 || rb > kMaxRB || a.stages < 1 || a.stages > kMaxStages) {
+    ptx::grid_dep_wait();
     if (tid == 0) atomicOr(a.status, kErrBadShape);
     return;
   }
   if (tid == 0) {
-    ptx::mbar_init(&full[0], 1);
-    ptx::mbar_init(&full[1], 1);
+    for (int s = 0; s < a.stages; ++s) ptx::mbar_init(&full[s], 1);
     ptx::fence_mbar_init();
   }
   if (tid < kRows * kMaxRB) red[tid / kMaxRB][tid % kMaxRB] = 0.0;
   __syncthreads();
   float acc[kMaxRB];
-  const bool ok = field_rows<VARIANT == 2 ? 1 : 0, float>(a.J, a.jp, a.n, row0, rows, a.x_in,
-                                                          a.xp, r0, rb, sJ, sV, full, acc);
+  const bool ok = field_rows<VARIANT == 2 ? 1 : 0, WIDE, float>(
+      a.J, a.jp, row0, rows, a.x_in, a.xp, r0, rb, a.stages, reinterpret_cast<float *>(smem), full, acc);
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
     return;
   }
-  if (warp < rows && lane < rb) {
-    float f = 0.0f;
+  // The fields go through shared memory so that the update runs on consecutive threads (thread
+  // t: row t % kRows, replica t / kRows) instead of one lane in each row's warp: the aSB local
+  // sub-steps are FP64, and packing the CTA's elements into one or two warps issues that FP64
+  // work once per CTA instead of once per row.
+  if (lane == 0 && warp < rows) {
 #pragma unroll
     for (int rr = 0; rr < kMaxRB; ++rr)
-      if (rr == lane) f = acc[rr];
-    const int i = row0 + warp, r = r0 + lane;
+      if (rr < rb) fsh[warp][rr] = acc[rr];
+  }
+  __syncthreads();
+  const int w = tid % kRows, rr = tid / kRows;
+  if (rr < rb && w < rows) {
+    const float f = fsh[w][rr];
+    const int i = row0 + w, r = r0 + rr;
     const size_t k = (size_t)r * a.xp + i;
     float x = a.x_in[k], y = a.y[k];
     const float hv = a.h ? a.h[i] : 0.0f;
@@ -189,7 +300,7 @@ __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
     } else {
       const float s = sgn(x);
       if (VARIANT == 2 && a.energy)
-        red[warp][lane] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
+        red[w][rr] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
       sb_update(f, hv, a.pump, a.c0, a.dt, a.dta0, x, y);
     }
     a.x_out[k] = x;
@@ -199,38 +310,37 @@ __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
     __syncthreads();
     if (tid < rb) {
       double e = 0.0;
-      for (int w = 0; w < rows; ++w) e += red[w][tid];
+      for (int q = 0; q < rows; ++q) e += red[q][tid];
       atomicAdd(a.energy + r0 + tid, e);
     }
   }
 }
 
-template <typename Acc>
+template <typename Acc, bool WIDE>
 __global__ void __launch_bounds__(kThreads) plain_energy_kernel(PlainEnergy a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  float *sJ = reinterpret_cast<float *>(smem);
-  float *sV = sJ + 2 * kRows * kChunk;
-  __shared__ __align__(8) uint64_t full[2];
+  __shared__ __align__(8) uint64_t full[kMaxStages];
   __shared__ double red[kRows][kMaxRB];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.x * kRows;
   const int r0 = blockIdx.y * a.rb;
   const int rb = min(a.rb, a.R - r0);
   const int rows = min(kRows, a.n - row0);
-  if (rows <= 0 || rb <= 0 || rb > kMaxRB) {
+  if (rows <= 0 || rb <= 0 || rb > kMaxRB || a.stages < 1 || a.stages > kMaxStages) {
+    ptx::grid_dep_wait();
     if (tid == 0) atomicOr(a.status, kErrBadShape);
     return;
   }
   if (tid == 0) {
-    ptx::mbar_init(&full[0], 1);
-    ptx::mbar_init(&full[1], 1);
+    for (int s = 0; s < a.stages; ++s) ptx::mbar_init(&full[s], 1);
     ptx::fence_mbar_init();
   }
   if (tid < kRows * kMaxRB) red[tid / kMaxRB][tid % kMaxRB] = 0.0;
   __syncthreads();
   Acc acc[kMaxRB];
   const bool ok =
-      field_rows<1, Acc>(a.J, a.jp, a.n, row0, rows, a.x, a.xp, r0, rb, sJ, sV, full, acc);
+      field_rows<1, WIDE, Acc>(a.J, a.jp, row0, rows, a.x, a.xp, r0, rb, a.stages,
+                               reinterpret_cast<float *>(smem), full, acc);
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
     return;
@@ -333,17 +443,22 @@ int grid_for(size_t total) {
 }  // namespace
 
 template <typename K>
-void set_smem_once(K kernel) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+void set_smem_once(K kernel, size_t bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 struct PlainAttrInit {
   PlainAttrInit() {
-    set_smem_once(plain_step_kernel<0>);
-    set_smem_once(plain_step_kernel<1>);
-    set_smem_once(plain_step_kernel<2>);
-    set_smem_once(plain_energy_kernel<float>);
-    set_smem_once(plain_energy_kernel<double>);
+    set_smem_once(plain_step_kernel<0, false>, kSmemBytes);
+    set_smem_once(plain_step_kernel<1, false>, kSmemBytes);
+    set_smem_once(plain_step_kernel<2, false>, kSmemBytes);
+    set_smem_once(plain_step_kernel<0, true>, kWideSmem);
+    set_smem_once(plain_step_kernel<1, true>, kWideSmem);
+    set_smem_once(plain_step_kernel<2, true>, kWideSmem);
+    set_smem_once(plain_energy_kernel<float, false>, kSmemBytes);
+    set_smem_once(plain_energy_kernel<double, false>, kSmemBytes);
+    set_smem_once(plain_energy_kernel<float, true>, kWideSmem);
+    set_smem_once(plain_energy_kernel<double, true>, kWideSmem);
   }
 };
 
@@ -351,34 +466,74 @@ void plain_attrs() { static PlainAttrInit once; }
 
 void init_kernel_attributes() { plain_attrs(); }
 
-cudaError_t launch_plain_step(const PlainStep &a, cudaStream_t st) {
+// Ring depth for at most two replicas per CTA: as many stages as fit the budget (at least two), at
+// most the number of chunks. A CTA with fewer replicas than the launch's (the last replica block)
+// uses smaller stages inside the same ring.
+size_t plain_smem(int rb, int stages) {
+  return rb > 2 ? kWideSmem : (size_t)stages * (kRows + rb) * kChunk * sizeof(float);
+}
+
+int plain_stages(int jp, int rb) {
+  const int nchunks = (jp + kChunk - 1) / kChunk;
+  int s = kStageBudget / ((kRows + rb) * kChunk * (int)sizeof(float));
+  s = s < 2 ? 2 : (s > kMaxStages ? kMaxStages : s);
+  return s < nchunks ? s : nchunks;
+}
+
+template <int V, bool WIDE>
+cudaError_t launch_step_variant(const PlainStep &a, dim3 grid, cudaStream_t st) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = plain_smem(a.rb, a.stages);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (a.overlap && !WIDE) ? 1 : 0;  // only the ring layout waits in grid_dep_wait
+  return cudaLaunchKernelEx(&cfg, plain_step_kernel<V, WIDE>, a);
+}
+
+cudaError_t launch_plain_step(const PlainStep &a0, cudaStream_t st) {
   plain_attrs();
-  if (a.rb < 1 || a.rb > kMaxRB || a.jp % 4 || a.xp % 4 || a.jp > a.xp) return cudaErrorInvalidValue;
+  if (a0.rb < 1 || a0.rb > kMaxRB || a0.jp % 4 || a0.xp % 4 || a0.jp > a0.xp || a0.jp < 4)
+    return cudaErrorInvalidValue;
+  PlainStep a = a0;
+  a.stages = plain_stages(a.jp, a.rb);
   dim3 grid((a.n + kRows - 1) / kRows, (a.R + a.rb - 1) / a.rb);
+  const bool wide = a.rb > 2;
   switch (a.variant) {
     case 0:
-      plain_step_kernel<0><<<grid, kThreads, kSmemBytes, st>>>(a);
-      break;
+      return wide ? launch_step_variant<0, true>(a, grid, st) : launch_step_variant<0, false>(a, grid, st);
     case 1:
-      plain_step_kernel<1><<<grid, kThreads, kSmemBytes, st>>>(a);
-      break;
+      return wide ? launch_step_variant<1, true>(a, grid, st) : launch_step_variant<1, false>(a, grid, st);
     case 2:
-      plain_step_kernel<2><<<grid, kThreads, kSmemBytes, st>>>(a);
-      break;
+      return wide ? launch_step_variant<2, true>(a, grid, st) : launch_step_variant<2, false>(a, grid, st);
     default:
       return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
-cudaError_t launch_plain_energy(const PlainEnergy &a, bool fp64, cudaStream_t st) {
+cudaError_t launch_plain_energy(const PlainEnergy &a0, bool fp64, cudaStream_t st) {
   plain_attrs();
-  if (a.rb < 1 || a.rb > kMaxRB || a.jp % 4 || a.xp % 4 || a.jp > a.xp) return cudaErrorInvalidValue;
+  if (a0.rb < 1 || a0.rb > kMaxRB || a0.jp % 4 || a0.xp % 4 || a0.jp > a0.xp || a0.jp < 4)
+    return cudaErrorInvalidValue;
+  PlainEnergy a = a0;
+  a.stages = plain_stages(a.jp, a.rb);
   dim3 grid((a.n + kRows - 1) / kRows, (a.R + a.rb - 1) / a.rb);
-  if (fp64) {
-    plain_energy_kernel<double><<<grid, kThreads, kSmemBytes, st>>>(a);
+  const size_t smem = plain_smem(a.rb, a.stages);
+  if (a.rb > 2) {
+    if (fp64)
+      plain_energy_kernel<double, true><<<grid, kThreads, smem, st>>>(a);
+    else
+      plain_energy_kernel<float, true><<<grid, kThreads, smem, st>>>(a);
   } else {
-    plain_energy_kernel<float><<<grid, kThreads, kSmemBytes, st>>>(a);
+    if (fp64)
+      plain_energy_kernel<double, false><<<grid, kThreads, smem, st>>>(a);
+    else
+      plain_energy_kernel<float, false><<<grid, kThreads, smem, st>>>(a);
   }
   return cudaGetLastError();
 }

@@ -94,6 +94,15 @@ __device__ __forceinline__ void prefetch_tmap(const void *tmap) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }
 
+// Programmatic dependent launch. grid_dep_wait: the calling thread waits until the grid before this
+// one in the stream has completed and its memory operations are visible (returns at once when this
+// launch was not allowed to overlap it). grid_dep_launch: this CTA lets the next grid of the stream
+// start launching; the next grid still waits in its own grid_dep_wait for this one to finish.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Generic-proxy global writes -> later async-proxy (TMA) reads.
 __device__ __forceinline__ void fence_proxy_async_global() {
   asm volatile("fence.proxy.async.global;" ::: "memory");
