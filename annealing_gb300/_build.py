@@ -21,7 +21,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["sb_plain.cu", "sb_tc.cu", "sb_tc_fp8.cu", "sb_tc_bf16.cu", "sb_tc_split.cu", "sb_tc_fp4.cu", "sb_grouped.cu", "sb_noalloc.cu",
-               "sb_api.cpp", "sb_batch.cpp", "sb_problem.cpp", "sb_serve.cpp", "sb_analysis.cpp", "sb_sqa.cu"]
+               "sb_api.cpp", "sb_batch.cpp", "sb_problem.cpp", "sb_serve.cpp", "sb_analysis.cpp", "sb_sqa.cu",
+               "sb_nmfa.cpp"]
 
 
 def _nvcc() -> str:
@@ -86,9 +87,12 @@ def build_oracle(force: bool = False) -> str:
     exact = os.path.join(ORACLE, "sb_oracle.c")
     base = os.path.join(ORACLE, "sb_cpu_baseline.c")
     sqa = os.path.join(ORACLE, "sqa_oracle.c")
+    nmfa = os.path.join(ORACLE, "nmfa_oracle.c")
+    math_h = os.path.join(ORACLE, "sb_math_oracle.h")
     o1 = os.path.join(out_dir, "sb_oracle.o")
     o2 = os.path.join(out_dir, "sb_cpu_baseline.o")
     o3 = os.path.join(out_dir, "sqa_oracle.o")
+    o4 = os.path.join(out_dir, "nmfa_oracle.o")
     lib = os.path.join(ORACLE, "libsboracle.so")
     jobs = []
     if force or not _newer(o1, [exact]):
@@ -97,14 +101,17 @@ def build_oracle(force: bool = False) -> str:
     if force or not _newer(o2, [base]):
         jobs.append(["gcc", "-O3", "-std=gnu11", "-fPIC", "-ffp-contract=fast", "-pthread",
                      "-c", base, "-o", o2])
-    if force or not _newer(o3, [sqa]):
+    if force or not _newer(o3, [sqa, math_h]):
         jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
                      "-c", sqa, "-o", o3])
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    if force or not _newer(o4, [nmfa, math_h]):
+        jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                     "-c", nmfa, "-o", o4])
+    with ThreadPoolExecutor(max_workers=4) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
     if force or jobs or not os.path.exists(lib):
-        _run(["gcc", "-shared", "-o", lib, o1, o2, o3, "-lm", "-pthread"])
+        _run(["gcc", "-shared", "-o", lib, o1, o2, o3, o4, "-lm", "-pthread"])
     return lib
 
 

@@ -9,6 +9,11 @@
 // SA_naive/CUDA_GPU/tests/test.sh:26-32). --variant sqa runs simulated quantum annealing, the
 // drop-in for the reference's SQA program (SQA_fully/fully_test/pre_calculate.cu: output.txt holds
 // each trial's final slice-0 energy, :242-246; --trace prints each step's energy, :236).
+// --variant nmfa runs noisy mean-field annealing, the drop-in for NMFA/CUDA_GPU/Ising.cpp (100
+// stages of its beta schedule, alpha = sigma = 0.15, seed 1234, one sample; the first line of stdout
+// is the elapsed ms it prints, Ising.cpp:48); --steps sets the stages, --replicas the samples,
+// --noise / --recombination sigma and alpha; output.txt holds each sample's energy
+// E = sum_{i<j} J_ij s_i s_j and best_spins.txt the best sample.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -22,12 +27,12 @@
 static void usage() {
   printf(
       "Usage:\n"
-      "  sb <graph> [--variant asb|bsb|dsb|sqa] [--steps S] [--replicas R] [--seed X]\n"
+      "  sb <graph> [--variant asb|bsb|dsb|sqa|nmfa] [--steps S] [--replicas R] [--seed X]\n"
       "             [--dt DT] [--a0 A0] [--c0 C0] [--xi XI] [--mts-m M]\n"
       "             [--field auto|fp32|tc] [--init uniform|reference]\n"
       "             [--n N] [--index-base 0|1] [--strict] [--trace] [--device D]\n"
       "             [--out output.txt] [--spins best_spins.txt] [--json]\n"
-      "             [--target E [--p-target P]] [--trotter M]\n"
+      "             [--target E [--p-target P]] [--trotter M] [--noise S] [--recombination A]\n"
       "Graph file: N [E] then lines 'i j J_ij' (i != j) and optional 'i i h_i'.\n");
 }
 
@@ -72,6 +77,39 @@ static int run_sqa(sb_ctx *ctx, const sb_problem *prob, const sb_sqa_params &q, 
   return 0;
 }
 
+// --variant nmfa: one sb_nmfa_solve
+static int run_nmfa(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params &q, const std::string &out_path,
+                    const std::string &spins_path, bool json) {
+  std::vector<int8_t> spins((size_t)prob->n);
+  std::vector<double> energies((size_t)q.samples);
+  sb_nmfa_result r;
+  memset(&r, 0, sizeof(r));
+  r.best_spins = spins.data();
+  r.energies = energies.data();
+  const sb_status s = sb_nmfa_solve(ctx, prob, &q, &r);
+  if (s != SB_OK) {
+    fprintf(stderr, "sb: nmfa failed: %s (%s)\n", sb_status_string(s), sb_last_error(ctx));
+    return 1;
+  }
+  printf("%g\n", r.device_ms);
+  FILE *f = fopen(out_path.c_str(), "w");
+  if (f) {
+    for (int k = 0; k < q.samples; ++k) fprintf(f, "%.17g\n", energies[k]);
+    fclose(f);
+  }
+  f = fopen(spins_path.c_str(), "w");
+  if (f) {
+    for (int i = 0; i < prob->n; ++i) fprintf(f, "%d\n", (int)spins[i]);
+    fclose(f);
+  }
+  if (json)
+    printf("{\"n\": %d, \"samples\": %d, \"stages\": %d, \"best_energy\": %.17g, \"best_sample\": %d, "
+           "\"energy_check_ok\": %d, \"device_ms\": %.6f, \"total_ms\": %.6f, \"spin_updates_per_s\": %.6e}\n",
+           prob->n, q.samples, q.stages, r.best_energy, r.best_sample, r.energy_check_ok, r.device_ms, r.total_ms,
+           r.spin_updates_per_s);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) {
     usage();
@@ -85,19 +123,27 @@ int main(int argc, char **argv) {
   sb_graph_opts go;
   sb_graph_opts_default(&go);
   int variant = SB_ASB;
-  bool sqa = false;
+  bool sqa = false, nmfa = false;
   // first pass: variant (it sets the defaults)
   for (int i = 1; i < argc; ++i)
     if (!strcmp(argv[i], "--variant") && i + 1 < argc) {
       const char *v = argv[i + 1];
       variant = !strcmp(v, "bsb") ? SB_BSB : !strcmp(v, "dsb") ? SB_DSB : SB_ASB;
       sqa = !strcmp(v, "sqa");
+      nmfa = !strcmp(v, "nmfa");
     }
   sb_params p;
   sb_params_default(&p, variant);
   sb_sqa_params q;
   sb_sqa_params_default(&q);
   if (sqa) p.steps = q.steps;
+  sb_nmfa_params nq;
+  sb_nmfa_params_default(&nq);
+  if (nmfa) {
+    p.steps = nq.stages;
+    p.replicas = nq.samples;
+    p.seed = nq.seed;
+  }
   for (int i = 1; i < argc; ++i) {
     const char *a = argv[i];
     auto next = [&](void) -> const char * {
@@ -134,6 +180,8 @@ int main(int argc, char **argv) {
       have_target = true;
     } else if (!strcmp(a, "--p-target")) p_target = atof(next());
     else if (!strcmp(a, "--trotter")) q.trotter = atoi(next());
+    else if (!strcmp(a, "--noise")) nq.noise = (float)atof(next());
+    else if (!strcmp(a, "--recombination")) nq.recombination = (float)atof(next());
     else if (!strcmp(a, "-h") || !strcmp(a, "--help")) {
       usage();
       return 0;
@@ -169,6 +217,15 @@ int main(int argc, char **argv) {
     q.rng_mode = p.init_mode == SB_INIT_REFERENCE ? SB_SQA_RNG_REFERENCE : SB_SQA_RNG_HASH;
     q.trace = p.trace;
     const int rc = run_sqa(ctx, &prob, q, out_path, spins_path, json);
+    sb_destroy(ctx);
+    sb_problem_free(&prob);
+    return rc;
+  }
+  if (nmfa) {
+    nq.stages = p.steps;
+    nq.samples = p.replicas;
+    nq.seed = (uint32_t)p.seed;
+    const int rc = run_nmfa(ctx, &prob, nq, out_path, spins_path, json);
     sb_destroy(ctx);
     sb_problem_free(&prob);
     return rc;

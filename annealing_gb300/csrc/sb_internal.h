@@ -46,8 +46,30 @@ struct PlainEnergy {
   int stages;              // set by launch_plain_energy
 };
 
+// One NMFA sweep (noisy mean-field annealing, NMFA/CUDA_GPU/src/nmfa.cu:99-136) over every sample:
+// the field J s through the plain kernel's rows machinery, then per (sample, spin)
+// s' = keep s + mix tanh(beta (norm_i f_i + z)). sb_plain.cu.
+struct NmfaSweep {
+  int n, R, jp, xp, rb;    // R samples, rb samples per CTA
+  const float *J;          // [n][jp]
+  const float *norm;       // [n]: -1 / sqrt(sum_j |J_ij|), 0 for an empty row
+  const float *s_in;       // [R][xp] states before the sweep (padding 0)
+  float *s_out;            // [R][xp] states after it
+  uint32_t *rng;           // [5][R][xp] XORWOW words of each (sample, spin)
+  float *z1;               // [R][xp] the stage's second Gaussian sample
+  int32_t *samples;        // [R][n] receives sign(s') as +-1 (the last sweep), or null
+  float beta, noise, keep, mix;  // keep = 1 - recombination, mix = recombination
+  int first;               // 1: first sweep of a stage, which draws the stage's two samples
+  uint32_t *status;
+  int overlap;             // as PlainStep::overlap
+  int stages;              // set by launch_nmfa_sweep
+};
+
 // Sets kernel attributes (dynamic shared memory limits) once per process; call before any capture.
 void init_kernel_attributes();
+cudaError_t launch_nmfa_sweep(const NmfaSweep &a, cudaStream_t st);
+// Initial XORWOW words of every (sample, spin); rng as in NmfaSweep.
+cudaError_t launch_nmfa_seed(uint32_t *rng, int n, int R, int xp, uint32_t seed, cudaStream_t st);
 cudaError_t launch_plain_step(const PlainStep &a, cudaStream_t st);
 cudaError_t launch_plain_energy(const PlainEnergy &a, bool fp64, cudaStream_t st);
 

@@ -24,6 +24,7 @@
 #include <string.h>
 
 #include "sb_internal.h"
+#include "sb_math.cuh"
 #include "sb_ptx.cuh"
 
 namespace sbk {
@@ -363,6 +364,120 @@ __global__ void __launch_bounds__(kThreads) plain_energy_kernel(PlainEnergy a) {
   }
 }
 
+// ---- NMFA: noisy mean-field annealing (NMFA/CUDA_GPU/src/nmfa.cu:54-140) ----
+// The reference runs one CTA per sample and one thread per spin with its row of J in registers; here
+// the samples are the replicas of the plain kernel's layout (8 rows of J per CTA, up to 8 samples),
+// and each of a stage's two sweeps is one fused launch. A sweep reads the states of the previous
+// sweep (the reference's sweeps inside a stage have no barrier between one warp's writes and
+// another's reads; for up to 32 spins, one warp, it computes exactly this).
+
+// XORWOW (Marsaglia, "Xorshift RNGs", p. 5) on words w[0..3] and the additive counter w[4], in the
+// update order of nmfa.cu:29-40.
+__device__ __forceinline__ uint32_t xorwow(uint32_t (&w)[5]) {
+  uint32_t t = w[3];
+  t ^= t >> 2;
+  t ^= t << 1;
+  w[3] = w[2];
+  w[2] = w[1];
+  w[1] = w[0];
+  t ^= w[0];
+  t ^= w[0] << 4;
+  w[0] = t;
+  w[4] += 362437u;
+  return t + w[4];
+}
+
+// The stage's two Gaussian samples by the Box-Muller transform (nmfa.cu:103-109): two words a, b,
+// radius sqrt(-2 log(a / 2^32)) noise, angle 2 pi b / 2^32; z0 = sin(angle) radius, z1 = cos.
+__device__ __forceinline__ void nmfa_gauss(uint32_t (&w)[5], float noise, float &z0, float &z1) {
+  const uint32_t a = xorwow(w);
+  const uint32_t b = xorwow(w);
+  const float u = __fmul_rn(__uint2float_rn(a), 0x1p-32f);
+  const float rad = __fmul_rn(__fsqrt_rn(__fmul_rn(-2.0f, sbm::log_unit(u))), noise);
+  const float ang = __fmul_rn(__uint2float_rn(b), 0x1.921fb6p-30f);
+  float sn, cs;
+  sbm::sincos_f(ang, sn, cs);
+  z0 = __fmul_rn(sn, rad);
+  z1 = __fmul_rn(cs, rad);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[kMaxStages];
+  __shared__ float fsh[kRows][kMaxRB];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * kRows;
+  const int r0 = blockIdx.y * a.rb;
+  const int rb = min(a.rb, a.R - r0);
+  const int rows = min(kRows, a.n - row0);
+  if (rows <= 0 || rb <= 0 || rb > kMaxRB || a.stages < 1 || a.stages > kMaxStages) {
+    ptx::grid_dep_wait();
+    if (tid == 0) atomicOr(a.status, kErrBadShape);
+    return;
+  }
+  if (tid == 0) {
+    for (int s = 0; s < a.stages; ++s) ptx::mbar_init(&full[s], 1);
+    ptx::fence_mbar_init();
+  }
+  __syncthreads();
+  float acc[kMaxRB];
+  const bool ok = field_rows<0, WIDE, float>(a.J, a.jp, row0, rows, a.s_in, a.xp, r0, rb, a.stages,
+                                             reinterpret_cast<float *>(smem), full, acc);
+  if (!ok) {
+    if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
+    return;
+  }
+  if (lane == 0 && warp < rows) {
+#pragma unroll
+    for (int q = 0; q < kMaxRB; ++q)
+      if (q < rb) fsh[warp][q] = acc[q];
+  }
+  __syncthreads();
+  const int w = tid % kRows, rr = tid / kRows;
+  if (rr < rb && w < rows) {
+    const int i = row0 + w, r = r0 + rr;
+    const size_t k = (size_t)r * a.xp + i;
+    const size_t plane = (size_t)a.R * a.xp;
+    float z;
+    if (a.first) {
+      uint32_t wd[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) wd[q] = a.rng[q * plane + k];
+      float z1;
+      nmfa_gauss(wd, a.noise, z, z1);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) a.rng[q * plane + k] = wd[q];
+      a.z1[k] = z1;
+    } else {
+      z = a.z1[k];
+    }
+    // nmfa.cu:124-128: mf = f norm + z; s' = (1 - alpha) s + alpha tanh(beta mf)
+    const float mf = __fadd_rn(__fmul_rn(fsh[w][rr], a.norm[i]), z);
+    const float th = sbm::tanh_f(__fmul_rn(mf, a.beta));
+    const float st = __fadd_rn(__fmul_rn(a.keep, a.s_in[k]), __fmul_rn(a.mix, th));
+    a.s_out[k] = st;
+    if (a.samples) a.samples[(size_t)r * a.n + i] = st > 0.0f ? 1 : -1;
+  }
+}
+
+// Initial words of (sample r, spin i), as nmfa.cu:62-76 seeds thread i of block r: t = seed + n r + i
+// (32-bit), four xorshift32 steps (nmfa.cu:43-47) giving words 0..3, the counter word 0.
+__global__ void nmfa_seed_kernel(uint32_t *rng, int n, int R, int xp, uint32_t seed) {
+  const size_t total = (size_t)n * R, plane = (size_t)R * xp;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / n, i = e % n, k = r * xp + i;
+    uint32_t t = seed + (uint32_t)n * (uint32_t)r + (uint32_t)i;
+    for (int q = 0; q < 4; ++q) {
+      t ^= t << 13;
+      t ^= t >> 17;
+      t ^= t << 5;
+      rng[q * plane + k] = t;
+    }
+    rng[4 * plane + k] = 0u;
+  }
+}
+
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z ^= z >> 30;
   z *= 0xBF58476D1CE4E5B9ULL;
@@ -459,6 +574,8 @@ struct PlainAttrInit {
     set_smem_once(plain_energy_kernel<double, false>, kSmemBytes);
     set_smem_once(plain_energy_kernel<float, true>, kWideSmem);
     set_smem_once(plain_energy_kernel<double, true>, kWideSmem);
+    set_smem_once(nmfa_sweep_kernel<false>, kSmemBytes);
+    set_smem_once(nmfa_sweep_kernel<true>, kWideSmem);
   }
 };
 
@@ -535,6 +652,33 @@ cudaError_t launch_plain_energy(const PlainEnergy &a0, bool fp64, cudaStream_t s
     else
       plain_energy_kernel<float, false><<<grid, kThreads, smem, st>>>(a);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nmfa_sweep(const NmfaSweep &a0, cudaStream_t st) {
+  plain_attrs();
+  if (a0.rb < 1 || a0.rb > kMaxRB || a0.jp % 4 || a0.xp % 4 || a0.jp > a0.xp || a0.jp < 4)
+    return cudaErrorInvalidValue;
+  NmfaSweep a = a0;
+  a.stages = plain_stages(a.jp, a.rb);
+  const bool wide = a.rb > 2;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((a.n + kRows - 1) / kRows, (a.R + a.rb - 1) / a.rb);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = plain_smem(a.rb, a.stages);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (a.overlap && !wide) ? 1 : 0;
+  return wide ? cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<true>, a)
+              : cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<false>, a);
+}
+
+cudaError_t launch_nmfa_seed(uint32_t *rng, int n, int R, int xp, uint32_t seed, cudaStream_t st) {
+  nmfa_seed_kernel<<<grid_for((size_t)n * R), 256, 0, st>>>(rng, n, R, xp, seed);
   return cudaGetLastError();
 }
 

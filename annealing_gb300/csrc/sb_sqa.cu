@@ -26,8 +26,8 @@
 //     read different banks, and a ring shallow enough for two CTAs per SM is preferred.
 // No two slices of one iteration touch the same spin, and a slice's Trotter neighbours read other
 // spins than the ones it flips (M <= N), so the CTA reproduces the reference's iteration semantics
-// exactly. The acceptance log is this library's own (sqa_log below; the oracle carries the same
-// function), so host and device results are bit-identical.
+// exactly. The acceptance log is this library's own (sbm::log_unit, sb_math.cuh; the oracle carries the
+// same function), so host and device results are bit-identical.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -43,6 +43,7 @@
 #include "sb_ctx.h"
 #include "sb_host.h"
 #include "sb_internal.h"
+#include "sb_math.cuh"
 #include "sb_ptx.cuh"
 
 namespace {
@@ -64,27 +65,6 @@ struct SqaArgs {
   int n, W, P, RW, M, steps, S, trace;
   int RS, SPS;            // shared-memory strides of a ring slot and of a slice (bank-spread padding)
 };
-
-// log(u) for u in [0, 1] (the oracle's sqa_log, operation for operation): u = 2^e m with m in
-// [sqrt(1/2), sqrt(2)), log u = e ln 2 + 2 atanh((m - 1) / (m + 1)), atanh by its series to s^9.
-__device__ __forceinline__ float sqa_log(float u) {
-  if (!(u > 0.0f)) return -INFINITY;
-  const uint32_t b = __float_as_uint(u);
-  int e = (int)((b >> 23) & 0xFFu) - 127;
-  float m = __uint_as_float((b & 0x007FFFFFu) | 0x3F800000u);
-  if (m > 0x1.6a09e6p+0f) {
-    m = __fmul_rn(m, 0.5f);
-    e += 1;
-  }
-  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
-  const float z = __fmul_rn(s, s);
-  float q = __fmaf_rn(z, 0x1.c71c72p-4f, 0x1.24924ap-3f);
-  q = __fmaf_rn(z, q, 0x1.99999ap-3f);
-  q = __fmaf_rn(z, q, 0x1.555556p-2f);
-  const float at = __fmaf_rn(__fmul_rn(s, z), q, s);
-  const float fe = (float)e;
-  return __fmaf_rn(fe, 0x1.62e4p-1f, __fmaf_rn(fe, 0x1.7f7d1cp-20f, __fmul_rn(2.0f, at)));
-}
 
 __device__ __forceinline__ uint64_t sqa_mix64(uint64_t z) {
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
@@ -171,7 +151,7 @@ __device__ __forceinline__ int sqa_field_group(const uint32_t *row, const uint32
 
 // Acceptance threshold -log(u) / beta of the reference's test (pre_calculate.cu:79), with this
 // library's log.
-__device__ __forceinline__ float sqa_threshold(float u, float beta) { return __fdiv_rn(-sqa_log(u), beta); }
+__device__ __forceinline__ float sqa_threshold(float u, float beta) { return __fdiv_rn(-sbm::log_unit(u), beta); }
 
 constexpr int kSqaChunk = 16;  // wavefront iterations whose hash-mode thresholds are made at once
 constexpr int kSqaGroup = 8;   // lanes per slice in the field sums

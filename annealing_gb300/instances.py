@@ -39,6 +39,12 @@ def erdos_renyi(n: int, density: float, seed: int, jmax: int = 1, allow_zero: bo
     return up + up.T
 
 
+def nmfa_fully(n: int = 1024, seed: int = 1234) -> np.ndarray:
+    """The NMFA test graph's distribution (NMFA/CUDA_GPU/tests/fully.py:6-15): each pair is an edge
+    with probability 1/2, its weight uniform in {-1, 0, +1}; seeded."""
+    return erdos_renyi(n, 0.5, seed, jmax=1, allow_zero=True)
+
+
 def uneven_batch(count: int = 512, nmin: int = 64, nmax: int = 4096, seed: int = 1234):
     """(N, density, seed) of the uneven-size batch: N ~ U[nmin, nmax], density ~ U[0.05, 1]."""
     rng = np.random.default_rng(seed)

@@ -181,6 +181,58 @@ class SqaResult:
     final_spins: Optional[np.ndarray] = None    # [replicas, trotter, n]
 
 
+class NmfaParams(C.Structure):
+    _fields_ = [
+        ("samples", C.c_int32),
+        ("stages", C.c_int32),
+        ("betas", C.POINTER(C.c_float)),
+        ("noise", C.c_float),
+        ("recombination", C.c_float),
+        ("seed", C.c_uint32),
+    ]
+
+    @classmethod
+    def default(cls, **kw) -> "NmfaParams":
+        p = cls()
+        lib().sb_nmfa_params_default(C.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+
+class NmfaResultStruct(C.Structure):
+    _fields_ = [
+        ("samples", C.POINTER(C.c_int8)),
+        ("states", C.POINTER(C.c_float)),
+        ("energies", C.POINTER(C.c_double)),
+        ("best_spins", C.POINTER(C.c_int8)),
+        ("best_energy", C.c_double),
+        ("best_sample", C.c_int32),
+        ("energy_check_ok", C.c_int32),
+        ("device_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("spin_updates_per_s", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+
+@dataclass
+class NmfaResult:
+    samples: np.ndarray          # [samples, n] int8 +-1
+    energies: np.ndarray         # [samples] E = sum_{i<j} J_ij s_i s_j
+    best_spins: np.ndarray
+    best_energy: float
+    best_sample: int
+    energy_check_ok: bool
+    device_ms: float
+    total_ms: float
+    spin_updates_per_s: float
+    kernel_launches: int
+    states: Optional[np.ndarray] = None   # [samples, n] final mean-field states
+
+
 class TtsStruct(C.Structure):
     _fields_ = [
         ("trials", C.c_int32),
@@ -218,6 +270,13 @@ _SIGS = {
     "sb_sqa_schedule": (None, [C.c_int32, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "sb_sqa_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(SqaParams),
                                C.POINTER(SqaResultStruct)]),
+    "sb_nmfa_params_default": (C.c_int, [C.POINTER(NmfaParams)]),
+    "sb_nmfa_schedule": (C.c_int, [C.c_int32, C.POINTER(C.c_float)]),
+    "sb_nmfa_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(NmfaParams),
+                                C.POINTER(NmfaResultStruct)]),
+    "sb_gpu_nmfa": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32,
+                              C.c_int32, C.POINTER(C.c_int32), C.c_float, C.c_float, C.c_uint32,
+                              C.POINTER(C.c_float)]),
     "sb_time_to_target": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32, C.c_int32,
                                     C.c_int32, C.c_double, C.c_double, C.c_double, C.POINTER(TtsStruct)]),
     "sb_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(DeviceOpts)]),
@@ -511,6 +570,49 @@ class Context:
                          total_ms=r.total_ms, spin_updates_per_s=r.spin_updates_per_s,
                          kernel_launches=r.kernel_launches, energy_trace=trace, final_spins=allsp)
 
+    def nmfa_solve(self, problem: Problem, params: Optional[NmfaParams] = None, betas=None,
+                   want_states: bool = False) -> NmfaResult:
+        """Noisy mean-field annealing (sb_nmfa_solve); betas (stages,) overrides the schedule."""
+        params = params if params is not None else NmfaParams.default()
+        keep = None
+        if betas is not None:
+            keep = np.ascontiguousarray(betas, np.float32)
+            params.stages = len(keep)
+            params.betas = keep.ctypes.data_as(C.POINTER(C.c_float))
+        n, R = problem.n, params.samples
+        samples = np.zeros((R, n), np.int8)
+        energies = np.zeros(R, np.float64)
+        best = np.zeros(n, np.int8)
+        states = np.zeros((R, n), np.float32) if want_states else None
+        r = NmfaResultStruct()
+        r.samples = samples.ctypes.data_as(C.POINTER(C.c_int8))
+        r.energies = energies.ctypes.data_as(C.POINTER(C.c_double))
+        r.best_spins = best.ctypes.data_as(C.POINTER(C.c_int8))
+        if states is not None:
+            r.states = states.ctypes.data_as(C.POINTER(C.c_float))
+        try:
+            _check(lib().sb_nmfa_solve(self.h, C.byref(problem.s), C.byref(params), C.byref(r)), self.h)
+        finally:
+            if keep is not None:
+                params.betas = None
+        return NmfaResult(samples=samples, energies=energies, best_spins=best, best_energy=r.best_energy,
+                          best_sample=r.best_sample, energy_check_ok=bool(r.energy_check_ok), device_ms=r.device_ms,
+                          total_ms=r.total_ms, spin_updates_per_s=r.spin_updates_per_s,
+                          kernel_launches=r.kernel_launches, states=states)
+
+    def gpu_nmfa(self, J: np.ndarray, betas, num_samples: int, noise: float = 0.15, recombination: float = 0.15,
+                 seed: int = 1234):
+        """The reference's entry point gpu_nmfa (sb_gpu_nmfa): (samples [num_samples, n] int32, elapsed ms)."""
+        J = np.ascontiguousarray(J, np.float32)
+        b = np.ascontiguousarray(betas, np.float32)
+        n = J.shape[0]
+        out = np.zeros((num_samples, n), np.int32)
+        ms = C.c_float()
+        _check(lib().sb_gpu_nmfa(self.h, n, J.ctypes.data_as(C.POINTER(C.c_float)), b.ctypes.data_as(C.POINTER(C.c_float)),
+                                 len(b), num_samples, out.ctypes.data_as(C.POINTER(C.c_int32)), noise, recombination,
+                                 seed, C.byref(ms)), self.h)
+        return out, ms.value
+
     def plan(self, problem: Problem, params: Params, want_state: bool = False) -> Plan:
         return Plan(self, problem, params, want_state)
 
@@ -561,6 +663,13 @@ def sqa_schedule(steps: int, trotter: int):
     j = np.zeros(steps, np.float32)
     lib().sb_sqa_schedule(steps, trotter, b.ctypes.data_as(C.POINTER(C.c_float)), j.ctypes.data_as(C.POINTER(C.c_float)))
     return b, j
+
+
+def nmfa_schedule(stages: int = 100) -> np.ndarray:
+    """The NMFA inverse temperatures of NMFA/CUDA_GPU/Ising.cpp:37-43 (sb_nmfa_schedule)."""
+    b = np.zeros(stages, np.float32)
+    _check(lib().sb_nmfa_schedule(stages, b.ctypes.data_as(C.POINTER(C.c_float))))
+    return b
 
 
 def time_to_target(energies: np.ndarray, times_ms: np.ndarray, threshold: float, run_ms: float,

@@ -51,6 +51,10 @@ WORKLOADS = {
     "sqa": ("sqa", 4096, 304, 100, "sqa",
             "SQA: complete N=4096, J iid +-1, M=64 Trotter slices, 100 annealing steps (the sizes of "
             "SQA_fully/fully_test/pre_calculate.cu), 304 replicas (two per SM)"),
+    "nmfa": ("nmfa", 1024, 1024, 100, "nmfa",
+             "NMFA: N=1024 (the size of NMFA/CUDA_GPU/Ising.cpp), J drawn as NMFA/CUDA_GPU/tests/fully.py "
+             "(edge probability 1/2, weight in {-1,0,+1}), 100 stages x 2 sweeps of its beta schedule, "
+             "1024 samples"),
     "serving": ("dsb", 0, 32, 0, "serving",
                 "serving stream: Poisson arrivals at 200/s, N log-uniform in [128,16384], density "
                 "~ U[0.01,1], J ~ U{-8..8}, R=32, step budget ~ U[500,4000]"),
@@ -192,6 +196,8 @@ def run_reference(args, rank, world):
         return
     if args.workload == "sqa":
         return run_reference_sqa(args, world)
+    if args.workload == "nmfa":
+        return run_reference_nmfa(args, world)
     J, h = make_problem(args.workload)
     variant, n, R, steps, field, desc = WORKLOADS[args.workload]
     budget = args.cpu_budget or max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
@@ -690,6 +696,122 @@ def run_sqa(args, rank, world, local_rank):
     ctx.close()
 
 
+def nmfa_cpu_sample(J, budget_s=10.0):
+    """The NMFA oracle (single-threaded C restatement of gpu_nmfa_kernel with the library's sweep
+    semantics) on whole anneals of one sample, as many as fit ~budget_s (at least one)."""
+    from oracle import binding as orc
+
+    n = J.shape[0]
+    betas = orc.nmfa_schedule(100)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        orc.nmfa_run(J, 1, betas, 0.15, 0.15, 1234 + k)
+        k += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n * 2 * 100 * k / dt, "unit": "spin-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{k} anneals (100 stages x 2 sweeps) x 1 sample (N={n}), single thread", "seconds": dt}
+
+
+def run_reference_nmfa(args, world):
+    from annealing_gb300 import instances
+
+    _, n, R, stages, _, desc = WORKLOADS["nmfa"]
+    J = instances.nmfa_fully(n, seed=1234)
+    budget = args.cpu_budget or max(2.0, min(10.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        nmfa_cpu_sample(J, budget_s=budget / 4)
+    samples = [nmfa_cpu_sample(J, budget_s=budget) for _ in range(args.steps)]
+    value = float(statistics.median(s["value"] for s in samples))
+    updates = float(n) * R * 2 * stages
+    line = {
+        "impl": "reference", "metric": "NMFA spin-updates/s", "value": value, "unit": "spin-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * updates / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": desc, "n": n, "samples": R, "stages": stages},
+        "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": 1, "kind": "port",
+                         "sample": samples[0]["sample"]},
+        "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the C restatement of NMFA/CUDA_GPU/src/nmfa.cu (oracle/nmfa_oracle.c), one thread",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_nmfa(args, rank, world, local_rank):
+    import torch
+
+    import annealing_gb300 as sb
+    from annealing_gb300 import instances
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    _, n, R, stages, _, desc = WORKLOADS["nmfa"]
+    J = instances.nmfa_fully(n, seed=1234)
+    prob = sb.Problem.from_dense(J)
+    betas = sb.nmfa_schedule(stages)
+    stream = torch.cuda.current_stream(dev)
+    ctx = sb.Context(local_rank, stream=stream.cuda_stream)
+    prm = sb.NmfaParams.default(samples=R, stages=stages, seed=1234 + rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for k in range(args.warmup):
+        ctx.nmfa_solve(prob, prm)
+        ctx.gpu_nmfa(J, betas, R, 0.15, 0.15, 1234 + k)
+    barrier()
+    dev_ms, tot_ms, results = [], [], []
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize(dev)
+            prm.seed = 7000 + k
+            results.append(ctx.nmfa_solve(prob, prm))
+            dev_ms.append(results[-1].device_ms)
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            ctx.gpu_nmfa(J, betas, R, 0.15, 0.15, 9000 + k)  # H2D of J, anneal, D2H of the samples
+            tot_ms.append(1e3 * (time.perf_counter() - t0))
+        barrier()
+    updates = float(n) * R * 2 * stages
+    total_dev = reduce_max(float(sum(dev_ms)), world)
+    total_e2e = reduce_max(float(sum(tot_ms)), world)
+    value = weak_scaling_value(updates, world, args.steps, total_dev)
+    e2e = weak_scaling_value(updates, world, args.steps, total_e2e)
+    if rank != 0:
+        ctx.close()
+        return
+    flops = 2.0 * n * n * R * 2 * stages / (total_dev / args.steps * 1e-3)
+    line = {
+        "metric": "NMFA spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (field, mean-field states)", "data": "synthetic (seeded graph)",
+        "config": {"workload": desc, "n": n, "samples": R, "stages": stages, "sweeps_per_stage": 2,
+                   "parallelism": f"samples-only x{world}",
+                   "l2": "flushed between timed solves (256 MB write outside the timed region)"},
+        "e2e": {"value": e2e, "unit": "spin-updates/s", "h2d_bytes_per_step": int(J.nbytes + betas.nbytes),
+                "d2h_bytes_per_step": int(R * n * 4), "entry_point": "sb_gpu_nmfa (the reference's gpu_nmfa)"},
+        "gpu_launches": int(sum(r.kernel_launches for r in results)),
+        "throughput": {"field_flops_per_s": flops,
+                       "note": "FP32 CUDA-core field, 2 N^2 FLOPs per sample and sweep; one fused launch per sweep"},
+        "clocks": clk.summary(),
+        "quality": {"best_energy": min(r.best_energy for r in results),
+                    "mean_energy": float(np.mean([r.energies.mean() for r in results])),
+                    "energy_check_ok": all(r.energy_check_ok for r in results)},
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = nmfa_cpu_sample(J)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -713,7 +835,7 @@ def main():
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched-dsb": 40, "plain-dsb": 40, "batched-bsb": 10, "uneven-batch": 5, "serving": 1,
-                      "sqa": 5}[args.workload] if args.impl == "ours" else 5
+                      "sqa": 5, "nmfa": 5}[args.workload] if args.impl == "ours" else 5
     if args.sb_steps > 0 and args.workload != "serving":
         v, n, R, _, field, desc = WORKLOADS[args.workload]
         WORKLOADS[args.workload] = (v, n, R, args.sb_steps, field,
@@ -733,6 +855,8 @@ def main():
         run_serving(args, rank, world, local_rank)
     elif args.workload == "sqa":
         run_sqa(args, rank, world, local_rank)
+    elif args.workload == "nmfa":
+        run_nmfa(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1 and args.impl == "ours":

@@ -15,6 +15,10 @@
  *                      (filled into sb_result.energy_trace)
  *   sb_sqa_solve    <- the SQA program SQA_fully/fully_test/pre_calculate.cu (main :158-257;
  *                      preapare_spins :38-51, reduce :99-149, update_spins :53-84)
+ *   sb_nmfa_solve / sb_gpu_nmfa
+ *                   <- gpu_nmfa (NMFA/CUDA_GPU/src/cuda_nmfa.h:10-14, nmfa.cu:142-199) and its
+ *                      kernel gpu_nmfa_kernel (nmfa.cu:54-140); sb_nmfa_schedule <- the beta
+ *                      schedule of NMFA/CUDA_GPU/Ising.cpp:37-43
  *   sb_time_to_target
  *                   <- the trace analysis of plot_energy_decrease/plot.r:88-240 and the
  *                      success-probability time of SA_naive/CUDA_GPU/tests/test.sh:26-32
@@ -367,6 +371,58 @@ sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *p, const sb_sqa_params *pa
 sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, int32_t n, int32_t replicas,
                                int32_t steps, uint64_t seed, float dt, float a0, float c0,
                                float *d_x, float *d_y, double *d_energies, void *stream);
+
+/* ---- NMFA: noisy mean-field annealing (NMFA/CUDA_GPU/src/nmfa.cu:54-199) ----
+ * Per sample, from s = 0, for each stage (inverse temperature beta) two Gaussian samples z0, z1 are
+ * drawn (a per-(sample, spin) XORWOW stream seeded as nmfa.cu:62-76, Box-Muller as :103-109) and two
+ * sweeps run, the first with z0 and the second with z1 (:114-134):
+ *     s_i <- (1 - alpha) s_i + alpha tanh(beta (norm_i sum_j J_ij s_j + z)),
+ *     norm_i = -1 / sqrt(sum_j |J_ij|)   (:93; 0 for a row without couplings),
+ * and the sample is sign(s) (s > 0 ? +1 : -1, :139). NMFA minimises E(s) = sum_{i<j} J_ij s_i s_j
+ * (its field is -J s); energies below are in that convention (the opposite sign to H above). A
+ * sweep reads the states of the previous sweep: the reference's two sweeps of a stage have no
+ * barrier between warps, which for up to 32 spins (one warp) is exactly this and beyond that depends
+ * on warp timing. The transcendental functions are this library's own FP32 ones (the same
+ * operations in the CPU oracle), the reference's are CUDA fast-math intrinsics. */
+typedef struct sb_nmfa_params {
+  int32_t samples;          /* independent samples (the reference's num_samples, one CTA each there) */
+  int32_t stages;           /* number of betas (the reference's SWEEP, Ising.cpp:10) */
+  const float *betas;       /* [stages], or NULL for sb_nmfa_schedule(stages) */
+  float noise;              /* Gaussian noise scale sigma (Ising.cpp:12, SIGMA = 0.15) */
+  float recombination;      /* alpha (Ising.cpp:11, ALPHA = 0.15) */
+  uint32_t seed;            /* Ising.cpp:13, SEED = 1234 */
+} sb_nmfa_params;
+
+typedef struct sb_nmfa_result {
+  int8_t *samples;          /* [samples][n] +-1, or NULL */
+  float *states;            /* [samples][n] final mean-field states, or NULL */
+  double *energies;         /* [samples] E of each sample (NMFA's convention), or NULL */
+  int8_t *best_spins;       /* [n] the sample of lowest E, or NULL */
+  double best_energy;       /* its E */
+  int32_t best_sample;
+  int32_t energy_check_ok;  /* 1 when the host re-evaluation of the best sample agrees */
+  double device_ms;         /* seeding + all sweeps + the energy pass, CUDA events */
+  double total_ms;          /* the whole call, host clock */
+  double spin_updates_per_s;  /* n * samples * 2 * stages / device time */
+  int64_t kernel_launches;
+} sb_nmfa_result;
+
+/* samples 1, stages 100 with the reference schedule, noise 0.15, recombination 0.15, seed 1234
+ * (NMFA/CUDA_GPU/Ising.cpp:8-13) */
+sb_status sb_nmfa_params_default(sb_nmfa_params *p);
+/* betas[k] = 1/16 + k (8 - 1/16) / stages, accumulated in FP32 as Ising.cpp:37-43 does */
+sb_status sb_nmfa_schedule(int32_t stages, float *betas);
+/* NMFA on one problem (no fields h: the reference has none). */
+sb_status sb_nmfa_solve(sb_ctx *ctx, const sb_problem *p, const sb_nmfa_params *params, sb_nmfa_result *res);
+/* The reference's entry point (cuda_nmfa.h:10-14: float gpu_nmfa(int N, float *J, std::vector<float>
+ * betas, int num_samples, int *samples, float noise, float recombination, uint32_t seed)) with C
+ * types: J dense n x n row-major on the host, betas[num_betas], samples[num_samples][n] receives
+ * +-1, *elapsed_ms the device time (the reference's return value). The reference throws
+ * std::invalid_argument when N differs from its compile-time size; here any n >= 1 runs and bad
+ * arguments return SB_ERR_INVALID_ARG. */
+sb_status sb_gpu_nmfa(sb_ctx *ctx, int32_t n, const float *J, const float *betas, int32_t num_betas,
+                      int32_t num_samples, int32_t *samples, float noise, float recombination, uint32_t seed,
+                      float *elapsed_ms);
 
 #ifdef __cplusplus
 }

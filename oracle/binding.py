@@ -18,6 +18,7 @@ f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
 u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
 def lib():
@@ -65,6 +66,14 @@ def lib():
             "oracle_sqa_energy": (C.c_int64, [C.c_int, i8p, i8p]),
             "oracle_sqa_run": (C.c_int, [C.c_int, i8p, C.c_int, C.c_int, f32p, f32p, C.c_int, C.c_int,
                                          C.c_void_p, C.c_uint64, i8p, C.c_void_p]),
+            "oracle_nmfa_schedule": (None, [C.c_int, f32p]),
+            "oracle_nmfa_seed": (None, [C.c_int, C.c_int, C.c_uint32, u32p]),
+            "oracle_nmfa_xorwow": (C.c_uint32, [u32p]),
+            "oracle_nmfa_gauss": (None, [u32p, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "oracle_nmfa_tanh": (C.c_float, [C.c_float]),
+            "oracle_nmfa_sincos": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "oracle_nmfa_run": (C.c_int, [C.c_int, f32p, C.c_int, f32p, C.c_int, C.c_float, C.c_float, C.c_uint32,
+                                          f32p, i32p, C.c_void_p]),
         }
         for k, (r, a) in sig.items():
             fn = getattr(L, k)
@@ -235,3 +244,47 @@ def sqa_run(J, spins, steps, rng, rnd=None, seed=0, beta=None, jperp=None):
 def sqa_energy(J, s):
     J8 = np.ascontiguousarray(J, np.float32).astype(np.int8)
     return int(lib().oracle_sqa_energy(J8.shape[0], J8, np.ascontiguousarray(s, np.int8)))
+
+
+def nmfa_schedule(stages):
+    b = np.zeros(stages, np.float32)
+    lib().oracle_nmfa_schedule(stages, b)
+    return b
+
+
+def nmfa_seed(n, R, seed):
+    """XORWOW words [R, n, 5] of every (sample, spin)."""
+    w = np.zeros((R, n, 5), np.uint32)
+    lib().oracle_nmfa_seed(n, R, seed, w)
+    return w
+
+
+def nmfa_gauss(words, noise):
+    """One stage's two Gaussian samples from a (5,) uint32 state, advanced in place."""
+    z0, z1 = C.c_float(), C.c_float()
+    lib().oracle_nmfa_gauss(words, noise, C.byref(z0), C.byref(z1))
+    return z0.value, z1.value
+
+
+def nmfa_tanh(x):
+    return lib().oracle_nmfa_tanh(x)
+
+
+def nmfa_sincos(t):
+    s, c = C.c_float(), C.c_float()
+    lib().oracle_nmfa_sincos(t, C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+def nmfa_run(J, samples, betas, noise=0.15, recombination=0.15, seed=1234, trace=False):
+    """NMFA on J [n, n]: (states [R, n] float32, samples [R, n] int32, trace [stages, R, n] or None)."""
+    J = np.ascontiguousarray(J, np.float32)
+    n = J.shape[0]
+    betas = np.ascontiguousarray(betas, np.float32)
+    st = np.zeros((samples, n), np.float32)
+    sp = np.zeros((samples, n), np.int32)
+    tr = np.zeros((len(betas), samples, n), np.float32) if trace else None
+    rc = lib().oracle_nmfa_run(n, J, samples, betas, len(betas), noise, recombination, seed, st, sp, _vp(tr))
+    if rc != 0:
+        raise ValueError("bad NMFA sizes")
+    return st, sp, tr

@@ -31,6 +31,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "sb_math_oracle.h"
+
 /* pre_calculate.cu:28-36 */
 static uint32_t sqa_xorshift32(uint32_t *state) {
   uint32_t x = *state;
@@ -47,39 +49,10 @@ static uint64_t sqa_mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-static float f_of_bits(uint32_t b) {
-  float f;
-  memcpy(&f, &b, 4);
-  return f;
-}
-
-static uint32_t bits_of_f(float f) {
-  uint32_t b;
-  memcpy(&b, &f, 4);
-  return b;
-}
-
 /* log(u) for u in [0, 1]: u = 2^e m with m in [sqrt(1/2), sqrt(2)), log u = e ln 2 + 2 atanh(s),
  * s = (m - 1) / (m + 1), atanh(s) = s + s^3/3 + s^5/5 + s^7/7 + s^9/9 (|s| <= 0.172: the next
  * term is below 2^-27). ln 2 = hi + lo with hi exact in 16 bits. log(0) = -inf. */
-float oracle_sqa_log(float u) {
-  if (!(u > 0.0f)) return -INFINITY;
-  const uint32_t b = bits_of_f(u);
-  int e = (int)((b >> 23) & 0xFFu) - 127;
-  float m = f_of_bits((b & 0x007FFFFFu) | 0x3F800000u);
-  if (m > 0x1.6a09e6p+0f) {
-    m = m * 0.5f;
-    e += 1;
-  }
-  const float s = (m - 1.0f) / (m + 1.0f);
-  const float z = s * s;
-  float q = fmaf(z, 0x1.c71c72p-4f, 0x1.24924ap-3f);
-  q = fmaf(z, q, 0x1.99999ap-3f);
-  q = fmaf(z, q, 0x1.555556p-2f);
-  const float at = fmaf(s * z, q, s);
-  const float fe = (float)e;
-  return fmaf(fe, 0x1.62e4p-1f, fmaf(fe, 0x1.7f7d1cp-20f, 2.0f * at));
-}
+float oracle_sqa_log(float u) { return om_log_unit(u); /* sb_math_oracle.h */ }
 
 /* pre_calculate.cu:206-207, :210, :218-219, :225 */
 void oracle_sqa_schedule(int steps, int M, float *beta_out, float *jperp_out) {
