@@ -26,7 +26,7 @@ namespace sbk {
 struct TcEngine;
 
 struct TcSetup {
-  int variant;  // 1 bSB, 2 dSB
+  int variant;  // 1 bSB, 2 dSB, 3 NMFA
   int dtype;    // TcDtype
   int n, R;
   int xp;       // pitch of the x / y state rows (floats)
@@ -51,6 +51,12 @@ cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st);
 cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *y, const float *h,
                    float c0, float dt, float dta0, double *energy_trace, uint32_t *status,
                    cudaStream_t st);
+// NMFA (TcSetup::variant 3, BF16 operands): `sweeps` sweeps in one persistent launch; s [R][xp] the
+// states (in and out), z1 [R][xp] the stage's second noise sample, norm [n] the row norms, betas
+// [sweeps] the inverse temperature of each sweep (both sweeps of a stage repeat it), rng [5][R][xp]
+// the XORWOW words; the operand must hold s (tc_prepare) on entry.
+cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, float *z1, const float *norm,
+                        uint32_t *rng, float noise, float keep, float mix, uint32_t *status, cudaStream_t st);
 int tc_units(const TcEngine *e);
 int tc_replica_tile(const TcEngine *e);
 // Field-only pass on operand buffer (t & 1): energy of s(t) per replica (dSB, integer J).

@@ -82,4 +82,44 @@ __device__ __forceinline__ float tanh_f(float x) {
   return copysignf(__fdiv_rn(-e, __fadd_rn(2.0f, e)), x);
 }
 
+// XORWOW (Marsaglia, "Xorshift RNGs", p. 5) on words w[0..3] and the additive counter w[4], in the
+// update order of NMFA/CUDA_GPU/src/nmfa.cu:29-40.
+__device__ __forceinline__ uint32_t xorwow(uint32_t (&w)[5]) {
+  uint32_t t = w[3];
+  t ^= t >> 2;
+  t ^= t << 1;
+  w[3] = w[2];
+  w[2] = w[1];
+  w[1] = w[0];
+  t ^= w[0];
+  t ^= w[0] << 4;
+  w[0] = t;
+  w[4] += 362437u;
+  return t + w[4];
+}
+
+// The stage's two Gaussian samples by the Box-Muller transform (NMFA/CUDA_GPU/src/nmfa.cu:103-109):
+// two words a, b, radius sqrt(-2 log(a / 2^32)) noise, angle 2 pi b / 2^32; z0 = sin(angle) radius,
+// z1 = cos(angle) radius.
+__device__ __forceinline__ void nmfa_gauss(uint32_t (&w)[5], float noise, float &z0, float &z1) {
+  const uint32_t a = xorwow(w);
+  const uint32_t b = xorwow(w);
+  const float u = __fmul_rn(__uint2float_rn(a), 0x1p-32f);
+  const float rad = __fmul_rn(__fsqrt_rn(__fmul_rn(-2.0f, sbm::log_unit(u))), noise);
+  const float ang = __fmul_rn(__uint2float_rn(b), 0x1.921fb6p-30f);
+  float sn, cs;
+  sbm::sincos_f(ang, sn, cs);
+  z0 = __fmul_rn(sn, rad);
+  z1 = __fmul_rn(cs, rad);
+}
+
+// One mean-field update (NMFA/CUDA_GPU/src/nmfa.cu:124-128): field f, row norm, noise z:
+// s' = keep s + mix tanh(beta (f norm + z)), keep = 1 - alpha, mix = alpha.
+__device__ __forceinline__ float nmfa_update(float f, float norm, float z, float beta, float keep, float mix,
+                                             float s) {
+  const float mf = __fadd_rn(__fmul_rn(f, norm), z);
+  const float th = tanh_f(__fmul_rn(mf, beta));
+  return __fadd_rn(__fmul_rn(keep, s), __fmul_rn(mix, th));
+}
+
 }  // namespace sbm

@@ -2,11 +2,14 @@
 //
 // Replaces gpu_nmfa (NMFA/CUDA_GPU/src/nmfa.cu:142-199: copy J and the betas, one launch of
 // gpu_nmfa_kernel with one CTA per sample, copy the samples back, return the kernel's event time).
-// Here the samples are the replicas of the plain fused kernel's layout (sb_plain.cu): J is padded
-// to [n][jp] once, every (sample, spin) gets its XORWOW words from one seeding launch, and each of a
-// stage's two sweeps is one fused launch (field + noise + tanh update), issued back to back so that
-// consecutive launches overlap (programmatic dependent launch); the last sweep writes the +-1
-// samples and one energy pass gives every sample's energy.
+// Here the samples are replicas. J is padded to [n][jp] once and every (sample, spin) gets its
+// XORWOW words from one seeding launch; then either
+//   * FP32 (the plain fused kernel's layout, sb_plain.cu): each of a stage's two sweeps is one fused
+//     launch (field + noise + tanh update), issued back to back so that consecutive launches overlap
+//     (programmatic dependent launch); the last sweep writes the +-1 samples; or
+//   * tensor cores (sb_tc_kernel.cuh, variant 3): all sweeps in one persistent tcgen05 launch, the
+//     states as BF16 hi + lo against exact BF16 couplings, then one launch writes the samples;
+// and one energy pass gives every sample's energy.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -69,6 +72,15 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
   const int rb = R < 8 ? R : 8;
   const size_t plane = (size_t)R * xp;
   const bool exact = prob->integer_valued && (double)prob->max_abs_j * n < 16777216.0;
+  const bool tc_ok = exact && prob->max_abs_j <= 256;
+  if (prm->field_mode == SB_FIELD_TC && !tc_ok)
+    return fail(ctx, SB_ERR_UNSUPPORTED, std::string(who) + ": the tensor-core field needs integer couplings "
+                                                            "with |J| <= 256");
+  bool use_tc = prm->field_mode == SB_FIELD_TC || (prm->field_mode == SB_FIELD_AUTO && tc_ok && R >= 32);
+  sbk::TcEngine *te = nullptr;
+  std::vector<float> sweep_betas((size_t)2 * stages);
+  for (int t = 0; t < 2 * stages; ++t) sweep_betas[t] = betas[t / 2];
+  float *dbetas = nullptr;
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSuccess;
   float *dJ = nullptr, *dnorm = nullptr, *ds = nullptr, *dz1 = nullptr;
@@ -106,10 +118,38 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
   NM_CUDA(cudaMemsetAsync(ds, 0, 2 * plane * sizeof(float), st));
   NM_CUDA(cudaMemsetAsync(den, 0, (size_t)R * sizeof(double), st));
   NM_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(uint32_t), st));
+  if (use_tc) {
+    std::string terr;
+    sbk::TcSetup ts;
+    ts.variant = 3;
+    ts.dtype = sbk::kTcBf16;
+    ts.n = n;
+    ts.R = R;
+    ts.xp = xp;
+    const sb_status tst = sbk::tc_create(&te, ts, dJ, jp, terr, st);
+    if (tst != SB_OK) {
+      if (prm->field_mode == SB_FIELD_TC) {
+        out = tst;
+        ctx->last_error = std::string(who) + ": " + terr;
+        goto cleanup_noerr;
+      }
+      use_tc = false;  // auto: the FP32 path runs every shape
+    } else {
+      NM_CUDA(cudaMallocAsync((void **)&dbetas, sweep_betas.size() * sizeof(float), st));
+      NM_CUDA(cudaMemcpyAsync(dbetas, sweep_betas.data(), sweep_betas.size() * sizeof(float), cudaMemcpyHostToDevice,
+                              st));
+    }
+  }
   NM_CUDA(cudaEventRecord(ev0, st));
   NM_CUDA(sbk::launch_nmfa_seed(drng, n, R, xp, prm->seed, st));
   ++launches;
-  {
+  if (use_tc) {
+    NM_CUDA(sbk::tc_prepare(te, ds, st));
+    NM_CUDA(sbk::tc_run_nmfa(te, 2 * stages, dbetas, ds, dz1, dnorm, drng, prm->noise,
+                             (float)(1.0 - (double)prm->recombination), prm->recombination, dstatus, st));
+    NM_CUDA(sbk::launch_nmfa_signs(ds, n, R, xp, dsamp, st));
+    launches += 3;
+  } else {
     sbk::NmfaSweep a;
     memset(&a, 0, sizeof(a));
     a.n = n;
@@ -138,7 +178,10 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
         ++launches;
         cur ^= 1;
       }
-    // an even number of sweeps: the final states are back in buffer 0
+  }
+  {
+    // an even number of sweeps: the final states are back in buffer 0 (the persistent kernel
+    // updates them in place)
     sbk::PlainEnergy pe;
     memset(&pe, 0, sizeof(pe));
     pe.n = n;
@@ -209,7 +252,9 @@ cleanup_noerr:
   cudaFreeAsync(dsamp, st);
   cudaFreeAsync(den, st);
   cudaFreeAsync(dstatus, st);
+  if (dbetas) cudaFreeAsync(dbetas, st);
   cudaStreamSynchronize(st);
+  sbk::tc_destroy(te);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
 #undef NM_CUDA
@@ -229,6 +274,7 @@ extern "C" sb_status sb_nmfa_params_default(sb_nmfa_params *p) {
   p->noise = 0.15f;        // Ising.cpp:12
   p->recombination = 0.15f;  // Ising.cpp:11
   p->seed = 1234u;         // Ising.cpp:13
+  p->field_mode = SB_FIELD_AUTO;
   return SB_OK;
 }
 

@@ -371,36 +371,6 @@ __global__ void __launch_bounds__(kThreads) plain_energy_kernel(PlainEnergy a) {
 // sweep (the reference's sweeps inside a stage have no barrier between one warp's writes and
 // another's reads; for up to 32 spins, one warp, it computes exactly this).
 
-// XORWOW (Marsaglia, "Xorshift RNGs", p. 5) on words w[0..3] and the additive counter w[4], in the
-// update order of nmfa.cu:29-40.
-__device__ __forceinline__ uint32_t xorwow(uint32_t (&w)[5]) {
-  uint32_t t = w[3];
-  t ^= t >> 2;
-  t ^= t << 1;
-  w[3] = w[2];
-  w[2] = w[1];
-  w[1] = w[0];
-  t ^= w[0];
-  t ^= w[0] << 4;
-  w[0] = t;
-  w[4] += 362437u;
-  return t + w[4];
-}
-
-// The stage's two Gaussian samples by the Box-Muller transform (nmfa.cu:103-109): two words a, b,
-// radius sqrt(-2 log(a / 2^32)) noise, angle 2 pi b / 2^32; z0 = sin(angle) radius, z1 = cos.
-__device__ __forceinline__ void nmfa_gauss(uint32_t (&w)[5], float noise, float &z0, float &z1) {
-  const uint32_t a = xorwow(w);
-  const uint32_t b = xorwow(w);
-  const float u = __fmul_rn(__uint2float_rn(a), 0x1p-32f);
-  const float rad = __fmul_rn(__fsqrt_rn(__fmul_rn(-2.0f, sbm::log_unit(u))), noise);
-  const float ang = __fmul_rn(__uint2float_rn(b), 0x1.921fb6p-30f);
-  float sn, cs;
-  sbm::sincos_f(ang, sn, cs);
-  z0 = __fmul_rn(sn, rad);
-  z1 = __fmul_rn(cs, rad);
-}
-
 template <bool WIDE>
 __global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -445,19 +415,25 @@ __global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
 #pragma unroll
       for (int q = 0; q < 5; ++q) wd[q] = a.rng[q * plane + k];
       float z1;
-      nmfa_gauss(wd, a.noise, z, z1);
+      sbm::nmfa_gauss(wd, a.noise, z, z1);
 #pragma unroll
       for (int q = 0; q < 5; ++q) a.rng[q * plane + k] = wd[q];
       a.z1[k] = z1;
     } else {
       z = a.z1[k];
     }
-    // nmfa.cu:124-128: mf = f norm + z; s' = (1 - alpha) s + alpha tanh(beta mf)
-    const float mf = __fadd_rn(__fmul_rn(fsh[w][rr], a.norm[i]), z);
-    const float th = sbm::tanh_f(__fmul_rn(mf, a.beta));
-    const float st = __fadd_rn(__fmul_rn(a.keep, a.s_in[k]), __fmul_rn(a.mix, th));
+    const float st = sbm::nmfa_update(fsh[w][rr], a.norm[i], z, a.beta, a.keep, a.mix, a.s_in[k]);
     a.s_out[k] = st;
     if (a.samples) a.samples[(size_t)r * a.n + i] = st > 0.0f ? 1 : -1;
+  }
+}
+
+// samples[r][i] = s > 0 ? +1 : -1 (nmfa.cu:139) from the final states [R][xp]
+__global__ void nmfa_signs_kernel(const float *s, int n, int R, int xp, int32_t *samples) {
+  const size_t total = (size_t)n * R;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / n, i = e % n;
+    samples[e] = s[r * xp + i] > 0.0f ? 1 : -1;
   }
 }
 
@@ -675,6 +651,11 @@ cudaError_t launch_nmfa_sweep(const NmfaSweep &a0, cudaStream_t st) {
   cfg.numAttrs = (a.overlap && !wide) ? 1 : 0;
   return wide ? cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<true>, a)
               : cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<false>, a);
+}
+
+cudaError_t launch_nmfa_signs(const float *s, int n, int R, int xp, int32_t *samples, cudaStream_t st) {
+  nmfa_signs_kernel<<<grid_for((size_t)n * R), 256, 0, st>>>(s, n, R, xp, samples);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_nmfa_seed(uint32_t *rng, int n, int R, int xp, uint32_t seed, cudaStream_t st) {

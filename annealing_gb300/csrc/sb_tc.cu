@@ -82,7 +82,7 @@ __global__ void prepare_v_kernel(const float *x, int n, int R, int xp, uint8_t *
     const size_t idx = r * Kp + i;
     if (dt == kTcFp8) {
       v0[idx] = xv > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
-    } else if (dt == kTcBf16 || variant == 2) {
+    } else if ((dt == kTcBf16 && variant != 3) || variant == 2) {
       reinterpret_cast<uint16_t *>(v0)[idx] = xv > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80;
     } else {
       const __nv_bfloat16 hi = __float2bfloat16_rn(xv);
@@ -205,6 +205,15 @@ int choose_nr(int n, int R, int sms) {
   return mt * ((R + nr - 1) / nr) <= sms ? nr : 0;
 }
 
+// NMFA: the epilogue (noise draws, tanh) weighs as much as the contraction, so the smallest replica
+// tile whose units still fit the SMs (more units, fewer elements per epilogue).
+int choose_nr_nmfa(int n, int R, int sms) {
+  const int mt = (n + kBM - 1) / kBM;
+  for (int nr : {32, 64, 128})
+    if (mt * ((R + nr - 1) / nr) <= sms) return nr;
+  return 0;
+}
+
 }  // namespace
 
 // one counter per unit (per unit and replica half for the E2M1 kernel)
@@ -227,15 +236,19 @@ int64_t tc_footprint(const TcSetup &s) {
   const int64_t Np = (s.n + kBM - 1) / kBM * kBM, Kp = (s.n + 127) / 128 * 128;
   const int64_t Rp = (s.R + 127) / 128 * 128;
   const int ap = s.dtype == kTcBf16Split ? 2 : 1;
-  const int bp = (s.dtype == kTcBf16Split && s.variant == 1) ? 2 : 1;
+  const int bp = ((s.dtype == kTcBf16Split && s.variant == 1) || s.variant == 3) ? 2 : 1;
   return Np * Kp * elem * ap + 2 * Rp * Kp * elem * bp + 4096;
 }
 
 sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, std::string &err,
                     cudaStream_t st) {
   *out = nullptr;
-  if (s.variant != 1 && s.variant != 2) {
-    err = "tensor-core path runs bSB and dSB";
+  if (s.variant != 1 && s.variant != 2 && s.variant != 3) {
+    err = "tensor-core path runs bSB, dSB and NMFA";
+    return SB_ERR_UNSUPPORTED;
+  }
+  if (s.variant == 3 && s.dtype != kTcBf16) {
+    err = "NMFA on tensor cores needs BF16 operands (integer couplings)";
     return SB_ERR_UNSUPPORTED;
   }
   if (s.variant == 1 && s.dtype != kTcBf16Split) {
@@ -243,7 +256,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     return SB_ERR_UNSUPPORTED;
   }
   const int sms = sm_count();
-  const int nr = choose_nr(s.n, s.R, sms);
+  const int nr = s.variant == 3 ? choose_nr_nmfa(s.n, s.R, sms) : choose_nr(s.n, s.R, sms);
   if (nr == 0) {
     err = "problem too large for the single-pass tensor-core kernel (units > SMs)";
     return SB_ERR_UNSUPPORTED;
@@ -269,7 +282,7 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
   e->n_rtiles = e->Rp / nr;
   e->units = e->n_mtiles * e->n_rtiles;
   const int ap = s.dtype == kTcBf16Split ? 2 : 1;
-  const int bp = (s.dtype == kTcBf16Split && s.variant == 1) ? 2 : 1;
+  const int bp = ((s.dtype == kTcBf16Split && s.variant == 1) || s.variant == 3) ? 2 : 1;
   auto fail = [&](const char *what, cudaError_t ce) {
     err = std::string(what) + (ce != cudaSuccess ? std::string(": ") + cudaGetErrorString(ce) : "");
     tc_destroy(e);
@@ -389,6 +402,29 @@ cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *
   cudaError_t ce = cudaMemsetAsync(e->flags, 0, flag_bytes(e), st);
   if (ce != cudaSuccess) return ce;
   return launch(e, energy_trace ? kEmodeStepTrace : kEmodeStep, a, st);
+}
+
+cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, float *z1, const float *norm,
+                        uint32_t *rng, float noise, float keep, float mix, uint32_t *status, cudaStream_t st) {
+  if (sweeps <= 0) return cudaSuccess;
+  if (e->s.variant != 3) return cudaErrorInvalidValue;
+  TcArgs a = e->args;
+  a.x = s;
+  a.y = z1;
+  a.h = norm;
+  a.energy = nullptr;
+  a.status = status;
+  a.steps = sweeps;
+  a.t0 = 0;
+  a.buf0 = 0;
+  a.pumps = betas;
+  a.rng = rng;
+  a.noise = noise;
+  a.keep = keep;
+  a.mix = mix;
+  cudaError_t ce = cudaMemsetAsync(e->flags, 0, flag_bytes(e), st);
+  if (ce != cudaSuccess) return ce;
+  return launch(e, kEmodeStep, a, st);
 }
 
 void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes) {

@@ -22,6 +22,10 @@
 //   * steps are ordered by per-unit release/acquire flags instead of a grid barrier: a unit
 //     publishes its V(t+1) chunk and the units of its replica column wait only for the chunks they
 //     load (bounded spins).
+// VARIANT 3 is NMFA (noisy mean-field annealing, NMFA/CUDA_GPU/src/nmfa.cu:99-136) on the same
+// pipeline: x holds the mean-field state s, y the stage's second Gaussian sample, h the row norms,
+// pumps[t] the inverse temperature of sweep t; the operand is s as BF16 hi + lo against exact BF16
+// couplings, and the epilogue draws the stage's noise pair on even sweeps (XORWOW words in rng).
 // Operand dtypes: FP8 E4M3 holds +-1 and integers |J| <= 16 exactly; BF16 holds integers up to 256;
 // BF16 hi + lo (J = Jh + Jl, x = xh + xl) gives ~16 bits for real values, with the three products
 // Jh*xh + Jh*xl + Jl*xh accumulated in FP32. Integer fields are exact whenever every partial sum
@@ -36,6 +40,7 @@
 #include <stdint.h>
 
 #include "sb_internal.h"
+#include "sb_math.cuh"
 #include "sb_ptx.cuh"
 
 namespace sbk {
@@ -62,8 +67,10 @@ struct alignas(64) TcArgs {
   int n, R, xp, Kp, Rp, n_mtiles, n_rtiles, k_chunks;
   int steps, t0;           // steps to run; schedule offset
   int buf0;                // V buffer holding V(t0)
-  const float *pumps;      // pumps[t] = a0 - a(t), computed on the host
+  const float *pumps;      // pumps[t] = a0 - a(t), computed on the host (NMFA: beta of sweep t)
   float c0, dt, dta0;
+  uint32_t *rng;           // NMFA: [5][R][xp] XORWOW words of each (sample, spin)
+  float noise, keep, mix;  // NMFA: sigma, 1 - alpha, alpha
 };
 
 template <int DT>
@@ -85,8 +92,9 @@ template <int DT, int VARIANT>
 struct Cfg {
   static constexpr int kElem = DtTraits<DT>::kElem;
   static constexpr int kAParts = DtTraits<DT>::kParts;
-  // V = sign(x) needs one part even when J is split; bSB's x is split with J.
-  static constexpr int kBParts = (DT == kTcBf16Split && VARIANT == 1) ? 2 : 1;
+  // V = sign(x) needs one part even when J is split; bSB's x is split with J; NMFA's state is split
+  // against exact (integer) BF16 couplings.
+  static constexpr int kBParts = ((DT == kTcBf16Split && VARIANT == 1) || VARIANT == 3) ? 2 : 1;
   static constexpr int kKPerMma = 32 / kElem;  // 32 bytes of K per instruction
   static constexpr int kMmaPerChunk = kChunkBytes / 32;
 };
@@ -411,7 +419,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             e2[j] = in ? __fsub_rn(-__fmul_rn(sg, f), __fmul_rn(2.0f * hv, sg)) : 0.0f;
           }
           if (!kEOnly && in) {
-            sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
+            if constexpr (VARIANT == 3) {
+              // even sweeps open a stage: draw its pair, keep the second sample in y
+              float z = y;
+              if (((t & 1) == 0)) {
+                const size_t plane = (size_t)p.R * p.xp, k = (size_t)r * p.xp + row;
+                uint32_t wd[5];
+#pragma unroll
+                for (int q = 0; q < 5; ++q) wd[q] = p.rng[q * plane + k];
+                sbm::nmfa_gauss(wd, p.noise, z, y);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) p.rng[q * plane + k] = wd[q];
+              }
+              x = sbm::nmfa_update(f, hv, z, pump, p.keep, p.mix, x);
+            } else {
+              sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
+            }
             if constexpr (!kStageV) store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
           }
           if constexpr (kStageV && !kEOnly) {

@@ -189,6 +189,7 @@ class NmfaParams(C.Structure):
         ("noise", C.c_float),
         ("recombination", C.c_float),
         ("seed", C.c_uint32),
+        ("field_mode", C.c_int32),
     ]
 
     @classmethod

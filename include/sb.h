@@ -391,6 +391,11 @@ typedef struct sb_nmfa_params {
   float noise;              /* Gaussian noise scale sigma (Ising.cpp:12, SIGMA = 0.15) */
   float recombination;      /* alpha (Ising.cpp:11, ALPHA = 0.15) */
   uint32_t seed;            /* Ising.cpp:13, SEED = 1234 */
+  int32_t field_mode;       /* sb_field_mode. SB_FIELD_FP32: the fused FP32 kernel, one launch per sweep
+                               (bit-exact with the oracle). SB_FIELD_TC: one persistent tcgen05 launch,
+                               the state as BF16 hi + lo against exact BF16 couplings (integer |J| <= 256),
+                               FP32 accumulation; within a stated tolerance of the FP32 path.
+                               SB_FIELD_AUTO: TC for 32 samples or more when it applies, else FP32. */
 } sb_nmfa_params;
 
 typedef struct sb_nmfa_result {
@@ -408,7 +413,7 @@ typedef struct sb_nmfa_result {
 } sb_nmfa_result;
 
 /* samples 1, stages 100 with the reference schedule, noise 0.15, recombination 0.15, seed 1234
- * (NMFA/CUDA_GPU/Ising.cpp:8-13) */
+ * (NMFA/CUDA_GPU/Ising.cpp:8-13), field_mode SB_FIELD_AUTO */
 sb_status sb_nmfa_params_default(sb_nmfa_params *p);
 /* betas[k] = 1/16 + k (8 - 1/16) / stages, accumulated in FP32 as Ising.cpp:37-43 does */
 sb_status sb_nmfa_schedule(int32_t stages, float *betas);

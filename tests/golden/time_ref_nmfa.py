@@ -5,8 +5,10 @@ CTA of N threads per sample with its row of J in registers (:54-140, launched by
 script loads oracle/_ref/nmfa_states_n1024.cubin (that kernel, template expanded for N = 1024 by
 oracle/build_ref.py) and times that launch with CUDA events for several sample counts on a seeded
 N = 1024 graph with the distribution of NMFA/CUDA_GPU/tests/fully.py and the 100-stage schedule of
-Ising.cpp; then the same instance, schedule and sample counts through sb_nmfa_solve (device time:
-seeding, 200 fused sweep launches, the energy pass). Rates count N x samples x 200 spin updates.
+Ising.cpp; then the same instance, schedule and sample counts through sb_nmfa_solve (device time)
+with the FP32 field (seeding, 200 fused sweep launches, the energy pass) and the tensor-core field
+(seeding, one persistent launch for all sweeps, the samples and the energy pass; 32 samples and
+more). Rates count N x samples x 200 spin updates.
 
 Usage (on a machine with a GB300):  python tests/golden/time_ref_nmfa.py
 Prints one JSON line.
@@ -41,12 +43,18 @@ def main():
         out["reference_kernel"][str(R)] = {"ms": ms, "spin_updates_per_s": N * R * 2 * STAGES / (ms * 1e-3)}
     ctx = sb.Context(0)
     prob = sb.Problem.from_dense(J)
-    for R in COUNTS:
-        p = sb.NmfaParams.default(samples=R)
-        ctx.nmfa_solve(prob, p, betas=betas)
-        ms = min(ctx.nmfa_solve(prob, p, betas=betas).device_ms for _ in range(3))
-        out["ours"][str(R)] = {"ms": ms, "spin_updates_per_s": N * R * 2 * STAGES / (ms * 1e-3)}
+    for field, mode in (("fp32", sb.FIELD_FP32), ("tc", sb.FIELD_TC)):
+        out["ours_" + field] = {}
+        for R in COUNTS:
+            if mode == sb.FIELD_TC and R < 32:
+                continue
+            p = sb.NmfaParams.default(samples=R, field_mode=mode)
+            ctx.nmfa_solve(prob, p, betas=betas)
+            ms = min(ctx.nmfa_solve(prob, p, betas=betas).device_ms for _ in range(3))
+            out["ours_" + field][str(R)] = {"ms": ms, "spin_updates_per_s": N * R * 2 * STAGES / (ms * 1e-3)}
     ctx.close()
+    # the library's default (SB_FIELD_AUTO): the tensor-core field from 32 samples on
+    out["ours"] = {k: out["ours_tc"].get(k, v) for k, v in out["ours_fp32"].items()}
     out["speedup"] = {k: out["reference_kernel"][k]["ms"] / out["ours"][k]["ms"] for k in out["ours"]}
     print(json.dumps(out))
 

@@ -48,7 +48,7 @@ def _energies(J, samples):
 def test_bit_exact_vs_oracle(ctx, n, R, stages, kind):
     J = instances.nmfa_fully(n, seed=n + 7) if kind == "fully" else instances.complete_pm1(n, seed=n + 7)
     betas = sb.nmfa_schedule(100)[:stages]
-    p = sb.NmfaParams.default(samples=R, seed=99 + n)
+    p = sb.NmfaParams.default(samples=R, seed=99 + n, field_mode=sb.FIELD_FP32)
     res = ctx.nmfa_solve(sb.Problem.from_dense(J), p, betas=betas, want_states=True)
     st, sp, _ = orc.nmfa_run(J, R, betas, 0.15, 0.15, 99 + n)
     assert np.array_equal(res.states.view(np.uint32), st.view(np.uint32)), \
@@ -64,8 +64,8 @@ def test_real_couplings_bit_exact(ctx):
     """Real-valued J (FP32 fields, FP64 energy pass): states and samples bit-exact."""
     J, _ = instances.gaussian(70, seed=5)
     betas = sb.nmfa_schedule(100)[:8]
-    res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=4, seed=3), betas=betas,
-                         want_states=True)
+    res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=4, seed=3, field_mode=sb.FIELD_FP32),
+                         betas=betas, want_states=True)
     st, sp, _ = orc.nmfa_run(J, 4, betas, 0.15, 0.15, 3)
     assert np.array_equal(res.states.view(np.uint32), st.view(np.uint32))
     assert np.array_equal(res.samples.astype(np.int32), sp)
@@ -80,7 +80,7 @@ def test_parameters(ctx):
     J = instances.nmfa_fully(64, seed=11)
     betas = sb.nmfa_schedule(30)
     for noise, rc, seed in ((0.0, 0.15, 1), (0.5, 0.3, 2), (0.15, 1.0, 4294967295)):
-        p = sb.NmfaParams.default(samples=3, noise=noise, recombination=rc, seed=seed)
+        p = sb.NmfaParams.default(samples=3, noise=noise, recombination=rc, seed=seed, field_mode=sb.FIELD_FP32)
         res = ctx.nmfa_solve(sb.Problem.from_dense(J), p, betas=betas, want_states=True)
         st, _, _ = orc.nmfa_run(J, 3, betas, noise, rc, seed)
         assert np.array_equal(res.states.view(np.uint32), st.view(np.uint32)), (noise, rc, seed)
@@ -107,18 +107,22 @@ def test_rejects(ctx):
         ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(recombination=1.5))
 
 
-def test_reference_states_one_warp(ctx):
+@pytest.mark.parametrize("field", ["fp32", "tc"])
+def test_reference_states_one_warp(ctx, field):
     """N = 32: the reference kernel's states after the first K stages of the 100-stage anneal (256
     samples, its own seeds). Its noise and tanh are CUDA fast-math intrinsics, ours are the library's
     FP32 functions, and its field is summed in another order, so states agree to a tolerance: within
     2e-3 for every spin after one and two stages and for 99 % of the spins throughout; the final
-    samples (after 100 stages) agree in 99 % of the spins."""
+    samples (after 100 stages) agree in 99 % of the spins. The same bounds hold for the tensor-core
+    field (states as BF16 hi + lo)."""
     g = np.load(os.path.join(GOLDEN, "ref_nmfa_n32.npz"))
     J = g["J"].astype(np.float32)
     full = sb.nmfa_schedule(100)
+    mode = sb.FIELD_FP32 if field == "fp32" else sb.FIELD_TC
     for K in g["ks"]:
         ref = g[f"states_k{K}"]
-        res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=int(g["samples"])),
+        res = ctx.nmfa_solve(sb.Problem.from_dense(J),
+                             sb.NmfaParams.default(samples=int(g["samples"]), field_mode=mode),
                              betas=full[:K], want_states=True)
         d = np.abs(res.states - ref)
         print(f"K={K}: max |ds| {d.max():.3e}, 99th pct {np.quantile(d, 0.99):.3e}, "
@@ -130,8 +134,8 @@ def test_reference_states_one_warp(ctx):
             assert np.mean((res.states > 0) == (ref > 0)) >= 0.99
 
 
-@pytest.mark.parametrize("n", [128, 1024])
-def test_reference_energy_distribution(ctx, n):
+@pytest.mark.parametrize("n,field", [(128, "fp32"), (1024, "fp32"), (128, "tc"), (1024, "tc")])
+def test_reference_energy_distribution(ctx, n, field):
     """1000 samples of ours against 1000 of the reference kernel on the same seeded instance: the
     energy distributions pass a two-sample KS test (p >= 0.01) and the means agree within 3
     standard errors. Beyond one warp the reference's sweeps race, so only the distribution is
@@ -140,14 +144,45 @@ def test_reference_energy_distribution(ctx, n):
 
     g = np.load(os.path.join(GOLDEN, f"ref_nmfa_n{n}.npz"))
     J = instances.nmfa_fully(n, int(g["seed"]))
-    res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=1000, seed=20240))
+    mode = sb.FIELD_FP32 if field == "fp32" else sb.FIELD_TC
+    res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=1000, seed=20240, field_mode=mode))
     ours, ref = res.energies, g["energies"].astype(np.float64)
     ks = stats.ks_2samp(ours, ref)
     se = np.sqrt(ours.var() / len(ours) + ref.var() / len(ref))
-    print(f"n={n}: ours mean {ours.mean():.2f} sd {ours.std():.2f}, reference mean {ref.mean():.2f} "
+    print(f"n={n} {field}: ours mean {ours.mean():.2f} sd {ours.std():.2f}, reference mean {ref.mean():.2f} "
           f"sd {ref.std():.2f}, KS p {ks.pvalue:.3f}")
     assert ks.pvalue >= 0.01
     assert abs(ours.mean() - ref.mean()) <= 3 * se
+
+
+@pytest.mark.parametrize("n,R,stages", [
+    (32, 32, 20),      # one replica tile of 32 samples
+    (130, 40, 10),     # ragged spin tile, two replica tiles
+    (300, 200, 10),    # several spin and replica tiles
+    (1024, 256, 20),   # the bench's N
+])
+def test_tensor_core_vs_oracle(ctx, n, R, stages):
+    """The tcgen05 field (states as BF16 hi + lo, about 16 bits, FP32 accumulation) against the
+    oracle's FP32 field: states after `stages` stages within 2e-3 at the 99th percentile, and the
+    samples' signs equal for 99 % of the spins."""
+    J = instances.nmfa_fully(n, seed=n + 3)
+    betas = sb.nmfa_schedule(100)[:stages]
+    res = ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=R, seed=5, field_mode=sb.FIELD_TC),
+                         betas=betas, want_states=True)
+    st, sp, _ = orc.nmfa_run(J, R, betas, 0.15, 0.15, 5)
+    d = np.abs(res.states - st)
+    agree = np.mean(res.samples.astype(np.int32) == sp)
+    print(f"tc n={n} R={R} K={stages}: max |ds| {d.max():.3e}, 99th pct {np.quantile(d, 0.99):.3e}, "
+          f"median {np.median(d):.3e}, sign agreement {agree:.4f}")
+    assert np.quantile(d, 0.99) <= 2e-3
+    assert agree >= 0.99
+    assert res.energy_check_ok and res.kernel_launches == 5
+
+
+def test_tensor_core_needs_integer_couplings(ctx):
+    J, _ = instances.gaussian(64, seed=1)
+    with pytest.raises(sb.SBError):
+        ctx.nmfa_solve(sb.Problem.from_dense(J), sb.NmfaParams.default(samples=64, field_mode=sb.FIELD_TC))
 
 
 def test_cli_nmfa(tmp_path):
