@@ -57,6 +57,9 @@ cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *
 // the XORWOW words; the operand must hold s (tc_prepare) on entry.
 cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, float *z1, const float *norm,
                         uint32_t *rng, float noise, float keep, float mix, uint32_t *status, cudaStream_t st);
+// NMFA engine: energy[r] += -1/2 sign(s_r) J sign(s_r) for every sample (the dSB energy contraction on
+// the engine's BF16 couplings; exact for integer J); overwrites operand buffer 0.
+cudaError_t tc_nmfa_energy(TcEngine *e, const float *s, double *energy, uint32_t *status, cudaStream_t st);
 int tc_units(const TcEngine *e);
 int tc_replica_tile(const TcEngine *e);
 // Field-only pass on operand buffer (t & 1): energy of s(t) per replica (dSB, integer J).

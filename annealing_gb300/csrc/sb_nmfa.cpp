@@ -6,10 +6,11 @@
 // XORWOW words from one seeding launch; then either
 //   * FP32 (the plain fused kernel's layout, sb_plain.cu): each of a stage's two sweeps is one fused
 //     launch (field + noise + tanh update), issued back to back so that consecutive launches overlap
-//     (programmatic dependent launch); the last sweep writes the +-1 samples; or
+//     (programmatic dependent launch); the last sweep writes the +-1 samples and one energy pass
+//     gives every sample's energy; or
 //   * tensor cores (sb_tc_kernel.cuh, variant 3): all sweeps in one persistent tcgen05 launch, the
-//     states as BF16 hi + lo against exact BF16 couplings, then one launch writes the samples;
-// and one energy pass gives every sample's energy.
+//     states as BF16 hi + lo against exact BF16 couplings, then one launch writes the samples and
+//     the dSB energy contraction on the same couplings gives the energies.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -148,7 +149,8 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     NM_CUDA(sbk::tc_run_nmfa(te, 2 * stages, dbetas, ds, dz1, dnorm, drng, prm->noise,
                              (float)(1.0 - (double)prm->recombination), prm->recombination, dstatus, st));
     NM_CUDA(sbk::launch_nmfa_signs(ds, n, R, xp, dsamp, st));
-    launches += 3;
+    NM_CUDA(sbk::tc_nmfa_energy(te, ds, den, dstatus, st));
+    launches += 5;
   } else {
     sbk::NmfaSweep a;
     memset(&a, 0, sizeof(a));
@@ -178,10 +180,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
         ++launches;
         cur ^= 1;
       }
-  }
-  {
-    // an even number of sweeps: the final states are back in buffer 0 (the persistent kernel
-    // updates them in place)
+    // an even number of sweeps: the final states are back in buffer 0
     sbk::PlainEnergy pe;
     memset(&pe, 0, sizeof(pe));
     pe.n = n;
@@ -236,6 +235,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     res->best_sample = best;
     res->device_ms = dev_ms;
     res->kernel_launches = launches;
+    res->field_used = use_tc ? SB_FIELD_TC : SB_FIELD_FP32;
     const double updates = (double)n * R * 2.0 * stages;
     res->spin_updates_per_s = dev_ms > 0 ? updates / ((double)dev_ms * 1e-3) : 0.0;
   }

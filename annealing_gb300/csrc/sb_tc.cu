@@ -427,6 +427,43 @@ cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, f
   return launch(e, kEmodeStep, a, st);
 }
 
+cudaError_t tc_nmfa_energy(TcEngine *e, const float *s, double *energy, uint32_t *status, cudaStream_t st) {
+  if (e->s.variant != 3) return cudaErrorInvalidValue;
+  // the dSB energy contraction on the same BF16 couplings: operand buffer 0 part 0 takes sign(s)
+  // (its padding is still zero), the kernel adds -1/2 s_i (J s)_i per sample into energy
+  const void *k = nullptr;
+  size_t smem = 0;
+  if (!tc_kernel_bf16(2, e->nr, kEmodeEnergy, &k, &smem)) return cudaErrorInvalidValue;
+  cudaError_t ce = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ce != cudaSuccess) return ce;
+  prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(s, e->s.n, e->s.R, e->s.xp, e->v[0][0], nullptr,
+                                                                      e->Kp, kTcBf16, 2);
+  if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+  TcArgs a = e->args;
+  a.x = const_cast<float *>(s);
+  a.y = nullptr;
+  a.h = nullptr;
+  a.energy = energy;
+  a.status = status;
+  a.steps = 1;
+  a.t0 = 0;
+  a.buf0 = 0;
+  a.pumps = nullptr;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)e->units);
+  cfg.blockDim = dim3((unsigned)e->threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  void *params[1] = {&a};
+  return cudaLaunchKernelExC(&cfg, k, params);
+}
+
 void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes) {
   const int r = choose_nr(n, R, sm_count());
   const size_t Np = (size_t)(n + kBM - 1) / kBM * kBM, Kp = (size_t)(n + 127) / 128 * 128;

@@ -788,11 +788,15 @@ def run_nmfa(args, rank, world, local_rank):
         ctx.close()
         return
     flops = 2.0 * n * n * R * 2 * stages / (total_dev / args.steps * 1e-3)
+    tc = results[-1].field_used == sb.FIELD_TC
+    _, bf16_peak, peak_kind = peaks()
     line = {
         "metric": "NMFA spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (field, mean-field states)", "data": "synthetic (seeded graph)",
+        "dtype": ("bf16 hi+lo states x bf16 couplings on tensor cores (f32 accumulate), f32 states" if tc
+                  else "f32 (field, mean-field states)"),
+        "data": "synthetic (seeded graph)",
         "config": {"workload": desc, "n": n, "samples": R, "stages": stages, "sweeps_per_stage": 2,
                    "parallelism": f"samples-only x{world}",
                    "l2": "flushed between timed solves (256 MB write outside the timed region)"},
@@ -800,12 +804,21 @@ def run_nmfa(args, rank, world, local_rank):
                 "d2h_bytes_per_step": int(R * n * 4), "entry_point": "sb_gpu_nmfa (the reference's gpu_nmfa)"},
         "gpu_launches": int(sum(r.kernel_launches for r in results)),
         "throughput": {"field_flops_per_s": flops,
-                       "note": "FP32 CUDA-core field, 2 N^2 FLOPs per sample and sweep; one fused launch per sweep"},
+                       "note": ("tensor-core field, 2 N^2 FLOPs per sample and sweep (the hi+lo operand runs "
+                                "twice that on the tensor pipe); all sweeps in one persistent launch" if tc else
+                                "FP32 CUDA-core field, 2 N^2 FLOPs per sample and sweep; one fused launch per sweep")},
         "clocks": clk.summary(),
         "quality": {"best_energy": min(r.best_energy for r in results),
                     "mean_energy": float(np.mean([r.energies.mean() for r in results])),
                     "energy_check_ok": all(r.energy_check_ok for r in results)},
     }
+    if tc:
+        pipe = 2 * flops / 1e12  # two products (hi, lo) per coupling and sample on the tensor pipe
+        line["roofline"] = {"bound": "tensor", "achieved": pipe, "peak": bf16_peak, "unit": "TFLOP/s",
+                            "frac": pipe / bf16_peak, "traffic": None,
+                            "kernel": "tc_sb_kernel<BF16, NMFA> (persistent, all 200 sweeps)",
+                            "timing": "solve device time (seeding, operand, persistent launch, samples, energies)",
+                            "peak_source": f"{peak_kind} dense BF16 burst"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = nmfa_cpu_sample(J)
     print(json.dumps(line), flush=True)
@@ -835,7 +848,7 @@ def main():
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"batched-dsb": 40, "plain-dsb": 40, "batched-bsb": 10, "uneven-batch": 5, "serving": 1,
-                      "sqa": 5, "nmfa": 5}[args.workload] if args.impl == "ours" else 5
+                      "sqa": 5, "nmfa": 50}[args.workload] if args.impl == "ours" else 5
     if args.sb_steps > 0 and args.workload != "serving":
         v, n, R, _, field, desc = WORKLOADS[args.workload]
         WORKLOADS[args.workload] = (v, n, R, args.sb_steps, field,
