@@ -638,6 +638,7 @@ sb_status sb_destroy(sb_ctx *ctx) {
     plan_free_device(ctx->cached);
     delete ctx->cached;
   }
+  sbh::nmfa_cache_free(ctx->nmfa);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SB_OK;

@@ -11,6 +11,7 @@
 namespace sbs {
 struct Server;
 }
+struct NmfaCache;  // sb_nmfa.cpp
 
 struct sb_ctx {
   int device = 0;
@@ -22,4 +23,5 @@ struct sb_ctx {
   int max_inflight = 64;
   sb_plan *cached = nullptr;  // most recent sb_solve plan, reused when the shape matches
   sbs::Server *server = nullptr;
+  NmfaCache *nmfa = nullptr;  // device buffers of the last NMFA shape
 };

@@ -20,6 +20,12 @@ double coupling_std(const sb_problem *p, int threads);
 float default_c0(const sb_problem *p, int threads);
 }  // namespace sbh
 
+struct NmfaCache;
+namespace sbh {
+// Frees an NMFA buffer cache (sb_nmfa.cpp); null is a no-op.
+void nmfa_cache_free(NmfaCache *c);
+}  // namespace sbh
+
 namespace sbk {
 
 // Tensor-core field engine for one dense instance with R replicas (sb_tc.cu).

@@ -33,18 +33,41 @@ sb_status fail(sb_ctx *ctx, sb_status s, const std::string &msg) {
   return s;
 }
 
-// norm_i = -1 / sqrt(sum_j |J_ij|) (nmfa.cu:88-93), the sum in double over j in index order (exact
-// for integer couplings); 0 for a row without couplings, whose field is then 0.
-void row_norms(const sb_problem *p, std::vector<float> &norm) {
-  const int n = p->n;
-  norm.assign((size_t)n, 0.0f);
-  for (int i = 0; i < n; ++i) {
-    double a = 0.0;
-    const float *row = p->J + (size_t)i * n;
-    for (int j = 0; j < n; ++j) a += fabs((double)row[j]);
-    norm[i] = a > 0.0 ? (float)(-1.0 / sqrt(a)) : 0.0f;
-  }
+}  // namespace
+
+// Device buffers of the last NMFA shape a context ran (sb_nmfa_solve / sb_gpu_nmfa keep them between
+// calls, as sb_solve keeps its plan): a call with the same n and sample count uploads J and runs.
+struct NmfaCache {
+  int n = 0, R = 0, jp = 0, xp = 0;
+  sbk::TcEngine *te = nullptr;  // built on the first tensor-core call for this shape
+  float *dJ = nullptr, *dnorm = nullptr, *ds = nullptr, *dz1 = nullptr, *dbetas = nullptr;
+  size_t betas_cap = 0;
+  uint32_t *drng = nullptr, *dstatus = nullptr;
+  int32_t *dsamp = nullptr;
+  double *den = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace sbh {
+void nmfa_cache_free(NmfaCache *c) {
+  if (!c) return;
+  sbk::tc_destroy(c->te);
+  cudaFree(c->dJ);
+  cudaFree(c->dnorm);
+  cudaFree(c->ds);
+  cudaFree(c->dz1);
+  cudaFree(c->dbetas);
+  cudaFree(c->drng);
+  cudaFree(c->dstatus);
+  cudaFree(c->dsamp);
+  cudaFree(c->den);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  delete c;
 }
+}  // namespace sbh
+
+namespace {
 
 // Everything sb_nmfa_solve and sb_gpu_nmfa share; samples32 (when set) receives int32 +-1.
 sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *prm, sb_nmfa_result *res,
@@ -66,90 +89,107 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     memcpy(betas.data(), prm->betas, (size_t)stages * sizeof(float));
   else
     sb_nmfa_schedule(stages, betas.data());
-  std::vector<float> norm;
-  row_norms(prob, norm);
-  cudaSetDevice(ctx->device);
-  const int jp = (n + 3) & ~3, xp = jp;
-  const int rb = R < 8 ? R : 8;
-  const size_t plane = (size_t)R * xp;
   const bool exact = prob->integer_valued && (double)prob->max_abs_j * n < 16777216.0;
   const bool tc_ok = exact && prob->max_abs_j <= 256;
   if (prm->field_mode == SB_FIELD_TC && !tc_ok)
     return fail(ctx, SB_ERR_UNSUPPORTED, std::string(who) + ": the tensor-core field needs integer couplings "
                                                             "with |J| <= 256");
   bool use_tc = prm->field_mode == SB_FIELD_TC || (prm->field_mode == SB_FIELD_AUTO && tc_ok && R >= 32);
-  sbk::TcEngine *te = nullptr;
   std::vector<float> sweep_betas((size_t)2 * stages);
   for (int t = 0; t < 2 * stages; ++t) sweep_betas[t] = betas[t / 2];
-  float *dbetas = nullptr;
+  cudaSetDevice(ctx->device);
+  const int jp = (n + 3) & ~3, xp = jp;
+  const int rb = R < 8 ? R : 8;
+  const size_t plane = (size_t)R * xp;
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSuccess;
-  float *dJ = nullptr, *dnorm = nullptr, *ds = nullptr, *dz1 = nullptr;
-  uint32_t *drng = nullptr, *dstatus = nullptr;
-  int32_t *dsamp = nullptr;
-  double *den = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   uint32_t hstatus = 0;
   float dev_ms = 0.0f;
-  std::vector<int32_t> hsamp((size_t)R * n);
+  // the samples go straight into the caller's int32 buffer when there is one
+  std::vector<int32_t> hsamp(samples32 ? 0 : (size_t)R * n);
+  int32_t *samp = samples32 ? samples32 : hsamp.data();
   std::vector<double> hen((size_t)R);
   std::string where;
   sb_status out = SB_OK;
   int64_t launches = 0;
+  NmfaCache *c = ctx->nmfa;
 #define NM_CUDA(call)                \
   if ((e = (call)) != cudaSuccess) { \
     where = #call;                   \
     goto cleanup;                    \
   }
   sbk::init_kernel_attributes();
-  NM_CUDA(cudaEventCreate(&ev0));
-  NM_CUDA(cudaEventCreate(&ev1));
-  NM_CUDA(cudaMallocAsync((void **)&dJ, (size_t)n * jp * sizeof(float), st));
-  NM_CUDA(cudaMallocAsync((void **)&dnorm, (size_t)n * sizeof(float), st));
-  NM_CUDA(cudaMallocAsync((void **)&ds, 2 * plane * sizeof(float), st));
-  NM_CUDA(cudaMallocAsync((void **)&dz1, plane * sizeof(float), st));
-  NM_CUDA(cudaMallocAsync((void **)&drng, 5 * plane * sizeof(uint32_t), st));
-  NM_CUDA(cudaMallocAsync((void **)&dsamp, (size_t)R * n * sizeof(int32_t), st));
-  NM_CUDA(cudaMallocAsync((void **)&den, (size_t)R * sizeof(double), st));
-  NM_CUDA(cudaMallocAsync((void **)&dstatus, sizeof(uint32_t), st));
-  if (jp != n) NM_CUDA(cudaMemsetAsync(dJ, 0, (size_t)n * jp * sizeof(float), st));
-  NM_CUDA(cudaMemcpy2DAsync(dJ, (size_t)jp * sizeof(float), prob->J, (size_t)n * sizeof(float),
+  if (c && (c->n != n || c->R != R)) {
+    sbh::nmfa_cache_free(c);
+    c = ctx->nmfa = nullptr;
+  }
+  if (!c) {
+    c = ctx->nmfa = new NmfaCache();
+    c->n = n;
+    c->R = R;
+    c->jp = jp;
+    c->xp = xp;
+    NM_CUDA(cudaEventCreate(&c->ev0));
+    NM_CUDA(cudaEventCreate(&c->ev1));
+    NM_CUDA(cudaMalloc((void **)&c->dJ, (size_t)n * jp * sizeof(float)));
+    NM_CUDA(cudaMalloc((void **)&c->dnorm, (size_t)n * sizeof(float)));
+    NM_CUDA(cudaMalloc((void **)&c->ds, 2 * plane * sizeof(float)));
+    NM_CUDA(cudaMalloc((void **)&c->dz1, plane * sizeof(float)));
+    NM_CUDA(cudaMalloc((void **)&c->drng, 5 * plane * sizeof(uint32_t)));
+    NM_CUDA(cudaMalloc((void **)&c->dsamp, (size_t)R * n * sizeof(int32_t)));
+    NM_CUDA(cudaMalloc((void **)&c->den, (size_t)R * sizeof(double)));
+    NM_CUDA(cudaMalloc((void **)&c->dstatus, sizeof(uint32_t)));
+    // the padding columns of J (and of the states) are never written afterwards
+    if (jp != n) NM_CUDA(cudaMemsetAsync(c->dJ, 0, (size_t)n * jp * sizeof(float), st));
+  }
+  if (c->betas_cap < sweep_betas.size()) {
+    cudaFree(c->dbetas);
+    c->dbetas = nullptr;
+    c->betas_cap = 0;
+    NM_CUDA(cudaMalloc((void **)&c->dbetas, sweep_betas.size() * sizeof(float)));
+    c->betas_cap = sweep_betas.size();
+  }
+  NM_CUDA(cudaMemcpy2DAsync(c->dJ, (size_t)jp * sizeof(float), prob->J, (size_t)n * sizeof(float),
                             (size_t)n * sizeof(float), (size_t)n, cudaMemcpyHostToDevice, st));
-  NM_CUDA(cudaMemcpyAsync(dnorm, norm.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
-  NM_CUDA(cudaMemsetAsync(ds, 0, 2 * plane * sizeof(float), st));
-  NM_CUDA(cudaMemsetAsync(den, 0, (size_t)R * sizeof(double), st));
-  NM_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(uint32_t), st));
+  // norm_i = -1 / sqrt(sum_j |J_ij|) (nmfa.cu:88-93), on the device from the uploaded couplings
+  NM_CUDA(sbk::launch_nmfa_norms(c->dJ, n, jp, c->dnorm, st));
+  NM_CUDA(cudaMemcpyAsync(c->dbetas, sweep_betas.data(), sweep_betas.size() * sizeof(float), cudaMemcpyHostToDevice,
+                          st));
+  NM_CUDA(cudaMemsetAsync(c->ds, 0, 2 * plane * sizeof(float), st));
+  NM_CUDA(cudaMemsetAsync(c->den, 0, (size_t)R * sizeof(double), st));
+  NM_CUDA(cudaMemsetAsync(c->dstatus, 0, sizeof(uint32_t), st));
   if (use_tc) {
-    std::string terr;
-    sbk::TcSetup ts;
-    ts.variant = 3;
-    ts.dtype = sbk::kTcBf16;
-    ts.n = n;
-    ts.R = R;
-    ts.xp = xp;
-    const sb_status tst = sbk::tc_create(&te, ts, dJ, jp, terr, st);
-    if (tst != SB_OK) {
-      if (prm->field_mode == SB_FIELD_TC) {
-        out = tst;
-        ctx->last_error = std::string(who) + ": " + terr;
-        goto cleanup_noerr;
-      }
-      use_tc = false;  // auto: the FP32 path runs every shape
+    if (c->te) {
+      NM_CUDA(sbk::tc_reload(c->te, c->dJ, jp, st));
     } else {
-      NM_CUDA(cudaMallocAsync((void **)&dbetas, sweep_betas.size() * sizeof(float), st));
-      NM_CUDA(cudaMemcpyAsync(dbetas, sweep_betas.data(), sweep_betas.size() * sizeof(float), cudaMemcpyHostToDevice,
-                              st));
+      std::string terr;
+      sbk::TcSetup ts;
+      ts.variant = 3;
+      ts.dtype = sbk::kTcBf16;
+      ts.n = n;
+      ts.R = R;
+      ts.xp = xp;
+      const sb_status tst = sbk::tc_create(&c->te, ts, c->dJ, jp, terr, st);
+      if (tst != SB_OK) {
+        c->te = nullptr;
+        if (prm->field_mode == SB_FIELD_TC) {
+          out = tst;
+          ctx->last_error = std::string(who) + ": " + terr;
+          goto cleanup_noerr;
+        }
+        use_tc = false;  // auto: the FP32 path runs every shape
+      }
     }
   }
-  NM_CUDA(cudaEventRecord(ev0, st));
-  NM_CUDA(sbk::launch_nmfa_seed(drng, n, R, xp, prm->seed, st));
+  NM_CUDA(cudaEventRecord(c->ev0, st));
+  NM_CUDA(sbk::launch_nmfa_seed(c->drng, n, R, xp, prm->seed, st));
   ++launches;
   if (use_tc) {
-    NM_CUDA(sbk::tc_prepare(te, ds, st));
-    NM_CUDA(sbk::tc_run_nmfa(te, 2 * stages, dbetas, ds, dz1, dnorm, drng, prm->noise,
-                             (float)(1.0 - (double)prm->recombination), prm->recombination, dstatus, st));
-    NM_CUDA(sbk::launch_nmfa_signs(ds, n, R, xp, dsamp, st));
-    NM_CUDA(sbk::tc_nmfa_energy(te, ds, den, dstatus, st));
+    NM_CUDA(sbk::tc_prepare(c->te, c->ds, st));
+    NM_CUDA(sbk::tc_run_nmfa(c->te, 2 * stages, c->dbetas, c->ds, c->dz1, c->dnorm, c->drng, prm->noise,
+                             (float)(1.0 - (double)prm->recombination), prm->recombination, c->dstatus, st));
+    NM_CUDA(sbk::launch_nmfa_signs(c->ds, n, R, xp, c->dsamp, st));
+    NM_CUDA(sbk::tc_nmfa_energy(c->te, c->ds, c->den, c->dstatus, st));
     launches += 5;
   } else {
     sbk::NmfaSweep a;
@@ -159,23 +199,23 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     a.jp = jp;
     a.xp = xp;
     a.rb = rb;
-    a.J = dJ;
-    a.norm = dnorm;
-    a.rng = drng;
-    a.z1 = dz1;
+    a.J = c->dJ;
+    a.norm = c->dnorm;
+    a.rng = c->drng;
+    a.z1 = c->dz1;
     a.noise = prm->noise;
     a.keep = (float)(1.0 - (double)prm->recombination);  // nmfa.cu:95, 1.0 - recombination
     a.mix = prm->recombination;
-    a.status = dstatus;
+    a.status = c->dstatus;
     a.overlap = 1;
     int cur = 0;
     for (int t = 0; t < stages; ++t)
       for (int k = 0; k < 2; ++k) {
-        a.s_in = ds + (size_t)cur * plane;
-        a.s_out = ds + (size_t)(cur ^ 1) * plane;
+        a.s_in = c->ds + (size_t)cur * plane;
+        a.s_out = c->ds + (size_t)(cur ^ 1) * plane;
         a.beta = betas[t];
         a.first = k == 0 ? 1 : 0;
-        a.samples = (t + 1 == stages && k == 1) ? dsamp : nullptr;
+        a.samples = (t + 1 == stages && k == 1) ? c->dsamp : nullptr;
         NM_CUDA(sbk::launch_nmfa_sweep(a, st));
         ++launches;
         cur ^= 1;
@@ -188,29 +228,30 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     pe.jp = jp;
     pe.xp = xp;
     pe.rb = rb;
-    pe.J = dJ;
+    pe.J = c->dJ;
     pe.h = nullptr;
-    pe.x = ds;
-    pe.energy = den;
-    pe.status = dstatus;
+    pe.x = c->ds;
+    pe.energy = c->den;
+    pe.status = c->dstatus;
     NM_CUDA(sbk::launch_plain_energy(pe, !exact, st));
     ++launches;
   }
-  NM_CUDA(cudaEventRecord(ev1, st));
-  NM_CUDA(cudaMemcpyAsync(hsamp.data(), dsamp, hsamp.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  NM_CUDA(cudaMemcpyAsync(hen.data(), den, hen.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  NM_CUDA(cudaEventRecord(c->ev1, st));
+  NM_CUDA(cudaMemcpyAsync(samp, c->dsamp, (size_t)R * n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  NM_CUDA(cudaMemcpyAsync(hen.data(), c->den, hen.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (res && res->states)
-    NM_CUDA(cudaMemcpy2DAsync(res->states, (size_t)n * sizeof(float), ds, (size_t)xp * sizeof(float),
+    NM_CUDA(cudaMemcpy2DAsync(res->states, (size_t)n * sizeof(float), c->ds, (size_t)xp * sizeof(float),
                               (size_t)n * sizeof(float), (size_t)R, cudaMemcpyDeviceToHost, st));
-  NM_CUDA(cudaMemcpyAsync(&hstatus, dstatus, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  NM_CUDA(cudaMemcpyAsync(&hstatus, c->dstatus, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   NM_CUDA(cudaStreamSynchronize(st));
   if (hstatus) {
     out = (hstatus & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
     ctx->last_error = std::string(who) + ": device status " + std::to_string(hstatus);
+    sbh::nmfa_cache_free(c);
+    ctx->nmfa = nullptr;
     goto cleanup_noerr;
   }
-  NM_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));
-  if (samples32) memcpy(samples32, hsamp.data(), hsamp.size() * sizeof(int32_t));
+  NM_CUDA(cudaEventElapsedTime(&dev_ms, c->ev0, c->ev1));
   if (res) {
     // the energy pass gives H = -1/2 s J s (fields are 0): NMFA's E is -H
     int best = 0;
@@ -219,9 +260,9 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
       if (hen[r] < hen[best]) best = r;
     }
     std::vector<int8_t> sp((size_t)n);
-    for (int i = 0; i < n; ++i) sp[i] = (int8_t)hsamp[(size_t)best * n + i];
+    for (int i = 0; i < n; ++i) sp[i] = (int8_t)samp[(size_t)best * n + i];
     if (res->samples)
-      for (size_t k = 0; k < hsamp.size(); ++k) res->samples[k] = (int8_t)hsamp[k];
+      for (size_t k = 0; k < (size_t)R * n; ++k) res->samples[k] = (int8_t)samp[k];
     if (res->energies) memcpy(res->energies, hen.data(), (size_t)R * sizeof(double));
     if (res->best_spins) memcpy(res->best_spins, sp.data(), (size_t)n);
     double check;
@@ -243,20 +284,10 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
 cleanup:
   out = e == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
   ctx->last_error = std::string(who) + ": " + where + ": " + cudaGetErrorString(e);
-cleanup_noerr:
-  cudaFreeAsync(dJ, st);
-  cudaFreeAsync(dnorm, st);
-  cudaFreeAsync(ds, st);
-  cudaFreeAsync(dz1, st);
-  cudaFreeAsync(drng, st);
-  cudaFreeAsync(dsamp, st);
-  cudaFreeAsync(den, st);
-  cudaFreeAsync(dstatus, st);
-  if (dbetas) cudaFreeAsync(dbetas, st);
   cudaStreamSynchronize(st);
-  sbk::tc_destroy(te);
-  if (ev0) cudaEventDestroy(ev0);
-  if (ev1) cudaEventDestroy(ev1);
+  sbh::nmfa_cache_free(ctx->nmfa);  // a failed call leaves nothing behind
+  ctx->nmfa = nullptr;
+cleanup_noerr:
 #undef NM_CUDA
   if (out == SB_OK && res)
     res->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -428,6 +428,17 @@ __global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
   }
 }
 
+// norm[i] = -1 / sqrt(sum_j |J_ij|) (nmfa.cu:88-93) with the sum in double over j in index order and
+// the result rounded once to float (the host oracle's operations, IEEE double); 0 for an empty row.
+__global__ void nmfa_norms_kernel(const float *J, int n, int jp, float *norm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *row = J + (size_t)i * jp;
+  double a = 0.0;
+  for (int j = 0; j < n; ++j) a = __dadd_rn(a, fabs((double)row[j]));
+  norm[i] = a > 0.0 ? __double2float_rn(__ddiv_rn(-1.0, __dsqrt_rn(a))) : 0.0f;
+}
+
 // samples[r][i] = s > 0 ? +1 : -1 (nmfa.cu:139) from the final states [R][xp]
 __global__ void nmfa_signs_kernel(const float *s, int n, int R, int xp, int32_t *samples) {
   const size_t total = (size_t)n * R;
@@ -651,6 +662,11 @@ cudaError_t launch_nmfa_sweep(const NmfaSweep &a0, cudaStream_t st) {
   cfg.numAttrs = (a.overlap && !wide) ? 1 : 0;
   return wide ? cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<true>, a)
               : cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<false>, a);
+}
+
+cudaError_t launch_nmfa_norms(const float *J, int n, int jp, float *norm, cudaStream_t st) {
+  nmfa_norms_kernel<<<(n + 127) / 128, 128, 0, st>>>(J, n, jp, norm);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_nmfa_signs(const float *s, int n, int R, int xp, int32_t *samples, cudaStream_t st) {

@@ -232,21 +232,53 @@ extern "C" double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
 // ---------------------------------------------------------------------------------------------
 // Problem bookkeeping.
 
+// Integrality, max |J| and the edge count of the couplings: branch-free row loops (vectorised), rows
+// dealt round-robin to host threads for large n; none of the three depends on the order.
 void sbh::problem_scan(sb_problem *p) {
   const int n = p->n;
+  const int nt = auto_threads(n, 0);
+  std::vector<int> nonint((size_t)nt, 0);
+  std::vector<float> mx((size_t)nt, 0.0f);
+  std::vector<int64_t> ed((size_t)nt, 0);
+  auto rows = [&](int t) {
+    int bad = 0;
+    float m = 0.0f;
+    int64_t e = 0;
+    for (int i = t; i < n; i += nt) {
+      const float *Ji = p->J + (size_t)i * n;
+      int rb = 0;
+      float rm = 0.0f;
+      for (int j = 0; j < n; ++j) {
+        const float w = Ji[j];
+        rb |= (w != floorf(w)) ? 1 : 0;  // NaN is not integral
+        const float a = fabsf(w);
+        rm = a > rm ? a : rm;
+      }
+      int64_t re = 0;
+      for (int j = i + 1; j < n; ++j) re += Ji[j] != 0.0f ? 1 : 0;
+      bad |= rb;
+      m = rm > m ? rm : m;
+      e += re;
+    }
+    nonint[t] = bad;
+    mx[t] = m;
+    ed[t] = e;
+  };
+  if (nt == 1) {
+    rows(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(rows, t);
+    rows(0);
+    for (auto &x : th) x.join();
+  }
   bool integral = true;
   double maxabs = 0.0;
   int64_t edges = 0;
-  for (int i = 0; i < n; ++i) {
-    const float *Ji = p->J + (size_t)i * n;
-    for (int j = 0; j < n; ++j) {
-      const float w = Ji[j];
-      if (w == 0.0f) continue;
-      if (j > i) ++edges;
-      if (w != floorf(w)) integral = false;
-      const double a = fabs((double)w);
-      if (a > maxabs) maxabs = a;
-    }
+  for (int t = 0; t < nt; ++t) {
+    integral = integral && !nonint[t];
+    maxabs = (double)mx[t] > maxabs ? (double)mx[t] : maxabs;
+    edges += ed[t];
   }
   if (p->h)
     for (int i = 0; i < n; ++i)
