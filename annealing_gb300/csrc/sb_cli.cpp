@@ -12,8 +12,8 @@
 // --variant nmfa runs noisy mean-field annealing, the drop-in for NMFA/CUDA_GPU/Ising.cpp (100
 // stages of its beta schedule, alpha = sigma = 0.15, seed 1234, one sample; the first line of stdout
 // is the elapsed ms it prints, Ising.cpp:48); --steps sets the stages, --replicas the samples,
-// --noise / --recombination sigma and alpha; output.txt holds each sample's energy
-// E = sum_{i<j} J_ij s_i s_j and best_spins.txt the best sample.
+// --noise / --recombination sigma and alpha, --field fp32|tc the field; output.txt holds each
+// sample's energy E = sum_{i<j} J_ij s_i s_j and best_spins.txt the best sample.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -225,6 +225,7 @@ int main(int argc, char **argv) {
     nq.stages = p.steps;
     nq.samples = p.replicas;
     nq.seed = (uint32_t)p.seed;
+    nq.field_mode = p.field_mode;
     const int rc = run_nmfa(ctx, &prob, nq, out_path, spins_path, json);
     sb_destroy(ctx);
     sb_problem_free(&prob);
