@@ -201,7 +201,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   constexpr bool kStageV = C::kBParts == 1;
   constexpr int kVRow = kBM * C::kElem;      // bytes of one replica row of the unit's V tile
   constexpr uint32_t kTx = (uint32_t)kStage;
-  constexpr uint32_t kCols = 4 * NR <= 32 ? 32 : (4 * NR <= 64 ? 64 : (4 * NR <= 128 ? 128 : (4 * NR <= 256 ? 256 : 512)));
+  // NMFA draws stage k+1's noise pair ahead, in the idle time after stage k's sweeps publish (the
+  // first chunk of a thread's columns after the first sweep, the rest after the second), when three
+  // more column blocks fit TMEM (z0, and z1 alternating between y and y1 by stage parity);
+  // otherwise on the stage's first sweep
+  constexpr bool kNoiseAhead = VARIANT == 3 && 6 * NR <= 512;
+  constexpr int kUsedCols = kNoiseAhead ? 6 * NR : 4 * NR;
+  constexpr uint32_t kCols = kUsedCols <= 32 ? 32 : (kUsedCols <= 64 ? 64 : (kUsedCols <= 128 ? 128 : (kUsedCols <= 256 ? 256 : 512)));
   constexpr uint32_t kIdesc = make_idesc(DT, kBM, NR);
   constexpr int kHalf = NR / 2;               // columns per epilogue warp
   static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
@@ -246,8 +252,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
-  // columns: accumulators [0, NR) and [NR, 2NR), x [2NR, 3NR), y [3NR, 4NR)
-  const uint32_t t_x = tmem + 2 * NR, t_y = tmem + 3 * NR;
+  // columns: accumulators [0, NR) and [NR, 2NR), x [2NR, 3NR), y [3NR, 4NR); NMFA with the noise
+  // drawn ahead: z0 [4NR, 5NR), y1 [5NR, 6NR) (stage k's z1 in y for even k, in y1 for odd k)
+  const uint32_t t_x = tmem + 2 * NR, t_y = tmem + 3 * NR, t_z0 = tmem + 4 * NR, t_y1 = tmem + 5 * NR;
 
   if (warp == 0) {
     // ---------------- TMA producer (lane 0 issues; the warp polls the column's flags) ----------------
@@ -374,6 +381,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       }
       ptx::tmem_st_wait();
     }
+    // NMFA: one stage's Gaussian pair (nmfa.cu:103-109) for this thread's columns [c0, c1) (whole
+    // 16-column chunks), z0 into the z0 columns and z1 into t_zdst; the XORWOW words are loaded
+    // kDrawBatch elements at a time
+    constexpr int kDrawBatch = 4;
+    auto draw_stage = [&](int c0, int c1, uint32_t t_zdst) {
+      const size_t plane = (size_t)p.R * p.xp;
+#pragma unroll 1
+      for (int c = c0; c < c1; c += 16) {
+        uint32_t z0[16], z1[16];
+#pragma unroll
+        for (int g = 0; g < 16; g += kDrawBatch) {
+          uint32_t wd[kDrawBatch][5];
+#pragma unroll
+          for (int jj = 0; jj < kDrawBatch; ++jj) {
+            const int r = r0 + c + g + jj;
+            const bool in = row < p.n && r < p.R;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) wd[jj][q] = in ? p.rng[q * plane + (size_t)r * p.xp + row] : 0u;
+          }
+#pragma unroll
+          for (int jj = 0; jj < kDrawBatch; ++jj) {
+            const int r = r0 + c + g + jj;
+            float a = 0.0f, b = 0.0f;
+            if (row < p.n && r < p.R) {
+              sbm::nmfa_gauss(wd[jj], p.noise, a, b);
+#pragma unroll
+              for (int q = 0; q < 5; ++q) p.rng[q * plane + (size_t)r * p.xp + row] = wd[jj][q];
+            }
+            z0[g + jj] = __float_as_uint(a);
+            z1[g + jj] = __float_as_uint(b);
+          }
+        }
+        ptx::tmem_st16(t_z0 + lane_off + c, z0);
+        ptx::tmem_st16(t_zdst + lane_off + c, z1);
+      }
+      ptx::tmem_st_wait();
+    };
+    // the persistent NMFA run starts on a stage's first sweep (t0 even): draw that stage
+    if constexpr (kNoiseAhead) {
+      if (nsteps > 0 && (p.t0 & 1) == 0) draw_stage(c_lo, c_lo + kHalf, ((p.t0 >> 1) & 1) ? t_y1 : t_y);
+    }
     float pump_next = (!kEOnly && nsteps > 0) ? p.pumps[p.t0] : 0.0f;
     for (int ls = 0; ls < nsteps; ++ls) {
       const int t = p.t0 + ls;
@@ -396,7 +444,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         ptx::tmem_ld16(t_acc + lane_off + c, va);
         if constexpr (!kEOnly) {
           ptx::tmem_ld16(t_x + lane_off + c, vx);
-          ptx::tmem_ld16(t_y + lane_off + c, vy);
+          // NMFA with the noise drawn ahead: vy holds this sweep's sample (z0 on a stage's first
+          // sweep, z1 = y on its second), and y is never written here
+          ptx::tmem_ld16((kNoiseAhead ? ((t & 1) == 0 ? t_z0 : (((t >> 1) & 1) ? t_y1 : t_y)) : t_y) + lane_off + c,
+                         vy);
         }
         ptx::tmem_ld_wait();
         float e2[16];
@@ -420,9 +471,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           }
           if (!kEOnly && in) {
             if constexpr (VARIANT == 3) {
-              // even sweeps open a stage: draw its pair, keep the second sample in y
+              // even sweeps open a stage: its first sample (drawn ahead, or drawn here with the
+              // second kept in y); odd sweeps use the second
               float z = y;
-              if (((t & 1) == 0)) {
+              if constexpr (kNoiseAhead) {
+              } else if (((t & 1) == 0)) {
                 const size_t plane = (size_t)p.R * p.xp, k = (size_t)r * p.xp + row;
                 uint32_t wd[5];
 #pragma unroll
@@ -450,7 +503,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         }
         if constexpr (!kEOnly) {
           ptx::tmem_st16(t_x + lane_off + c, vx);
-          ptx::tmem_st16(t_y + lane_off + c, vy);
+          if constexpr (!kNoiseAhead) ptx::tmem_st16(t_y + lane_off + c, vy);
         }
         if constexpr (want_e) {
 #pragma unroll
@@ -479,6 +532,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         ptx::fence_proxy_async_global();
         __threadfence();
         st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
+      }
+      // NMFA: the next stage's noise, while the column's units finish this sweep and the next
+      // contraction streams in: its first chunk after this stage's first sweep (whose z0 is
+      // consumed; its z1 goes to the other z1 block), the rest after the second
+      if constexpr (kNoiseAhead) {
+        const uint32_t t_znext = (((t >> 1) + 1) & 1) ? t_y1 : t_y;
+        constexpr int kFirst = kHalf > 16 ? 16 : 0;  // columns drawn after the first sweep
+        if ((t & 1) == 0 && ls + 2 < nsteps && kFirst > 0) draw_stage(c_lo, c_lo + kFirst, t_znext);
+        if ((t & 1) == 1 && ls + 1 < nsteps) draw_stage(c_lo + kFirst, c_lo + kHalf, t_znext);
       }
       if constexpr (want_e) {
         for (int c = threadIdx.x - kEpiFirstThread; c < NR; c += kEpiThreads) {
