@@ -68,8 +68,9 @@ struct NmfaSweep {
 // Sets kernel attributes (dynamic shared memory limits) once per process; call before any capture.
 void init_kernel_attributes();
 cudaError_t launch_nmfa_sweep(const NmfaSweep &a, cudaStream_t st);
-// The NMFA row norms -1 / sqrt(sum_j |J_ij|) from the padded couplings [n][jp].
-cudaError_t launch_nmfa_norms(const float *J, int n, int jp, float *norm, cudaStream_t st);
+// The NMFA row norms -1 / sqrt(sum_j |J_ij|) from the padded couplings [n][jp]; integral: every
+// coupling an integer with n max|J| < 2^53 (the sum is then exact in any order).
+cudaError_t launch_nmfa_norms(const float *J, int n, int jp, float *norm, bool integral, cudaStream_t st);
 // samples[r][i] = +-1 from the signs of the states [R][xp].
 cudaError_t launch_nmfa_signs(const float *s, int n, int R, int xp, int32_t *samples, cudaStream_t st);
 // Initial XORWOW words of every (sample, spin); rng as in NmfaSweep.

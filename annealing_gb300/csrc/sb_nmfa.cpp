@@ -152,7 +152,8 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
   NM_CUDA(cudaMemcpy2DAsync(c->dJ, (size_t)jp * sizeof(float), prob->J, (size_t)n * sizeof(float),
                             (size_t)n * sizeof(float), (size_t)n, cudaMemcpyHostToDevice, st));
   // norm_i = -1 / sqrt(sum_j |J_ij|) (nmfa.cu:88-93), on the device from the uploaded couplings
-  NM_CUDA(sbk::launch_nmfa_norms(c->dJ, n, jp, c->dnorm, st));
+  NM_CUDA(sbk::launch_nmfa_norms(c->dJ, n, jp, c->dnorm,
+                                  prob->integer_valued && (double)prob->max_abs_j * n < 9.0e15, st));
   NM_CUDA(cudaMemcpyAsync(c->dbetas, sweep_betas.data(), sweep_betas.size() * sizeof(float), cudaMemcpyHostToDevice,
                           st));
   NM_CUDA(cudaMemsetAsync(c->ds, 0, 2 * plane * sizeof(float), st));

@@ -439,6 +439,19 @@ __global__ void nmfa_norms_kernel(const float *J, int n, int jp, float *norm) {
   norm[i] = a > 0.0 ? __double2float_rn(__ddiv_rn(-1.0, __dsqrt_rn(a))) : 0.0f;
 }
 
+// The same norms for integer couplings (n max|J| < 2^53): every partial sum is an exact integer in
+// double, so one warp per row sums coalesced strips and a butterfly, with the sequential sum's value.
+__global__ void nmfa_norms_int_kernel(const float *J, int n, int jp, float *norm) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const float *row = J + (size_t)i * jp;
+  double a = 0.0;
+  for (int j = lane; j < n; j += 32) a += fabs((double)row[j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) norm[i] = a > 0.0 ? __double2float_rn(__ddiv_rn(-1.0, __dsqrt_rn(a))) : 0.0f;
+}
+
 // samples[r][i] = s > 0 ? +1 : -1 (nmfa.cu:139) from the final states [R][xp]
 __global__ void nmfa_signs_kernel(const float *s, int n, int R, int xp, int32_t *samples) {
   const size_t total = (size_t)n * R;
@@ -664,8 +677,11 @@ cudaError_t launch_nmfa_sweep(const NmfaSweep &a0, cudaStream_t st) {
               : cudaLaunchKernelEx(&cfg, nmfa_sweep_kernel<false>, a);
 }
 
-cudaError_t launch_nmfa_norms(const float *J, int n, int jp, float *norm, cudaStream_t st) {
-  nmfa_norms_kernel<<<(n + 127) / 128, 128, 0, st>>>(J, n, jp, norm);
+cudaError_t launch_nmfa_norms(const float *J, int n, int jp, float *norm, bool integral, cudaStream_t st) {
+  if (integral)
+    nmfa_norms_int_kernel<<<(n + 7) / 8, 256, 0, st>>>(J, n, jp, norm);
+  else
+    nmfa_norms_kernel<<<(n + 127) / 128, 128, 0, st>>>(J, n, jp, norm);
   return cudaGetLastError();
 }
 

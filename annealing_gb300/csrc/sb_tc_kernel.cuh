@@ -25,7 +25,8 @@
 // VARIANT 3 is NMFA (noisy mean-field annealing, NMFA/CUDA_GPU/src/nmfa.cu:99-136) on the same
 // pipeline: x holds the mean-field state s, y the stage's second Gaussian sample, h the row norms,
 // pumps[t] the inverse temperature of sweep t; the operand is s as BF16 hi + lo against exact BF16
-// couplings, and the epilogue draws the stage's noise pair on even sweeps (XORWOW words in rng).
+// couplings; the epilogue applies the NMFA update and draws each stage's noise pair (XORWOW words
+// in rng) a stage ahead into TMEM, or on the stage's first sweep when the extra columns do not fit.
 // Operand dtypes: FP8 E4M3 holds +-1 and integers |J| <= 16 exactly; BF16 holds integers up to 256;
 // BF16 hi + lo (J = Jh + Jl, x = xh + xl) gives ~16 bits for real values, with the three products
 // Jh*xh + Jh*xl + Jl*xh accumulated in FP32. Integer fields are exact whenever every partial sum
