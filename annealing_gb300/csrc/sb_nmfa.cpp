@@ -277,7 +277,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     res->best_sample = best;
     res->device_ms = dev_ms;
     res->kernel_launches = launches;
-    res->field_used = use_tc ? SB_FIELD_TC : SB_FIELD_FP32;
+    res->field_mode_used = use_tc ? SB_FIELD_TC : SB_FIELD_FP32;
     const double updates = (double)n * R * 2.0 * stages;
     res->spin_updates_per_s = dev_ms > 0 ? updates / ((double)dev_ms * 1e-3) : 0.0;
   }

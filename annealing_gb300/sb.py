@@ -216,7 +216,7 @@ class NmfaResultStruct(C.Structure):
         ("total_ms", C.c_double),
         ("spin_updates_per_s", C.c_double),
         ("kernel_launches", C.c_int64),
-        ("field_used", C.c_int32),
+        ("field_mode_used", C.c_int32),
     ]
 
 
@@ -232,7 +232,7 @@ class NmfaResult:
     total_ms: float
     spin_updates_per_s: float
     kernel_launches: int
-    field_used: int = 0                   # FIELD_FP32 or FIELD_TC
+    field_mode_used: int = 0                   # FIELD_FP32 or FIELD_TC
     states: Optional[np.ndarray] = None   # [samples, n] final mean-field states
 
 
@@ -601,7 +601,7 @@ class Context:
         return NmfaResult(samples=samples, energies=energies, best_spins=best, best_energy=r.best_energy,
                           best_sample=r.best_sample, energy_check_ok=bool(r.energy_check_ok), device_ms=r.device_ms,
                           total_ms=r.total_ms, spin_updates_per_s=r.spin_updates_per_s,
-                          kernel_launches=r.kernel_launches, field_used=r.field_used, states=states)
+                          kernel_launches=r.kernel_launches, field_mode_used=r.field_mode_used, states=states)
 
     def gpu_nmfa(self, J: np.ndarray, betas, num_samples: int, noise: float = 0.15, recombination: float = 0.15,
                  seed: int = 1234):

@@ -788,7 +788,7 @@ def run_nmfa(args, rank, world, local_rank):
         ctx.close()
         return
     flops = 2.0 * n * n * R * 2 * stages / (total_dev / args.steps * 1e-3)
-    tc = results[-1].field_used == sb.FIELD_TC
+    tc = results[-1].field_mode_used == sb.FIELD_TC
     _, bf16_peak, peak_kind = peaks()
     line = {
         "metric": "NMFA spin-updates/s", "value": value, "unit": "spin-updates/s", "n_gpus": world,

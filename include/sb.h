@@ -410,7 +410,7 @@ typedef struct sb_nmfa_result {
   double total_ms;          /* the whole call, host clock */
   double spin_updates_per_s;  /* n * samples * 2 * stages / device time */
   int64_t kernel_launches;
-  int32_t field_used;       /* SB_FIELD_FP32 or SB_FIELD_TC: the path that ran */
+  int32_t field_mode_used;  /* SB_FIELD_FP32 or SB_FIELD_TC: the path that ran */
 } sb_nmfa_result;
 
 /* samples 1, stages 100 with the reference schedule, noise 0.15, recombination 0.15, seed 1234

@@ -57,7 +57,7 @@ def test_bit_exact_vs_oracle(ctx, n, R, stages, kind):
     e = _energies(J, sp)
     assert np.array_equal(res.energies, e.astype(np.float64))
     assert res.best_energy == e.min() and res.energy_check_ok
-    assert res.kernel_launches == 1 + 2 * stages + 1 and res.field_used == sb.FIELD_FP32
+    assert res.kernel_launches == 1 + 2 * stages + 1 and res.field_mode_used == sb.FIELD_FP32
 
 
 def test_real_couplings_bit_exact(ctx):
@@ -176,7 +176,7 @@ def test_tensor_core_vs_oracle(ctx, n, R, stages):
           f"median {np.median(d):.3e}, sign agreement {agree:.4f}")
     assert np.quantile(d, 0.99) <= 2e-3
     assert agree >= 0.99
-    assert res.energy_check_ok and res.field_used == sb.FIELD_TC and res.kernel_launches == 6
+    assert res.energy_check_ok and res.field_mode_used == sb.FIELD_TC and res.kernel_launches == 6
     assert np.array_equal(res.energies, _energies(J, res.samples).astype(np.float64))
 
 
