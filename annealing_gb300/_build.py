@@ -3,6 +3,9 @@
 Everything is compiled with plain nvcc / gcc calls (no cmake), object files in parallel:
   annealing_gb300/libsbsolve.so   CUDA kernels (sm_103a) + C ABI (include/sb.h)
   annealing_gb300/sb              command-line drop-in for the reference's `./opt <graph>`
+  annealing_gb300/_checked/libsbsolve.so
+                                  the same library with device bounds checks (-DSB_CHECKS), built
+                                  on request (build_library(checks=True)) for the checked test run
   oracle/libsboracle.so           CPU oracle + multithreaded CPU baseline (test infrastructure)
 """
 from __future__ import annotations
@@ -17,6 +20,7 @@ PKG = os.path.join(ROOT, "annealing_gb300")
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
+CHECKED = os.path.join(PKG, "_checked")
 ORACLE = os.path.join(ROOT, "oracle")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -51,15 +55,17 @@ def _headers() -> list[str]:
     return hs
 
 
-def build_library(force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build_library(force: bool = False, checks: bool = False) -> str:
+    """The solver library (and its CLI); checks=True: the bounds-checked library only, in _checked/."""
+    bdir = os.path.join(CHECKED, "_build") if checks else BUILD
+    os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC] + (["-DSB_CHECKS"] if checks else [])
     hdrs = _headers()
     objs, jobs = [], []
     for src in LIB_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(bdir, src + ".o")
         objs.append(o)
         if force or not _newer(o, [s] + hdrs):
             if src.endswith(".cu"):
@@ -70,9 +76,11 @@ def build_library(force: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
-    lib = os.path.join(PKG, "libsbsolve.so")
+    lib = os.path.join(CHECKED if checks else PKG, "libsbsolve.so")
     if force or jobs or not os.path.exists(lib):
         _run([nvcc, *GENCODE, "-shared", "-o", lib, *objs, "-lpthread"])
+    if checks:
+        return lib
     cli = os.path.join(PKG, "sb")
     cli_src = os.path.join(CSRC, "sb_cli.cpp")
     if force or not _newer(cli, [cli_src, lib] + hdrs):

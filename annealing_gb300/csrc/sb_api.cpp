@@ -513,8 +513,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   }
   SB_CUDA(cudaEventRecord(pl->ev1, st));
   if (status != 0) {
-    err = "device status " + std::to_string(status) +
-          ((status & sbk::kErrWaitTimeout) ? " (a bounded wait timed out)" : "");
+    err = sbh::device_status_text(status);
     return (status & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
   }
   int best = 0;

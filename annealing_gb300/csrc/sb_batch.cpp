@@ -258,7 +258,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
     return SB_ERR_CUDA;
   }
   if (status) {
-    err = "device status " + std::to_string(status);
+    err = sbh::device_status_text(status);
     return (status & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
   }
   float dev_ms = 0;

@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int r = w.r0 + c + j;
-            if (row < n && r < R) {
+            if (row < n && r < R && SB_BOUNDS(row < xp && (FP4 || row < kb) && r < in->Rp, status)) {
               const size_t k = (size_t)r * xp + row;
               xs[k] = xv[j];
               ys[k] = yv[j];
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
               const int r = w.r0 + c + (odd ? 8 : 0) + j;
-              if (row_e < n && r < R)
+              if (row_e < n && r < R && SB_BOUNDS((row_e >> 1) < kb && r < in->Rp, status))
                 vn[(size_t)r * kb + (row_e >> 1)] =
                     (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
             }

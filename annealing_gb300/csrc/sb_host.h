@@ -22,6 +22,8 @@ float default_c0(const sb_problem *p, int threads);
 
 struct NmfaCache;
 namespace sbh {
+// "device status S (...)": the status word of a kernel run, its bits spelled out.
+std::string device_status_text(uint32_t status);
 // Frees an NMFA buffer cache (sb_nmfa.cpp); null is a no-op.
 void nmfa_cache_free(NmfaCache *c);
 }  // namespace sbh

@@ -12,7 +12,17 @@ enum : uint32_t {
   kErrWaitTimeout = 1u,     // a bounded mbarrier / flag wait gave up
   kErrBadShape = 2u,        // launch shape does not match the arguments
   kErrTmemAlloc = 4u,       // TMEM allocation failed
+  kErrBounds = 8u,          // a checked build found an index outside its buffer (the access was skipped)
 };
+
+// Bounds checks of the checked build (-DSB_CHECKS, the debug stand-in for a memory sanitizer): a
+// failing check records kErrBounds in the status word and the guarded access is skipped. In the
+// normal build the condition is not evaluated and the access is unconditional.
+#ifdef SB_CHECKS
+#define SB_BOUNDS(cond, status) ((cond) ? true : (atomicOr((status), sbk::kErrBounds), false))
+#else
+#define SB_BOUNDS(cond, status) true
+#endif
 
 // Row pitch (elements) of the padded state and coupling layouts.
 inline int pitch_for(int n, int align) { return (n + align - 1) / align * align; }

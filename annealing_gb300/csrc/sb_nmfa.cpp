@@ -247,7 +247,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
   NM_CUDA(cudaStreamSynchronize(st));
   if (hstatus) {
     out = (hstatus & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
-    ctx->last_error = std::string(who) + ": device status " + std::to_string(hstatus);
+    ctx->last_error = std::string(who) + ": " + sbh::device_status_text(hstatus);
     sbh::nmfa_cache_free(c);
     ctx->nmfa = nullptr;
     goto cleanup_noerr;

@@ -166,7 +166,7 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
     if (hstatus & kErrNotFp8Exact)
       return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: couplings must be integers with |J| <= 16");
     if (hstatus & sbk::kErrWaitTimeout) return fail(SB_ERR_TIMEOUT, "sb_dsb_solve_noalloc: a device wait timed out");
-    if (hstatus) return fail(SB_ERR_CUDA, "sb_dsb_solve_noalloc: device status " + std::to_string(hstatus));
+    if (hstatus) return fail(SB_ERR_CUDA, "sb_dsb_solve_noalloc: " + sbh::device_status_text(hstatus));
   }
 #undef NA_CUDA
   return SB_OK;

@@ -130,7 +130,8 @@ template <int MODE, typename Acc>
 __device__ __forceinline__ bool field_rows_ring(const float *__restrict__ J, int jp, int row0, int rows,
                                                 const float *__restrict__ xv, int xp, int r0, int rb,
                                                 int stages, float *smem, uint64_t *full,
-                                                Acc (&acc)[kMaxRB]) {
+                                                Acc (&acc)[kMaxRB], size_t jlim, size_t xlim,
+                                                uint32_t *status) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = (jp + kChunk - 1) / kChunk;
   const int stage_floats = (kRows + rb) * kChunk;
@@ -140,15 +141,17 @@ __device__ __forceinline__ bool field_rows_ring(const float *__restrict__ J, int
     const uint32_t bytes = (uint32_t)len_of(c) * 4u;
     ptx::mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)(rows + rb));
     for (int w = 0; w < rows; ++w)
-      ptx::bulk_g2s(smem + s * stage_floats + w * kChunk, J + (size_t)(row0 + w) * jp + c * kChunk,
-                    bytes, &full[s]);
+      if (SB_BOUNDS((size_t)(row0 + w) * jp + c * kChunk + bytes / 4 <= jlim, status))
+        ptx::bulk_g2s(smem + s * stage_floats + w * kChunk, J + (size_t)(row0 + w) * jp + c * kChunk,
+                      bytes, &full[s]);
   };
   auto issue_x = [&](int c) {
     const int s = c % stages;
     const uint32_t bytes = (uint32_t)len_of(c) * 4u;
     for (int rr = 0; rr < rb; ++rr)
-      ptx::bulk_g2s(smem + s * stage_floats + (kRows + rr) * kChunk,
-                    xv + (size_t)(r0 + rr) * xp + c * kChunk, bytes, &full[s]);
+      if (SB_BOUNDS((size_t)(r0 + rr) * xp + c * kChunk + bytes / 4 <= xlim, status))
+        ptx::bulk_g2s(smem + s * stage_floats + (kRows + rr) * kChunk,
+                      xv + (size_t)(r0 + rr) * xp + c * kChunk, bytes, &full[s]);
   };
   const int pre = min(nchunks, stages);
   if (tid == 0)
@@ -184,7 +187,8 @@ __device__ __forceinline__ bool field_rows_ring(const float *__restrict__ J, int
 template <int MODE, typename Acc>
 __device__ __forceinline__ bool field_rows_wide(const float *__restrict__ J, int jp, int row0, int rows,
                                                 const float *__restrict__ xv, int xp, int r0, int rb,
-                                                float *smem, uint64_t *full, Acc (&acc)[kMaxRB]) {
+                                                float *smem, uint64_t *full, Acc (&acc)[kMaxRB], size_t jlim,
+                                                size_t xlim, uint32_t *status) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunks = (jp + kChunk - 1) / kChunk;
   float *sJ = smem, *sV = smem + 2 * kRows * kChunk;
@@ -193,8 +197,9 @@ __device__ __forceinline__ bool field_rows_wide(const float *__restrict__ J, int
     const uint32_t bytes = (uint32_t)min(kChunk, jp - k0) * 4u;
     ptx::mbar_arrive_expect_tx(&full[c & 1], bytes * (uint32_t)rows);
     for (int w = 0; w < rows; ++w)
-      ptx::bulk_g2s(sJ + ((c & 1) * kRows + w) * kChunk, J + (size_t)(row0 + w) * jp + k0, bytes,
-                    &full[c & 1]);
+      if (SB_BOUNDS((size_t)(row0 + w) * jp + k0 + bytes / 4 <= jlim, status))
+        ptx::bulk_g2s(sJ + ((c & 1) * kRows + w) * kChunk, J + (size_t)(row0 + w) * jp + k0, bytes,
+                      &full[c & 1]);
   };
   if (tid == 0) {
     issue(0);
@@ -208,6 +213,7 @@ __device__ __forceinline__ bool field_rows_wide(const float *__restrict__ J, int
       const float *src = xv + (size_t)(r0 + rr) * xp + k0;
       float *dst = sV + rr * kChunk;
       for (int q = tid * 4; q < len; q += kThreads * 4) {
+        if (!SB_BOUNDS((size_t)(r0 + rr) * xp + k0 + q + 4 <= xlim, status)) continue;
         float4 t = *reinterpret_cast<const float4 *>(src + q);
         if (MODE == 1) {
           t.x = sgn(t.x);
@@ -235,14 +241,16 @@ __device__ __forceinline__ bool field_rows_wide(const float *__restrict__ J, int
 template <int MODE, bool WIDE, typename Acc>
 __device__ __forceinline__ bool field_rows(const float *__restrict__ J, int jp, int row0, int rows,
                                            const float *__restrict__ xv, int xp, int r0, int rb, int stages,
-                                           float *smem, uint64_t *full, Acc (&acc)[kMaxRB]) {
+                                           float *smem, uint64_t *full, Acc (&acc)[kMaxRB], size_t jlim,
+                                           size_t xlim, uint32_t *status) {
 #pragma unroll
   for (int q = 0; q < kMaxRB; ++q) acc[q] = Acc(0);
   bool ok;
   if constexpr (WIDE)
-    ok = field_rows_wide<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, smem, full, acc);
+    ok = field_rows_wide<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, smem, full, acc, jlim, xlim, status);
   else
-    ok = field_rows_ring<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, stages, smem, full, acc);
+    ok = field_rows_ring<MODE, Acc>(J, jp, row0, rows, xv, xp, r0, rb, stages, smem, full, acc, jlim, xlim,
+                                    status);
   // every thread leaves with the same verdict, so no thread skips a later barrier
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
   warp_sums(acc);
@@ -273,7 +281,8 @@ __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
   __syncthreads();
   float acc[kMaxRB];
   const bool ok = field_rows<VARIANT == 2 ? 1 : 0, WIDE, float>(
-      a.J, a.jp, row0, rows, a.x_in, a.xp, r0, rb, a.stages, reinterpret_cast<float *>(smem), full, acc);
+      a.J, a.jp, row0, rows, a.x_in, a.xp, r0, rb, a.stages, reinterpret_cast<float *>(smem), full, acc,
+      (size_t)a.n * a.jp, (size_t)a.R * a.xp, a.status);
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
     return;
@@ -304,8 +313,10 @@ __global__ void __launch_bounds__(kThreads) plain_step_kernel(PlainStep a) {
         red[w][rr] = -0.5 * (double)s * (double)f - (double)hv * (double)s;
       sb_update(f, hv, a.pump, a.c0, a.dt, a.dta0, x, y);
     }
-    a.x_out[k] = x;
-    a.y[k] = y;
+    if (SB_BOUNDS(k < (size_t)a.R * a.xp && i < a.n, a.status)) {
+      a.x_out[k] = x;
+      a.y[k] = y;
+    }
   }
   if (VARIANT == 2 && a.energy) {
     __syncthreads();
@@ -341,7 +352,8 @@ __global__ void __launch_bounds__(kThreads) plain_energy_kernel(PlainEnergy a) {
   Acc acc[kMaxRB];
   const bool ok =
       field_rows<1, WIDE, Acc>(a.J, a.jp, row0, rows, a.x, a.xp, r0, rb, a.stages,
-                               reinterpret_cast<float *>(smem), full, acc);
+                               reinterpret_cast<float *>(smem), full, acc, (size_t)a.n * a.jp, (size_t)a.R * a.xp,
+                               a.status);
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
     return;
@@ -393,7 +405,8 @@ __global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
   __syncthreads();
   float acc[kMaxRB];
   const bool ok = field_rows<0, WIDE, float>(a.J, a.jp, row0, rows, a.s_in, a.xp, r0, rb, a.stages,
-                                             reinterpret_cast<float *>(smem), full, acc);
+                                             reinterpret_cast<float *>(smem), full, acc, (size_t)a.n * a.jp,
+                                             (size_t)a.R * a.xp, a.status);
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
     return;
@@ -409,6 +422,7 @@ __global__ void __launch_bounds__(kThreads) nmfa_sweep_kernel(NmfaSweep a) {
     const int i = row0 + w, r = r0 + rr;
     const size_t k = (size_t)r * a.xp + i;
     const size_t plane = (size_t)a.R * a.xp;
+    if (!SB_BOUNDS(k < plane && i < a.n, a.status)) return;
     float z;
     if (a.first) {
       uint32_t wd[5];

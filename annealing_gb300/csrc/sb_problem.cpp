@@ -12,6 +12,7 @@
 
 #include "sb.h"
 #include "sb_host.h"
+#include "sb_internal.h"
 
 extern "C" {
 
@@ -231,6 +232,15 @@ extern "C" double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
 
 // ---------------------------------------------------------------------------------------------
 // Problem bookkeeping.
+
+std::string sbh::device_status_text(uint32_t status) {
+  std::string t = "device status " + std::to_string(status);
+  if (status & sbk::kErrWaitTimeout) t += " (a bounded wait timed out)";
+  if (status & sbk::kErrBadShape) t += " (a launch shape did not match its arguments)";
+  if (status & sbk::kErrTmemAlloc) t += " (TMEM allocation failed)";
+  if (status & sbk::kErrBounds) t += " (a device bounds check failed)";
+  return t;
+}
 
 // Integrality, max |J| and the edge count of the couplings: branch-free row loops (vectorised), rows
 // dealt round-robin to host threads for large n; none of the three depends on the order.

@@ -199,7 +199,8 @@ __global__ void __launch_bounds__(kSqaMaxWarps * 32, 1) sqa_kernel(const __grid_
     // (a write after reads: the barrier orders them, no proxy fence)
     for (; issued <= last; ++issued) {
       sbk::ptx::mbar_arrive_expect_tx(&bar[iss_slot], row_bytes);
-      sbk::ptx::bulk_g2s(ring + (size_t)iss_slot * RS, p.rows + (size_t)iss_row * RW, row_bytes, &bar[iss_slot]);
+      if (SB_BOUNDS(iss_row >= 0 && iss_row < n && iss_slot < S, p.status))
+        sbk::ptx::bulk_g2s(ring + (size_t)iss_slot * RS, p.rows + (size_t)iss_row * RW, row_bytes, &bar[iss_slot]);
       if (++iss_slot == S) iss_slot = 0;
       if (++iss_pos == per_step) {
         iss_pos = 0;
@@ -543,7 +544,7 @@ extern "C" sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *prob, const sb_
   SQ_CUDA(cudaStreamSynchronize(st));
   if (hstatus) {
     out = (hstatus & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
-    ctx->last_error = "sb_sqa_solve: device status " + std::to_string(hstatus);
+    ctx->last_error = "sb_sqa_solve: " + sbh::device_status_text(hstatus);
     goto cleanup_noerr;
   }
   SQ_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));

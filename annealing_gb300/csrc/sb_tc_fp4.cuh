@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           ptx::bulk_commit();
           ptx::bulk_wait_all();             // the half tile is in global memory
           ptx::fence_proxy_async_global();  // the bulk store's writes, then the flag (release)
-          st_release(p.flags + (size_t)(rt * H + h) * p.n_mtiles + mt, (uint32_t)(ls + 1));
+          if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status))
+            st_release(p.flags + (size_t)(rt * H + h) * p.n_mtiles + mt, (uint32_t)(ls + 1));
         }
       }
     }
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int r = r0 + c + j;
-            if (row < p.n && r < p.R) {
+            if (row < p.n && r < p.R && SB_BOUNDS(row < p.xp, p.status)) {
               p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
               p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
             }

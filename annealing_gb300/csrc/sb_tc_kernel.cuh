@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
 #pragma unroll
           for (int jj = 0; jj < kDrawBatch; ++jj) {
             const int r = r0 + c + g + jj;
-            const bool in = row < p.n && r < p.R;
+            const bool in = row < p.n && r < p.R && SB_BOUNDS(row < p.xp, p.status);
 #pragma unroll
             for (int q = 0; q < 5; ++q) wd[jj][q] = in ? p.rng[q * plane + (size_t)r * p.xp + row] : 0u;
           }
@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           for (int jj = 0; jj < kDrawBatch; ++jj) {
             const int r = r0 + c + g + jj;
             float a = 0.0f, b = 0.0f;
-            if (row < p.n && r < p.R) {
+            if (row < p.n && r < p.R && row < p.xp) {
               sbm::nmfa_gauss(wd[jj], p.noise, a, b);
 #pragma unroll
               for (int q = 0; q < 5; ++q) p.rng[q * plane + (size_t)r * p.xp + row] = wd[jj][q];
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
               // second kept in y); odd sweeps use the second
               float z = y;
               if constexpr (kNoiseAhead) {
-              } else if (((t & 1) == 0)) {
+              } else if (((t & 1) == 0) && SB_BOUNDS(row < p.xp, p.status)) {
                 const size_t plane = (size_t)p.R * p.xp, k = (size_t)r * p.xp + row;
                 uint32_t wd[5];
 #pragma unroll
@@ -489,7 +489,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             } else {
               sb_update(f, hv, pump, p.c0, p.dt, p.dta0, x, y);
             }
-            if constexpr (!kStageV) store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
+            if constexpr (!kStageV)
+              if (SB_BOUNDS((size_t)r * p.Kp + row < (size_t)p.Rp * p.Kp, p.status))
+                store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
           }
           if constexpr (kStageV && !kEOnly) {
             // every element of the tile is written (zero outside the problem) so the padding stays 0
@@ -532,7 +534,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         }
         ptx::fence_proxy_async_global();
         __threadfence();
-        st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
+        if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status))
+          st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
       }
       // NMFA: the next stage's noise, while the column's units finish this sweep and the next
       // contraction streams in: its first chunk after this stage's first sweep (whose z0 is
@@ -565,7 +568,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int r = r0 + c + j;
-          if (row < p.n && r < p.R) {
+          if (row < p.n && r < p.R && SB_BOUNDS(row < p.xp, p.status)) {
             p.x[(size_t)r * p.xp + row] = __uint_as_float(vx[j]);
             p.y[(size_t)r * p.xp + row] = __uint_as_float(vy[j]);
           }

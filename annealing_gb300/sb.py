@@ -15,7 +15,8 @@ from typing import Optional
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libsbsolve.so")
+# SB_LIBRARY selects another build of the same ABI (the bounds-checked one in _checked/)
+LIB_PATH = os.environ.get("SB_LIBRARY") or os.path.join(_HERE, "libsbsolve.so")
 
 # enums (sb.h)
 SB_OK, SB_ERR_PENDING = 0, 12
