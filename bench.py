@@ -69,6 +69,9 @@ NCU_TRAFFIC = {
     "batched-dsb": (19.58e6, "profiles/tc_fp4_kernel_batched_dsb_n2000_r1024.md"),
     # plain dSB, N=2000, R=1: bytes per launch (ncu runs the launch with cold caches)
     "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
+    # batched bSB, N=8192, R=256, BF16 hi+lo: bytes per SB step (8-step capture: 2.278 GB; 4 steps:
+    # 1.146 GB), times the launch's steps
+    "batched-bsb": (2.278e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
     # uneven batch: measured bytes per algorithmic byte on a 48-instance batch (441.2 MB of
     # 451.8 MB); the launch of the full batch is scaled by its algorithmic bytes
     "uneven-batch": (441.2 / 451.8, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
@@ -316,7 +319,12 @@ def run_ours(args, rank, world, local_rank):
                         "fp8e4m3": (2.0, "2 x {} dense BF16 burst (FP8 E4M3 rate)")}.get(fdt, (1.0, "{} dense BF16 burst"))
         tc_peak = scale * bf16
         achieved = flops_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e12
-        traffic = NCU_TRAFFIC["batched-dsb"] if (fdt == "fp4e2m1" and n == 2000 and R == 1024) else (None, None)
+        if fdt == "fp4e2m1" and n == 2000 and R == 1024:
+            traffic = NCU_TRAFFIC["batched-dsb"]
+        elif fdt == "bf16x2" and n == 8192 and R == 256:
+            traffic = (NCU_TRAFFIC["batched-bsb"][0] * rp.steps_per_launch, NCU_TRAFFIC["batched-bsb"][1])
+        else:
+            traffic = (None, None)
         roof = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
                 "frac": achieved / tc_peak, "traffic": traffic[0], "traffic_source": traffic[1],
                 "kernel": ("tc_fp4_kernel" if fdt == "fp4e2m1" else "tc_sb_kernel") + " (persistent, one launch per solve)",
