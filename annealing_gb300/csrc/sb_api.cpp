@@ -44,6 +44,7 @@ struct sb_plan {
   int n = 0, R = 0, jp = 0, xp = 0;
   int mode = SB_FIELD_FP32, dtype = 0;
   bool integral = false;
+  bool split_exact = false;  // integer couplings held exactly by BF16 hi + lo (|J| < 2^16)
   float c0 = 0, coeff = 0, dta0 = 0;
   float *dJ = nullptr, *dh = nullptr, *dx[2] = {nullptr, nullptr}, *dy = nullptr;
   double *denergy = nullptr;
@@ -247,6 +248,7 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   pl->mode = mode;
   pl->dtype = dtype;
   pl->integral = p->integer_valued != 0;
+  pl->split_exact = pl->integral && p->max_abs_j < 65536;
   pl->c0 = prm->c0 > 0.0f ? prm->c0 : sb_default_c0(p);
   const float xi = prm->xi > 0.0f ? prm->xi : (float)(0.7 * (double)prm->detune / sqrt((double)p->n));
   pl->coeff = (float)((double)prm->coupling_dt * (double)xi);
@@ -306,6 +308,11 @@ cudaError_t enqueue_energy(sb_plan *pl, const float *x, double *slot, cudaStream
                            int rows = -1) {
   if (pl->tc && pl->dtype != sbk::kTcBf16Split && pl->prm.variant == SB_DSB && t >= 0)
     return sbk::tc_energy(pl->tc, t, x, pl->dh, slot, pl->dstatus, st);
+  // split couplings (bSB, real-valued dSB): the final pass on the tensor cores too (FP32 sums of the
+  // hi and lo products: exact for integer couplings, and for real ones it ranks the replicas whose
+  // best kTopK are recomputed in FP64 below); FP64 passes stay on the plain kernel
+  if (pl->tc && pl->dtype == sbk::kTcBf16Split && t >= 0 && !fp64 && (pl->split_exact || !pl->integral))
+    return sbk::tc_energy_signs(pl->tc, x, pl->dh, slot, pl->dstatus, st);
   sbk::PlainEnergy a;
   const int R = rows > 0 ? rows : pl->R;
   a.n = pl->n;
@@ -490,6 +497,8 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
                           cudaMemcpyDeviceToHost, st));
   SB_CUDA(cudaMemcpyAsync(&status, pl->dstatus, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   SB_CUDA(cudaStreamSynchronize(st));
+  bool refined = false;
+  int order_best = 0;
   if (refine && R > kTopK && status == 0) {
     std::vector<int> order((size_t)R);
     for (int r = 0; r < R; ++r) order[r] = r;
@@ -509,16 +518,23 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
     SB_CUDA(cudaMemcpyAsync(ek, pl->dek, sizeof(ek), cudaMemcpyDeviceToHost, st));
     SB_CUDA(cudaStreamSynchronize(st));
     for (int q = 0; q < kTopK; ++q) e_final[order[q]] = ek[q];
-    // the best replica is chosen among the FP64-refined candidates
+    refined = true;
+    order_best = order[0];
+    for (int q = 1; q < kTopK; ++q)
+      if (e_final[order[q]] < e_final[order_best]) order_best = order[q];
   }
   SB_CUDA(cudaEventRecord(pl->ev1, st));
   if (status != 0) {
     err = sbh::device_status_text(status);
     return (status & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
   }
-  int best = 0;
-  for (int r = 1; r < R; ++r)
-    if (e_final[r] < e_final[best]) best = r;
+  // after a refinement the best replica is chosen among the FP64-refined candidates: a replica in
+  // the same state as one of them but outside the top kTopK keeps its FP32 energy, which may sit a
+  // rounding below the exact one
+  int best = refined ? order_best : 0;
+  if (!refined)
+    for (int r = 1; r < R; ++r)
+      if (e_final[r] < e_final[best]) best = r;
   SB_CUDA(cudaEventSynchronize(pl->ev1));
   std::vector<float> xb((size_t)n);
   SB_CUDA(cudaMemcpyAsync(xb.data(), final_x(pl) + (size_t)best * pl->xp, (size_t)n * sizeof(float),

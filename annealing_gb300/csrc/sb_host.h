@@ -65,9 +65,11 @@ cudaError_t tc_run(TcEngine *e, int steps, const float *pumps, float *x, float *
 // the XORWOW words; the operand must hold s (tc_prepare) on entry.
 cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, float *z1, const float *norm,
                         uint32_t *rng, float noise, float keep, float mix, uint32_t *status, cudaStream_t st);
-// NMFA engine: energy[r] += -1/2 sign(s_r) J sign(s_r) for every sample (the dSB energy contraction on
-// the engine's BF16 couplings; exact for integer J); overwrites operand buffer 0.
-cudaError_t tc_nmfa_energy(TcEngine *e, const float *s, double *energy, uint32_t *status, cudaStream_t st);
+// Engines with BF16 or BF16 hi + lo couplings (NMFA, bSB, dSB with real J): energy[r] += the energy of
+// sign(x_r), -1/2 s J s - h s, for every replica (the dSB energy contraction on the engine's
+// couplings; exact for integer J and h); overwrites operand buffer 0.
+cudaError_t tc_energy_signs(TcEngine *e, const float *x, const float *h, double *energy, uint32_t *status,
+                            cudaStream_t st);
 int tc_units(const TcEngine *e);
 int tc_replica_tile(const TcEngine *e);
 // Field-only pass on operand buffer (t & 1): energy of s(t) per replica (dSB, integer J).

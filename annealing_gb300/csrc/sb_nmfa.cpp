@@ -190,7 +190,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     NM_CUDA(sbk::tc_run_nmfa(c->te, 2 * stages, c->dbetas, c->ds, c->dz1, c->dnorm, c->drng, prm->noise,
                              (float)(1.0 - (double)prm->recombination), prm->recombination, c->dstatus, st));
     NM_CUDA(sbk::launch_nmfa_signs(c->ds, n, R, xp, c->dsamp, st));
-    NM_CUDA(sbk::tc_nmfa_energy(c->te, c->ds, c->den, c->dstatus, st));
+    NM_CUDA(sbk::tc_energy_signs(c->te, c->ds, nullptr, c->den, c->dstatus, st));
     launches += 5;
   } else {
     sbk::NmfaSweep a;

@@ -427,22 +427,25 @@ cudaError_t tc_run_nmfa(TcEngine *e, int sweeps, const float *betas, float *s, f
   return launch(e, kEmodeStep, a, st);
 }
 
-cudaError_t tc_nmfa_energy(TcEngine *e, const float *s, double *energy, uint32_t *status, cudaStream_t st) {
-  if (e->s.variant != 3) return cudaErrorInvalidValue;
-  // the dSB energy contraction on the same BF16 couplings: operand buffer 0 part 0 takes sign(s)
-  // (its padding is still zero), the kernel adds -1/2 s_i (J s)_i per sample into energy
+cudaError_t tc_energy_signs(TcEngine *e, const float *x, const float *h, double *energy, uint32_t *status,
+                            cudaStream_t st) {
+  // the dSB energy contraction on the engine's couplings (BF16 or BF16 hi + lo): operand buffer 0
+  // part 0 takes sign(x) (its padding is still zero) and the kernel adds -1/2 s_i (J s)_i - h_i s_i
+  // per replica into energy
   const void *k = nullptr;
   size_t smem = 0;
-  if (!tc_kernel_bf16(2, e->nr, kEmodeEnergy, &k, &smem)) return cudaErrorInvalidValue;
+  const bool have = e->s.dtype == kTcBf16 ? tc_kernel_bf16(2, e->nr, kEmodeEnergy, &k, &smem)
+                    : e->s.dtype == kTcBf16Split ? tc_kernel_split(2, e->nr, kEmodeEnergy, &k, &smem) : false;
+  if (!have) return cudaErrorInvalidValue;
   cudaError_t ce = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (ce != cudaSuccess) return ce;
-  prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(s, e->s.n, e->s.R, e->s.xp, e->v[0][0], nullptr,
-                                                                      e->Kp, kTcBf16, 2);
+  prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(x, e->s.n, e->s.R, e->s.xp, e->v[0][0], nullptr,
+                                                                      e->Kp, e->s.dtype, 2);
   if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
   TcArgs a = e->args;
-  a.x = const_cast<float *>(s);
+  a.x = const_cast<float *>(x);
   a.y = nullptr;
-  a.h = nullptr;
+  a.h = h;
   a.energy = energy;
   a.status = status;
   a.steps = 1;

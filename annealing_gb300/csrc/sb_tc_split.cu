@@ -1,4 +1,5 @@
-// Instantiations of the tcgen05 SB kernel for BF16 hi + lo operands (real couplings: dSB, and bSB with x split too).
+// Instantiations of the tcgen05 SB kernel for BF16 hi + lo operands (real couplings: dSB, and bSB with x split too;
+// the dSB energy mode also ranks bSB replicas: sign operands against the split couplings).
 #include "sb_tc_kernel.cuh"
 
 namespace sbk {
@@ -6,9 +7,9 @@ namespace sbk {
 bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem) {
   if (variant == 2) {
     switch (nr) {
-      case 32: return tck::tc_lookup<kTcBf16Split, 2, 32, 3>(emode, k, smem);
-      case 64: return tck::tc_lookup<kTcBf16Split, 2, 64, 3>(emode, k, smem);
-      case 128: return tck::tc_lookup<kTcBf16Split, 2, 128, 3>(emode, k, smem);
+      case 32: return tck::tc_lookup<kTcBf16Split, 2, 32, 7>(emode, k, smem);
+      case 64: return tck::tc_lookup<kTcBf16Split, 2, 64, 7>(emode, k, smem);
+      case 128: return tck::tc_lookup<kTcBf16Split, 2, 128, 7>(emode, k, smem);
     }
   }
   if (variant == 1) {

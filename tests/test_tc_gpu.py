@@ -106,6 +106,53 @@ def test_real_couplings_split_bf16_vs_fp64(ctx, variant):
     assert res.energy_check_ok
 
 
+@pytest.mark.parametrize("variant,n,R,jmax", [
+    (sb.BSB, 300, 64, 1),
+    (sb.BSB, 257, 96, 300),
+    (sb.DSB, 300, 64, 300),   # |J| > 256: dSB on hi + lo, still exact
+    (sb.DSB, 200, 40, 70000),  # |J| >= 2^16: hi + lo is not exact, the plain FP32 pass takes over
+])
+def test_split_integer_final_energies_exact(ctx, variant, n, R, jmax):
+    """BF16 hi + lo engines with integer couplings: the final energy pass runs on the tensor cores
+    (sign operands against the split couplings, exact while |J| < 2^16) or, past that, on the plain
+    FP32 kernel. Either way every replica's energy equals the oracle's energy of sign(x) exactly;
+    dSB trajectories on exact hi + lo couplings are bit-exact too."""
+    J = instances.erdos_renyi(n, 0.5, seed=n, jmax=jmax, allow_zero=True)
+    h = np.random.default_rng(n).integers(-5, 6, n).astype(np.float32)
+    steps = 20
+    prob, res = solve_tc(ctx, J, h, variant, R, steps, seed=3)
+    assert res.field_dtype == "bf16x2"
+    np.testing.assert_array_equal(res.replica_energies, orc.energies_of_x(J, h, res.final_x))
+    assert res.energy_check_ok
+    if variant == sb.DSB and jmax < 65536:
+        x, y, _ = oracle_dsb(J, h, R, steps, 3, prob.default_c0())
+        np.testing.assert_array_equal(res.final_x, x)
+        np.testing.assert_array_equal(res.final_y, y)
+
+
+@pytest.mark.parametrize("variant", [sb.BSB, sb.DSB])
+def test_split_real_final_energies_ranked_then_refined(ctx, variant):
+    """Real couplings, more replicas than the FP64 refinement takes (8): every replica's reported
+    energy is within 1e-5 (relative) of the FP64 energy of its sign state, and the best replica's is
+    that FP64 energy. A ferromagnetic instance drives most replicas into the same two ground
+    states: replicas outside the refined set tie with the refined ones, and the best must still be
+    a refined one."""
+    n, R = 256, 64
+    a = np.random.default_rng(5).uniform(0.1, 1.0, (n, n)).astype(np.float32)
+    J = np.triu(a, 1)
+    J = J + J.T
+    prob, res = solve_tc(ctx, J, None, variant, R, 300, seed=4)
+    assert res.field_dtype == "bf16x2"
+    spins = np.where(res.final_x > 0, 1, -1).astype(np.int8)
+    e64 = np.array([orc.energy_f64(J, None, s) for s in spins])
+    assert np.all(np.abs(res.replica_energies - e64) <= 1e-5 * np.abs(e64))
+    ties = int(np.sum(e64 == e64.min()))
+    print(f"replicas in a ground state: {ties} of {R}")
+    assert abs(res.best_energy - e64.min()) <= 1e-9 * abs(e64.min())
+    assert abs(res.best_energy - e64[res.best_replica]) <= 1e-9 * abs(e64.min())
+    assert res.energy_check_ok
+
+
 def test_profile_reports_persistent_launch(ctx):
     J = instances.complete_pm1(512, seed=1)
     prob = sb.Problem.from_dense(J)
