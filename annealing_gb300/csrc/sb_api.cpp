@@ -52,6 +52,9 @@ struct sb_plan {
   float *dpump = nullptr;  // [steps] a0 - a(t), the schedule every kernel reads
   float *dxk = nullptr;    // [kTopK][xp] rows of the best candidates (real-valued J)
   double *dek = nullptr;   // [kTopK] their FP64 energies
+  // compact copy of integer couplings for the host re-check, built on a background thread while
+  // the device solves (it reads the caller's problem: reset before that may go away)
+  std::unique_ptr<sbh::CouplingCopies> copies;
   sbk::TcEngine *tc = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -227,7 +230,9 @@ sb_status upload_problem(sb_plan *pl, const sb_problem *p, std::string &err) {
       if (ts != SB_OK) return ts;
     }
   }
+  pl->copies.reset();
   pl->prob = p;
+  if (p->integer_valued) pl->copies.reset(new sbh::CouplingCopies({p}));
   return SB_OK;
 }
 
@@ -578,7 +583,9 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   if (pl->prob) {
     if (pl->integral) {
       int64_t ei = 0;
-      if (sb_energy_i64(pl->prob, spins.data(), &ei) == SB_OK) {
+      const sb_status es = pl->copies ? pl->copies->energy(0, spins.data(), &ei, 0)
+                                      : sb_energy_i64(pl->prob, spins.data(), &ei);
+      if (es == SB_OK) {
         res->best_energy_i64 = ei;
         res->energy_check_ok = ((double)ei == e_final[best]) ? 1 : 0;
       }
@@ -742,6 +749,8 @@ sb_status sb_solve(sb_ctx *ctx, const sb_problem *p, const sb_params *params, sb
     pl->prm.profile = params->profile;
     s = plan_run(pl, params->seed, res, err);
   }
+  // the cached plan outlives this call, the caller's problem need not
+  if (pl && ctx->cached == pl) pl->copies.reset();
   if (s == SB_OK)
     res->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   ctx->last_error = err;

@@ -28,6 +28,9 @@ struct sb_batch {
   sb_params prm{};
   sbk::Grouped *g = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // compact copies of the couplings for the host re-check, built in the background (the first
+  // runs' device time hides them)
+  std::unique_ptr<sbh::CouplingCopies> copies;
 };
 
 namespace {
@@ -205,6 +208,8 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     destroy(b);
     return s;
   }
+  b->copies.reset(new sbh::CouplingCopies(
+      b->probs, (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2))));
   *out = b;
   return SB_OK;
 }
@@ -298,7 +303,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
         const auto &gi = g.insts[k];
         spins[k].resize(gi.n);
         for (int i = 0; i < gi.n; ++i) spins[k][i] = xb[k][i] > 0.0f ? 1 : -1;
-        if (sbh::energy_i64(b->probs[k], spins[k].data(), &e64[k], 1) == SB_OK)
+        if (b->copies->energy(k, spins[k].data(), &e64[k], 1) == SB_OK)
           okv[k] = (double)e64[k] == energies[k][best[k]] ? 1 : 0;
       }
     });

@@ -3,7 +3,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <memory>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "sb.h"
 
@@ -18,6 +22,42 @@ const char *thread_error();
 sb_status energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out, int threads);
 double coupling_std(const sb_problem *p, int threads);
 float default_c0(const sb_problem *p, int threads);
+
+// Exact compact copy of integer couplings for the host int64 energy re-check, which otherwise
+// reads the FP32 matrix: couplings in {-1, 0, +1} as two bit planes (row i, bit j: J_ij != 0,
+// J_ij < 0; N^2 / 4 bytes, row sums by popcount), |J| <= 127 as int8 (N^2 bytes). The energy is
+// the same integer sb_energy_i64 gives.
+struct CouplingCopy {
+  int n = 0;
+  int mode = 0;  // kNone, kBits, kInt8
+  int words = 0;  // 64-bit words per bit-plane row
+  std::vector<uint64_t> nz, neg;
+  std::vector<int32_t> upper;  // bit planes: nonzero couplings right of the diagonal, per row
+  std::vector<int8_t> j8;
+  std::vector<int64_t> h;  // empty: no field
+  static constexpr int kNone = 0, kBits = 1, kInt8 = 2;
+  // false (mode kNone) when a coupling or field is not integral or |J| > 127, or on `cancel`
+  bool build(const sb_problem *p, const std::atomic<bool> *cancel = nullptr);
+  int64_t energy(const int8_t *spins, int threads) const;
+};
+
+// Copies of several problems built on background threads (problem k on thread k % threads, in
+// order), so that a solve's device time hides the build; a problem whose copy is not ready yet is
+// evaluated from its FP32 couplings.
+class CouplingCopies {
+ public:
+  explicit CouplingCopies(std::vector<const sb_problem *> probs, int threads = 1);
+  ~CouplingCopies();  // stops the builder and joins it
+  sb_status energy(size_t k, const int8_t *spins, int64_t *out, int threads) const;
+  bool ready(size_t k) const;
+
+ private:
+  std::vector<const sb_problem *> probs_;
+  std::vector<CouplingCopy> copies_;
+  std::unique_ptr<std::atomic<int>[]> ready_;
+  std::atomic<bool> cancel_{false};
+  std::vector<std::thread> th_;
+};
 }  // namespace sbh
 
 struct NmfaCache;

@@ -216,6 +216,186 @@ sb_status sbh::energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out
   return SB_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Compact coupling copies for the int64 re-check.
+
+bool sbh::CouplingCopy::build(const sb_problem *p, const std::atomic<bool> *cancel) {
+  mode = kNone;
+  nz.clear();
+  neg.clear();
+  upper.clear();
+  j8.clear();
+  h.clear();
+  if (!p || !p->J || p->n <= 0) return false;
+  const int nn = p->n;
+  auto stop = [&] { return cancel && cancel->load(std::memory_order_relaxed); };
+  std::vector<int64_t> hv;
+  if (p->h) {
+    hv.resize((size_t)nn);
+    for (int i = 0; i < nn; ++i) {
+      const float v = p->h[i];
+      if (v != floorf(v) || !(fabsf(v) < 9.0e18f)) return false;
+      hv[(size_t)i] = (int64_t)v;
+    }
+  }
+  // the scan on creation (sb_problem_init / wrap / load / random) vouches for integral couplings
+  // and their largest magnitude, which picks the form
+  if (!p->integer_valued || p->max_abs_j > 127) return false;
+  const int amax = p->max_abs_j;
+  n = nn;
+  if (amax <= 1) {
+    words = (nn + 63) / 64;
+    nz.assign((size_t)nn * words, 0);
+    neg.assign((size_t)nn * words, 0);
+    for (int i = 0; i < nn; ++i) {
+      if ((i & 63) == 0 && stop()) return false;
+      const float *Ji = p->J + (size_t)i * nn;
+      uint64_t *zi = nz.data() + (size_t)i * words, *gi = neg.data() + (size_t)i * words;
+      for (int w = 0; w < words; ++w) {
+        const int j0 = 64 * w, j1 = std::min(nn, j0 + 64);
+        uint64_t z = 0, g = 0;
+        if (j1 - j0 == 64) {
+          // eight bytes of eight bits each
+          for (int q = 0; q < 8; ++q) {
+            const float *v = Ji + j0 + 8 * q;
+            uint32_t zb = 0, gb = 0;
+            for (int b = 0; b < 8; ++b) {
+              zb |= (uint32_t)(v[b] != 0.0f) << b;
+              gb |= (uint32_t)(v[b] < 0.0f) << b;
+            }
+            z |= (uint64_t)zb << (8 * q);
+            g |= (uint64_t)gb << (8 * q);
+          }
+        } else {
+          for (int j = j0; j < j1; ++j) {
+            z |= (uint64_t)(Ji[j] != 0.0f) << (j - j0);
+            g |= (uint64_t)(Ji[j] < 0.0f) << (j - j0);
+          }
+        }
+        zi[w] = z;
+        gi[w] = g;
+      }
+    }
+    upper.assign((size_t)nn, 0);
+    for (int i = 0; i + 1 < nn; ++i) {
+      const uint64_t *zi = nz.data() + (size_t)i * words;
+      const int w0 = (i + 1) >> 6;
+      int32_t c = 0;
+      for (int w = w0; w < words; ++w) c += __builtin_popcountll(zi[w] & (w == w0 ? ~0ull << ((i + 1) & 63) : ~0ull));
+      upper[(size_t)i] = c;
+    }
+    mode = kBits;
+  } else {
+    j8.resize((size_t)nn * nn);
+    for (int i = 0; i < nn; ++i) {
+      if ((i & 63) == 0 && stop()) return false;
+      const float *Ji = p->J + (size_t)i * nn;
+      int8_t *di = j8.data() + (size_t)i * nn;
+      for (int j = 0; j < nn; ++j) di[j] = (int8_t)Ji[j];
+    }
+    mode = kInt8;
+  }
+  h.swap(hv);
+  return true;
+}
+
+int64_t sbh::CouplingCopy::energy(const int8_t *spins, int threads) const {
+  // E = -sum_{i<j} J_ij s_i s_j - sum_i h_i s_i, rows i dealt round-robin to host threads
+  std::vector<uint64_t> sn;
+  if (mode == kBits) {
+    sn.assign((size_t)words, 0);
+    for (int j = 0; j < n; ++j) sn[(size_t)(j >> 6)] |= (uint64_t)(spins[j] < 0) << (j & 63);
+  }
+  auto rows = [&](int i0, int stride) -> int64_t {
+    int64_t e = 0;
+    for (int i = i0; i < n; i += stride) {
+      int64_t row = 0;
+      if (mode == kBits) {
+        // sum_{j>i} J_ij s_j = (nonzero couplings) - 2 (those whose product is -1)
+        const int j0 = i + 1;
+        if (j0 < n) {
+          const uint64_t *zi = nz.data() + (size_t)i * words, *gi = neg.data() + (size_t)i * words;
+          const int w0 = j0 >> 6;
+          int64_t minus = __builtin_popcountll(zi[w0] & (gi[w0] ^ sn[(size_t)w0]) & (~0ull << (j0 & 63)));
+          for (int w = w0 + 1; w < words; ++w) minus += __builtin_popcountll(zi[w] & (gi[w] ^ sn[(size_t)w]));
+          row = (int64_t)upper[(size_t)i] - 2 * minus;
+        }
+      } else {
+        const int8_t *Ji = j8.data() + (size_t)i * n;
+        int32_t acc = 0;  // |acc| <= 127 n
+        for (int j = i + 1; j < n; ++j) acc += (int32_t)Ji[j] * (int32_t)spins[j];
+        row = acc;
+      }
+      e -= row * (int64_t)spins[i];
+      if (!h.empty()) e -= h[(size_t)i] * (int64_t)spins[i];
+    }
+    return e;
+  };
+  const int nt = threads > 0 ? threads : (mode == kInt8 && n >= 4096 ? auto_threads(n, 0) : 1);
+  if (nt <= 1) return rows(0, 1);
+  std::vector<int64_t> part((size_t)nt, 0);
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back([&, t] { part[(size_t)t] = rows(t, nt); });
+  part[0] = rows(0, nt);
+  for (auto &x : th) x.join();
+  int64_t e = 0;
+  for (int64_t v : part) e += v;
+  return e;
+}
+
+sbh::CouplingCopies::CouplingCopies(std::vector<const sb_problem *> probs, int threads)
+    : probs_(std::move(probs)), copies_(probs_.size()), ready_(new std::atomic<int>[probs_.size()]) {
+  for (size_t k = 0; k < probs_.size(); ++k) ready_[k].store(0);
+  const size_t nt = std::max<size_t>(1, std::min<size_t>((size_t)std::max(1, threads), probs_.size()));
+  for (size_t t = 0; t < nt; ++t)
+    th_.emplace_back([this, t, nt] {
+      for (size_t k = t; k < probs_.size() && !cancel_.load(std::memory_order_relaxed); k += nt)
+        if (copies_[k].build(probs_[k], &cancel_)) ready_[k].store(1, std::memory_order_release);
+    });
+}
+
+sbh::CouplingCopies::~CouplingCopies() {
+  cancel_.store(true);
+  for (auto &t : th_)
+    if (t.joinable()) t.join();
+}
+
+bool sbh::CouplingCopies::ready(size_t k) const {
+  return k < probs_.size() && ready_[k].load(std::memory_order_acquire) != 0;
+}
+
+sb_status sbh::CouplingCopies::energy(size_t k, const int8_t *spins, int64_t *out, int threads) const {
+  if (k >= probs_.size() || !spins || !out) return SB_ERR_INVALID_ARG;
+  if (ready(k)) {
+    *out = copies_[k].energy(spins, threads);
+    return SB_OK;
+  }
+  return sbh::energy_i64(probs_[k], spins, out, threads);
+}
+
+extern "C" sb_status sb_energies_i64(const sb_problem *p, const int8_t *spins, int32_t count, int64_t *out) {
+  if (!p || !p->J || p->n <= 0 || !spins || !out || count < 0) return SB_ERR_INVALID_ARG;
+  const size_t n = (size_t)p->n;
+  sbh::CouplingCopy c;
+  if (count < 2 || !c.build(p)) {
+    // one vector, or couplings without a compact copy: the FP32 evaluator per vector
+    for (int32_t v = 0; v < count; ++v) {
+      const sb_status s = sbh::energy_i64(p, spins + (size_t)v * n, out + v, 0);
+      if (s != SB_OK) return s;
+    }
+    return SB_OK;
+  }
+  const int nt = std::max(1, std::min<int>(count, (int)std::min(8u, std::max(1u, std::thread::hardware_concurrency()))));
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t)
+    th.emplace_back([&, t] {
+      for (int32_t v = t; v < count; v += nt) out[v] = c.energy(spins + (size_t)v * n, 1);
+    });
+  for (int32_t v = 0; v < count; v += nt) out[v] = c.energy(spins + (size_t)v * n, 1);
+  for (auto &x : th) x.join();
+  return SB_OK;
+}
+
 extern "C" double sb_energy_f64(const sb_problem *p, const int8_t *spins) {
   if (!p || !p->J || !spins || p->n <= 0) return 0.0;
   const int n = p->n;

@@ -270,6 +270,8 @@ _SIGS = {
     "sb_energy_i64": (C.c_int, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8),
                                 C.POINTER(C.c_int64)]),
     "sb_energy_f64": (C.c_double, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8)]),
+    "sb_energies_i64": (C.c_int, [C.POINTER(ProblemStruct), C.POINTER(C.c_int8), C.c_int32,
+                                  C.POINTER(C.c_int64)]),
     "sb_sqa_params_default": (None, [C.POINTER(SqaParams)]),
     "sb_sqa_schedule": (None, [C.c_int32, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "sb_sqa_solve": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.POINTER(SqaParams),
@@ -410,6 +412,17 @@ class Problem:
                                        C.byref(out)))
             return int(out.value)
         return lib().sb_energy_f64(C.byref(self.s), sp.ctypes.data_as(C.POINTER(C.c_int8)))
+
+    def energies(self, spins: np.ndarray) -> np.ndarray:
+        """Exact int64 energies of several spin vectors (rows of `spins`, int8 +-1); couplings
+        in {-1, 0, +1} or |J| <= 127 are read from a compact copy (sb_energies_i64)."""
+        sp = np.ascontiguousarray(np.atleast_2d(spins), dtype=np.int8)
+        if sp.shape[1] != self.n:
+            raise ValueError("spins must have n columns")
+        out = np.zeros(sp.shape[0], np.int64)
+        _check(lib().sb_energies_i64(C.byref(self.s), sp.ctypes.data_as(C.POINTER(C.c_int8)), sp.shape[0],
+                                     out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
 
     def close(self) -> None:
         if self.s.J:

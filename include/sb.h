@@ -221,6 +221,10 @@ float sb_pump(float a0, int32_t t, int32_t steps);
 /* exact energies: int64 when every J, h is integral (else SB_ERR_UNSUPPORTED), double otherwise */
 sb_status sb_energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out);
 double sb_energy_f64(const sb_problem *p, const int8_t *spins);
+/* the int64 energies of `count` spin vectors (count x n int8, row after row) into out[count]; for
+ * couplings in {-1, 0, +1} or |J| <= 127 the matrix is first copied into bit planes / int8, so each
+ * vector reads 16x / 4x fewer bytes than sb_energy_i64 does; the same integers either way */
+sb_status sb_energies_i64(const sb_problem *p, const int8_t *spins, int32_t count, int64_t *out);
 
 /* ---- time to target (host only, no GPU needed) ----
  * Replaces the reference's trace analysis: per trial, the first time its energy trace goes below

@@ -93,6 +93,41 @@ def test_exact_energy_paths():
     assert lib().sb_energy_i64(C.byref(p.s), s.ctypes.data_as(C.POINTER(C.c_int8)), C.byref(out)) == 6
 
 
+@pytest.mark.parametrize("n,jmax,density,with_h", [
+    (1, 1, 1.0, False),
+    (63, 1, 1.0, True),      # one bit-plane word per row, a partial one
+    (64, 1, 0.5, False),     # exactly one word
+    (200, 1, 0.3, True),     # bit planes, zero couplings, a field
+    (1030, 1, 1.0, False),   # many words, ragged tail
+    (300, 7, 0.6, True),     # int8 copy
+    (700, 127, 1.0, False),  # int8 copy at its largest magnitude
+    (150, 300, 0.5, False),  # |J| > 127: no copy, the FP32 evaluator
+])
+def test_batched_exact_energies(n, jmax, density, with_h):
+    """sb_energies_i64 (bit planes for J in {-1, 0, 1}, int8 for |J| <= 127, else the FP32
+    evaluator) gives the oracle's int64 energy for every vector, including all-up and all-down."""
+    rng = np.random.default_rng(n + jmax)
+    J = instances.erdos_renyi(n, density, n + 1, jmax=jmax, allow_zero=True) if n > 1 else np.zeros((1, 1), np.float32)
+    h = rng.integers(-9, 10, n).astype(np.float32) if with_h else None
+    p = sb.Problem.from_dense(J, h)
+    S = (rng.integers(0, 2, (6, n)) * 2 - 1).astype(np.int8)
+    S[0] = 1
+    S[1] = -1
+    got = p.energies(S)
+    assert [int(v) for v in got] == [orc.energy_i64(J, h, s) for s in S]
+    assert int(p.energies(S[2])[0]) == orc.energy_i64(J, h, S[2])
+
+
+def test_batched_exact_energies_refuses_real_couplings():
+    Jg, hg = instances.gaussian(40, 5)
+    p = sb.Problem.from_dense(Jg, hg)
+    S = np.ones((3, 40), np.int8)
+    out = np.zeros(3, np.int64)
+    rc = lib().sb_energies_i64(C.byref(p.s), S.ctypes.data_as(C.POINTER(C.c_int8)), 3,
+                               out.ctypes.data_as(C.POINTER(C.c_int64)))
+    assert rc == 6  # SB_ERR_UNSUPPORTED
+
+
 def test_graph_reader_reference_format(tmp_path):
     J = instances.erdos_renyi(60, 0.3, 2, jmax=3)
     path = str(tmp_path / "g.txt")
