@@ -109,53 +109,99 @@ uint8_t fp8_code(int v) {
   return (uint8_t)(sign | ((e + 7) << 3) | m);
 }
 
-void pack_fp8(const float *J, int n, uint8_t *dst, int Np, int Kp) {
+// Off-diagonal sums of J and J^2 over integer couplings, gathered while packing: the coupling
+// statistics behind the default c0 (sbh::c0_from_sums gives the value sb_default_c0 computes).
+struct CouplingSums {
+  int64_t s = 0, s2 = 0;
+};
+
+// Rows [0, Np) of J packed by `nt` threads, `row(i, d, sum, sum2)` writing row i < n into d.
+template <typename RowFn>
+CouplingSums pack_rows(int n, uint8_t *dst, int Np, int row_bytes, int64_t elems_per_thread, RowFn row) {
+  const unsigned want = (unsigned)std::max<int64_t>(1, (int64_t)Np * row_bytes / elems_per_thread);
+  const unsigned nt = std::max(1u, std::min({std::thread::hardware_concurrency() / 2, want, 16u}));
+  const int rows_per = (Np + (int)nt - 1) / (int)nt;
+  std::vector<CouplingSums> part(nt);
+  auto work = [&, rows_per](unsigned w) {
+    const int r0 = (int)w * rows_per, r1 = std::min(Np, r0 + rows_per);
+    int64_t a = 0, a2 = 0;
+    for (int i = r0; i < r1; ++i) {
+      uint8_t *d = dst + (size_t)i * row_bytes;
+      if (i >= n) {
+        memset(d, 0, row_bytes);
+        continue;
+      }
+      int32_t rs = 0, rs2 = 0;  // |J| <= 16: at most 256 n per row
+      row(i, d, rs, rs2);
+      a += rs;
+      a2 += rs2;
+    }
+    part[w].s = a;
+    part[w].s2 = a2;
+  };
+  std::vector<std::thread> th;
+  for (unsigned w = 1; w < nt; ++w) th.emplace_back(work, w);
+  work(0);
+  for (auto &t : th) t.join();
+  CouplingSums out;
+  for (const auto &c : part) {
+    out.s += c.s;
+    out.s2 += c.s2;
+  }
+  return out;
+}
+
+// Couplings as FP8 E4M3 (integers |J| <= 16; fp8_code), rows of Kp bytes, zero padded.
+CouplingSums pack_fp8(const float *J, int n, uint8_t *dst, int Np, int Kp) {
   uint8_t lut[33];
   for (int v = -16; v <= 16; ++v) lut[v + 16] = fp8_code(v);
   // about 2 M elements per thread; several admissions pack at once
-  const unsigned want = (unsigned)std::max<int64_t>(1, (int64_t)Np * Kp / (2 << 20));
-  const unsigned nt = std::max(1u, std::min({std::thread::hardware_concurrency() / 2, want, 16u}));
-  const int rows_per = (Np + (int)nt - 1) / (int)nt;
-  std::vector<std::thread> th;
-  for (unsigned w = 0; w < nt; ++w)
-    th.emplace_back([=, &lut] {
-      const int r0 = (int)w * rows_per, r1 = std::min(Np, r0 + rows_per);
-      for (int i = r0; i < r1; ++i) {
-        uint8_t *d = dst + (size_t)i * Kp;
-        if (i >= n) {
-          memset(d, 0, Kp);
-          continue;
-        }
-        const float *Ji = J + (size_t)i * n;
-        for (int j = 0; j < n; ++j) d[j] = lut[(int)Ji[j] + 16];
-        memset(d + n, 0, Kp - n);
-      }
-    });
-  for (auto &t : th) t.join();
+  return pack_rows(n, dst, Np, Kp, 2 << 20, [&](int i, uint8_t *d, int32_t &rs, int32_t &rs2) {
+    const float *Ji = J + (size_t)i * n;
+    for (int j = 0; j < n; ++j) {
+      const int v = (int)Ji[j];
+      d[j] = lut[v + 16];
+      rs += v;
+      rs2 += v * v;
+    }
+    const int dg = (int)Ji[i];  // the diagonal does not count
+    rs -= dg;
+    rs2 -= dg * dg;
+    memset(d + n, 0, Kp - n);
+  });
 }
 
-// Couplings as packed E2M1 (integers |J| <= 4; e2m1_code), rows of kb bytes, zero padded.
-void pack_fp4(const float *J, int n, uint8_t *dst, int Np, int kb) {
-  uint8_t lut[9];
-  for (int v = -4; v <= 4; ++v) lut[v + 4] = (uint8_t)(e2m1_code((float)v) & 0xF);
-  const unsigned want = (unsigned)std::max<int64_t>(1, (int64_t)Np * kb / (1 << 20));
-  const unsigned nt = std::max(1u, std::min({std::thread::hardware_concurrency() / 2, want, 16u}));
-  const int rows_per = (Np + (int)nt - 1) / (int)nt;
-  std::vector<std::thread> th;
-  for (unsigned w = 0; w < nt; ++w)
-    th.emplace_back([=, &lut] {
-      const int r0 = (int)w * rows_per, r1 = std::min(Np, r0 + rows_per);
-      for (int i = r0; i < r1; ++i) {
-        uint8_t *d = dst + (size_t)i * kb;
-        memset(d, 0, kb);
-        if (i >= n) continue;
-        const float *Ji = J + (size_t)i * n;
-        for (int j = 0; j + 1 < n; j += 2)
-          d[j >> 1] = (uint8_t)(lut[(int)Ji[j] + 4] | (lut[(int)Ji[j + 1] + 4] << 4));
-        if (n & 1) d[n >> 1] = lut[(int)Ji[n - 1] + 4];
-      }
-    });
-  for (auto &t : th) t.join();
+// Couplings as packed E2M1 (integers |J| <= 4), rows of kb bytes, zero padded. The code of v is
+// |v| + min(|v|, 2) with the sign in bit 3 (0, 1, 2, 3, 4 -> 0x0, 0x2, 0x4, 0x5, 0x6: e2m1_code),
+// computed rather than looked up so that the loop vectorises.
+CouplingSums pack_fp4(const float *J, int n, uint8_t *dst, int Np, int kb) {
+  return pack_rows(n, dst, Np, kb, 1 << 20, [&](int i, uint8_t *d, int32_t &rs, int32_t &rs2) {
+    const float *Ji = J + (size_t)i * n;
+    auto code = [](int v) {
+      const int a = v < 0 ? -v : v;
+      return (a + (a < 2 ? a : 2)) | (v < 0 ? 8 : 0);
+    };
+    const int pairs = n >> 1;
+    int32_t s1 = 0, s2 = 0;
+    for (int b = 0; b < pairs; ++b) {
+      const int v0 = (int)Ji[2 * b], v1 = (int)Ji[2 * b + 1];
+      d[b] = (uint8_t)(code(v0) | (code(v1) << 4));
+      s1 += v0 + v1;
+      s2 += v0 * v0 + v1 * v1;
+    }
+    int used = pairs;
+    if (n & 1) {
+      const int v = (int)Ji[n - 1];
+      d[pairs] = (uint8_t)code(v);
+      s1 += v;
+      s2 += v * v;
+      used = pairs + 1;
+    }
+    memset(d + used, 0, kb - used);
+    const int dg = (int)Ji[i];  // the diagonal does not count
+    rs = s1 - dg;
+    rs2 = s2 - dg * dg;
+  });
 }
 
 int device_sms() {
@@ -235,7 +281,7 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   g.kbytes = fp4 ? g.Kp / 2 : g.Kp;
   g.Rp = (g.R + nr - 1) / nr * nr;
   g.xp = (g.n + 3) / 4 * 4;
-  g.c0 = prm->c0 > 0.0f ? prm->c0 : sbh::default_c0(p, 1);  // prepared one instance per thread
+  g.c0 = prm->c0;  // or, when unset, the default from the coupling sums the packing gathers
   g.dt = prm->dt;
   g.dta0 = prm->dt * prm->a0;
   cudaError_t e;
@@ -270,10 +316,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     if ((e = cudaMallocHost(&stg.pin, ab)) != cudaSuccess) return fail("cudaMallocHost(staging)");
     stg.bytes = ab;
   }
-  if (fp4)
-    pack_fp4(p->J, g.n, stg.pin, g.Np, g.kbytes);
-  else
-    pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
+  const CouplingSums sums =
+      fp4 ? pack_fp4(p->J, g.n, stg.pin, g.Np, g.kbytes) : pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
+  if (!(g.c0 > 0.0f)) g.c0 = sbh::c0_from_sums(g.n, sums.s, sums.s2);
   if ((e = cudaMemcpyAsync(g.a, stg.pin, ab, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
   std::vector<float> pumps((size_t)(g.steps > 0 ? g.steps : 1), 0.0f);
   for (int t = 0; t < g.steps; ++t) pumps[t] = sb_pump(prm->a0, t, g.steps);

@@ -22,6 +22,9 @@ const char *thread_error();
 sb_status energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out, int threads);
 double coupling_std(const sb_problem *p, int threads);
 float default_c0(const sb_problem *p, int threads);
+// The default c0 from the off-diagonal sums of J and J^2 (exact integers below 2^53): the value
+// default_c0 computes for those couplings.
+float c0_from_sums(int n, int64_t s, int64_t s2);
 
 // Exact compact copy of integer couplings for the host int64 energy re-check, which otherwise
 // reads the FP32 matrix: couplings in {-1, 0, +1} as two bit planes (row i, bit j: J_ij != 0,

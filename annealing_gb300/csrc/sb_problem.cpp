@@ -88,6 +88,19 @@ float sbh::default_c0(const sb_problem *p, int threads) {
   return (float)(0.5 / (sqrt((double)(p ? p->n : 1)) * sd));
 }
 
+static double std_from_sums(int n, double s, double s2) {
+  const double cnt = (double)n * (double)(n - 1);
+  const double mean = s / cnt;
+  const double var = s2 / cnt - mean * mean;
+  return var > 0.0 ? sqrt(var) : 0.0;
+}
+
+float sbh::c0_from_sums(int n, int64_t s, int64_t s2) {
+  double sd = n >= 2 ? std_from_sums(n, (double)s, (double)s2) : 0.0;
+  if (!(sd > 0.0)) sd = 1.0;
+  return (float)(0.5 / (sqrt((double)n) * sd));
+}
+
 double sbh::coupling_std(const sb_problem *p, int threads) {
   if (!p || !p->J || p->n < 2) return 0.0;
   const int n = p->n;
@@ -141,10 +154,7 @@ double sbh::coupling_std(const sb_problem *p, int threads) {
       }
     }
   }
-  double cnt = (double)n * (double)(n - 1);
-  double mean = s / cnt;
-  double var = s2 / cnt - mean * mean;
-  return var > 0.0 ? sqrt(var) : 0.0;
+  return std_from_sums(n, s, s2);
 }
 
 extern "C" {
