@@ -104,6 +104,8 @@ float sbh::c0_from_sums(int n, int64_t s, int64_t s2) {
 double sbh::coupling_std(const sb_problem *p, int threads) {
   if (!p || !p->J || p->n < 2) return 0.0;
   const int n = p->n;
+  // the scan's exact sums: the same doubles the integer pass below would produce
+  if (p->stats_valid && p->integer_valued) return std_from_sums(n, (double)p->sum_j, (double)p->sum_j2);
   double s = 0.0, s2 = 0.0;
   const double maxj = (double)p->max_abs_j;
   if (p->integer_valued && p->max_abs_j < 2000000000 && (double)n * n * maxj * maxj < 9.0e15) {
@@ -440,20 +442,28 @@ void sbh::problem_scan(sb_problem *p) {
   std::vector<int> nonint((size_t)nt, 0);
   std::vector<float> mx((size_t)nt, 0.0f);
   std::vector<int64_t> ed((size_t)nt, 0);
+  std::vector<double> sj((size_t)nt, 0.0), sj2((size_t)nt, 0.0);
   auto rows = [&](int t) {
     int bad = 0;
     float m = 0.0f;
     int64_t e = 0;
+    double a1 = 0.0, a2 = 0.0;
     for (int i = t; i < n; i += nt) {
       const float *Ji = p->J + (size_t)i * n;
       int rb = 0;
       float rm = 0.0f;
+      double r1 = 0.0, r2 = 0.0;  // exact for the integer couplings they are kept for
       for (int j = 0; j < n; ++j) {
         const float w = Ji[j];
         rb |= (w != floorf(w)) ? 1 : 0;  // NaN is not integral
         const float a = fabsf(w);
         rm = a > rm ? a : rm;
+        r1 += (double)w;
+        r2 += (double)w * (double)w;
       }
+      const double dg = (double)Ji[i];  // the diagonal does not count
+      a1 += r1 - dg;
+      a2 += r2 - dg * dg;
       int64_t re = 0;
       for (int j = i + 1; j < n; ++j) re += Ji[j] != 0.0f ? 1 : 0;
       bad |= rb;
@@ -463,6 +473,8 @@ void sbh::problem_scan(sb_problem *p) {
     nonint[t] = bad;
     mx[t] = m;
     ed[t] = e;
+    sj[t] = a1;
+    sj2[t] = a2;
   };
   if (nt == 1) {
     rows(0);
@@ -473,12 +485,14 @@ void sbh::problem_scan(sb_problem *p) {
     for (auto &x : th) x.join();
   }
   bool integral = true;
-  double maxabs = 0.0;
+  double maxabs = 0.0, s1 = 0.0, s2 = 0.0;
   int64_t edges = 0;
   for (int t = 0; t < nt; ++t) {
     integral = integral && !nonint[t];
     maxabs = (double)mx[t] > maxabs ? (double)mx[t] : maxabs;
     edges += ed[t];
+    s1 += sj[t];
+    s2 += sj2[t];
   }
   if (p->h)
     for (int i = 0; i < n; ++i)
@@ -486,6 +500,12 @@ void sbh::problem_scan(sb_problem *p) {
   p->integer_valued = integral ? 1 : 0;
   p->max_abs_j = (int32_t)ceil(maxabs > 2e9 ? 2e9 : maxabs);
   p->n_edges = edges;
+  // integer couplings whose sums stay below 2^53 (every partial sum above is then exact): the
+  // coupling statistics of the default c0, kept so that no solve reads J again for them
+  const bool exact = integral && (double)n * n * maxabs * maxabs < 9.0e15;
+  p->stats_valid = exact ? 1 : 0;
+  p->sum_j = exact ? (int64_t)s1 : 0;
+  p->sum_j2 = exact ? (int64_t)s2 : 0;
 }
 
 extern "C" sb_status sb_problem_init(sb_problem *p, int32_t n, const float *J, const float *h) {

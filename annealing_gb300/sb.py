@@ -41,6 +41,9 @@ class ProblemStruct(C.Structure):
         ("max_abs_j", C.c_int32),
         ("n_edges", C.c_int64),
         ("lib_owned", C.c_int32),
+        ("stats_valid", C.c_int32),
+        ("sum_j", C.c_int64),
+        ("sum_j2", C.c_int64),
     ]
 
 

@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define SB_ABI_VERSION 2
+#define SB_ABI_VERSION 3  /* 3: sb_problem gained stats_valid / sum_j / sum_j2 */
 
 typedef enum sb_status {
   SB_OK = 0,
@@ -128,6 +128,11 @@ typedef struct sb_problem {
   int32_t max_abs_j;       /* max |J_ij| rounded up (valid when integer_valued) */
   int64_t n_edges;         /* number of nonzero J_ij with i < j */
   int32_t lib_owned;       /* 1 when J/h were allocated by sb_load_graph (free with sb_problem_free) */
+  int32_t stats_valid;     /* 1 when sum_j / sum_j2 hold the exact off-diagonal sums (set by the scan
+                              of sb_problem_init / wrap / load / random, for integer couplings whose
+                              sums stay below 2^53): the default c0 then needs no pass over J */
+  int64_t sum_j;           /* sum of J_ij over i != j */
+  int64_t sum_j2;          /* sum of J_ij^2 over i != j */
 } sb_problem;
 
 typedef struct sb_params {

@@ -31,7 +31,7 @@ def test_every_declared_symbol_is_exported():
 
 
 def test_abi_version_and_status_strings():
-    assert lib().sb_abi_version() == 2
+    assert lib().sb_abi_version() == 3
     assert lib().sb_status_string(0) == b"ok"
     assert lib().sb_status_string(3) == b"parse error"
 
@@ -138,6 +138,25 @@ def test_graph_reader_reference_format(tmp_path):
     assert np.array_equal(p.J, Jr) and np.array_equal(p.J, J)
     assert p.h is None and p.integer_valued
     assert p.s.n_edges == int(np.count_nonzero(np.triu(J, 1)))
+    off = J.astype(np.float64) - np.diag(np.diag(J))
+    assert p.s.stats_valid == 1
+    assert p.s.sum_j == int(off.sum()) and p.s.sum_j2 == int((off * off).sum())
+
+
+@pytest.mark.parametrize("n,jmax,with_h", [(2, 1, False), (300, 1, False), (1100, 7, True), (513, 300, True)])
+def test_default_c0_from_scan_sums(n, jmax, with_h):
+    """The default c0 from the scan's exact coupling sums equals the one computed by a pass over J
+    (the same float, bit for bit); real couplings carry no sums."""
+    J = instances.erdos_renyi(n, 0.6, n, jmax=jmax, allow_zero=True)
+    h = np.random.default_rng(n).integers(-4, 5, n).astype(np.float32) if with_h else None
+    p = sb.Problem.from_dense(J, h)
+    assert p.s.stats_valid == 1
+    fast = p.default_c0()
+    p.s.stats_valid = 0
+    slow = p.default_c0()
+    assert np.float32(fast).tobytes() == np.float32(slow).tobytes()
+    Jg, _ = instances.gaussian(50, 2)
+    assert sb.Problem.from_dense(Jg).s.stats_valid == 0
 
 
 def test_graph_reader_fields_realweights_onebased(tmp_path):
