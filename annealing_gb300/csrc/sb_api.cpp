@@ -8,6 +8,7 @@
 // The step loop is captured once per plan into a CUDA graph and replayed.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -50,6 +51,9 @@ struct sb_plan {
   double *denergy = nullptr;
   uint32_t *dstatus = nullptr;
   float *dpump = nullptr;  // [steps] a0 - a(t), the schedule every kernel reads
+  // plain FP32 dSB that fits one cooperative launch: the sign words of PlainPersist
+  unsigned long long *dwords = nullptr;
+  size_t words_bytes = 0;
   float *dxk = nullptr;    // [kTopK][xp] rows of the best candidates (real-valued J)
   double *dek = nullptr;   // [kTopK] their FP64 energies
   // compact copy of integer couplings for the host re-check, built on a background thread while
@@ -195,6 +199,8 @@ void plan_free_device(sb_plan *pl) {
   cudaFree(pl->dpump);
   cudaFree(pl->dxk);
   cudaFree(pl->dek);
+  cudaFree(pl->dwords);
+  pl->dwords = nullptr;
   pl->dpump = nullptr;
   pl->dxk = nullptr;
   pl->dek = nullptr;
@@ -284,6 +290,16 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->denergy, energy_slots(*prm) * (size_t)pl->R * sizeof(double));
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
   PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
+  // plain FP32 dSB whose rows fit one co-resident grid runs every step in one launch, unless
+  // SB_PLAIN_PERSIST=0 keeps the one-launch-per-step kernel
+  if (mode == SB_FIELD_FP32 && prm->variant == SB_DSB && !needs_trace(*prm) && prm->steps > 0) {
+    const char *env = getenv("SB_PLAIN_PERSIST");
+    const int ctas = (env && env[0] == '0') ? 0 : sbk::plain_persist_ctas(pl->n, pl->R, pl->jp);
+    if (ctas > 0) {
+      pl->words_bytes = (size_t)2 * ctas * 128;  // one 128-byte line per CTA's word
+      PLAN_ALLOC(pl->dwords, pl->words_bytes);
+    }
+  }
 #undef PLAN_ALLOC
   {
     std::vector<float> pumps((size_t)(prm->steps > 0 ? prm->steps : 1), 0.0f);
@@ -348,6 +364,37 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
       cudaError_t e = sbk::tc_run(pl->tc, p.steps, pl->dpump, pl->dx[0], pl->dy, pl->dh, pl->c0, p.dt,
                                   pl->dta0, tr ? pl->denergy : nullptr, pl->dstatus, st);
       if (e != cudaSuccess) return e;
+      if (evs) cudaEventRecord((*evs)[1], st);
+      nl = 1;
+    }
+    if (launches) *launches = nl;
+    return cudaSuccess;
+  }
+  if (pl->dwords) {
+    // plain FP32 dSB in one cooperative launch (same fields and updates as the per-step kernel)
+    if (p.steps > 0) {
+      cudaError_t e = cudaMemsetAsync(pl->dwords, 0, pl->words_bytes, st);
+      if (e != cudaSuccess) return e;
+      sbk::PlainPersist a;
+      memset(&a, 0, sizeof(a));
+      a.n = pl->n;
+      a.R = R;
+      a.jp = pl->jp;
+      a.xp = pl->xp;
+      a.J = pl->dJ;
+      a.h = pl->dh;
+      a.x_in = pl->dx[0];
+      a.x_out = pl->dx[p.steps & 1];
+      a.y = pl->dy;
+      a.pumps = pl->dpump;
+      a.c0 = pl->c0;
+      a.dt = p.dt;
+      a.dta0 = pl->dta0;
+      a.steps = p.steps;
+      a.words = pl->dwords;
+      a.status = pl->dstatus;
+      if (evs) cudaEventRecord((*evs)[0], st);
+      if ((e = sbk::launch_plain_persist(a, st)) != cudaSuccess) return e;
       if (evs) cudaEventRecord((*evs)[1], st);
       nl = 1;
     }
@@ -442,7 +489,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   }
   double kernel_ms = 0.0;
   if (p.profile) {
-    const int nmeas = pl->mode == SB_FIELD_TC ? (p.steps > 0 ? 1 : 0) : p.steps;
+    const int nmeas = (pl->mode == SB_FIELD_TC || pl->dwords) ? (p.steps > 0 ? 1 : 0) : p.steps;
     std::vector<cudaEvent_t> evs((size_t)2 * (nmeas > 0 ? nmeas : 1));
     for (auto &ev : evs) SB_CUDA(cudaEventCreate(&ev));
     int64_t nl = 0;
@@ -460,7 +507,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
     }
     if (nmeas > 0) kernel_ms /= nmeas;
     launches += nl;
-  } else if (p.steps > 0 && pl->mode == SB_FIELD_TC) {
+  } else if (p.steps > 0 && (pl->mode == SB_FIELD_TC || pl->dwords)) {
     int64_t nl = 0;
     SB_CUDA(enqueue_loop(pl, st, nullptr, &nl));
     launches += nl;
@@ -596,7 +643,7 @@ sb_status plan_run(sb_plan *pl, uint64_t seed, sb_result *res, std::string &err)
   }
   res->device_ms = dev_ms;
   res->kernel_ms_avg = kernel_ms;
-  res->steps_per_launch = pl->mode == SB_FIELD_TC ? p.steps : 1;
+  res->steps_per_launch = (pl->mode == SB_FIELD_TC || pl->dwords) ? p.steps : 1;
   res->kernel_launches = launches;
   res->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   res->spin_updates_per_s =

@@ -47,6 +47,29 @@ struct PlainStep {
   int stages;              // set by launch_plain_step
 };
 
+// Plain FP32 dSB, the whole solve in one cooperative launch (sb_plain.cu): CTA (c, r) keeps rows
+// [16 c, 16 c + 16) of J in registers (one row per warp; a lane holds the float4 groups g = lane +
+// 32 k, which is the per-step kernel's summation order) and replica r's x, y of those rows; a step
+// exchanges only the signs: CTA (c, r) publishes one word (step tag << 32 | 16 sign bits) in
+// words[parity][r][c] and reads the G words of its replica. Eligible when jp <= kPersistMaxJp and
+// G R CTAs (G = ceil(n / 16)) are co-resident.
+struct PlainPersist {
+  int n, R, jp, xp;
+  const float *J, *h;         // J [n][jp], h [n] or null
+  const float *x_in;          // x(0) [R][xp]
+  float *x_out, *y;           // x(steps) (may alias x_in), y in place
+  const float *pumps;         // [steps] a0 - a(t)
+  float c0, dt, dta0;
+  int steps;
+  unsigned long long *words;  // [2][R][G] words, one per 128-byte line (16 x 8 bytes), zero on entry
+  uint32_t *status;
+};
+constexpr int kPersistRows = 16;
+constexpr int kPersistMaxJp = 2048;
+// Number of CTAs (G R) of the persistent launch, or 0 when this shape does not qualify.
+int plain_persist_ctas(int n, int R, int jp);
+cudaError_t launch_plain_persist(const PlainPersist &a, cudaStream_t st);
+
 struct PlainEnergy {
   int n, R, jp, xp, rb;
   const float *J, *h;

@@ -569,6 +569,128 @@ int grid_for(size_t total) {
   return (int)(g > 0 ? g : 1);
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Plain FP32 dSB, the whole solve in one cooperative launch (PlainPersist). Warp w of CTA (c, r)
+// owns row i = 16 c + w of replica r: its J row sits in the lanes' registers (lane L: float4 groups
+// g = L + 32 k, k < kPersistGroups, the order dot_chunk sums in), its x, y in registers too. A
+// step needs sign(x(t)) of every spin; CTA c's 16 signs travel in one 64-bit word
+// (tag t + 1 << 32 | bit w = x_i <= 0) at words[t & 1][r][c]: the tag is the flag, so one L2 round
+// trip per step moves all the data. A CTA rewrites parity t & 1 with step t + 2 only after every
+// CTA has published step t + 1, which each did after reading all of step t's words.
+constexpr int kPersistThreads = 32 * kPersistRows;
+constexpr int kPersistGroups = kPersistMaxJp / 128;  // float4 groups per lane
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(PlainPersist a) {
+  __shared__ uint32_t sbits[kPersistMaxJp / kPersistRows];  // the G words' sign bits of this step
+  __shared__ uint32_t sout[kPersistRows];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c = blockIdx.x, r = blockIdx.y, G = gridDim.x;
+  const int row = c * kPersistRows + warp;
+  const bool have = row < a.n;
+  const int ng = a.jp >> 2;  // float4 groups of a row
+  if (G * kPersistRows < a.n || G > kPersistMaxJp / kPersistRows || ng > kPersistGroups * 32 || ng > 4 * G ||
+      r >= a.R) {
+    if (tid == 0) atomicOr(a.status, kErrBadShape);
+    return;
+  }
+  float4 jr[kPersistGroups];
+#pragma unroll
+  for (int k = 0; k < kPersistGroups; ++k) {
+    const int g = lane + 32 * k;
+    jr[k] = (have && g < ng && SB_BOUNDS((size_t)row * a.jp + 4 * g + 4 <= (size_t)a.n * a.jp, a.status))
+                ? reinterpret_cast<const float4 *>(a.J + (size_t)row * a.jp)[g]
+                : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const size_t k_xy = (size_t)r * a.xp + row;
+  float x = 0.0f, y = 0.0f;
+  if (have && SB_BOUNDS(k_xy < (size_t)a.R * a.xp, a.status)) {
+    x = a.x_in[k_xy];
+    y = a.y[k_xy];
+  }
+  const float hv = (have && a.h) ? a.h[row] : 0.0f;
+  // one 128-byte line per word: a CTA's store and the other CTAs' polls of it share no line with
+  // any other CTA's word
+  constexpr int kLine = 16;                                       // words per line
+  unsigned long long *wr = a.words + (size_t)r * G * kLine;      // parity 0 of replica r
+  const size_t par = (size_t)a.R * G * kLine;                     // parity stride
+  // rows past n publish sign -1 (x = 0), as the per-step kernel reads padding spins
+  auto publish = [&](int t) {  // sign(x(t)) with tag t + 1
+    if (lane == 0) sout[warp] = (!have || !(x > 0.0f)) ? 1u : 0u;  // sgn: x > 0 -> +1, else -1
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t b = 0;
+      for (int w = 0; w < kPersistRows; ++w) b |= sout[w] << w;
+      st_relaxed_u64(wr + (size_t)(t & 1) * par + (size_t)c * kLine,
+                     ((unsigned long long)(uint32_t)(t + 1) << 32) | b);
+    }
+  };
+  publish(0);
+  bool ok = true;
+  float pump_next = a.steps > 0 ? a.pumps[0] : 0.0f;
+  for (int t = 0; t < a.steps && ok; ++t) {
+    const float pump = pump_next;
+    if (t + 1 < a.steps) pump_next = a.pumps[t + 1];  // off the step's critical path
+    // gather sign(x(t)): thread q < G waits for CTA q's word of step t
+    bool mine = true;
+    if (tid < G) {
+      const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
+      unsigned long long v = ld_relaxed_u64(src);
+      if ((uint32_t)(v >> 32) != (uint32_t)(t + 1)) {
+        const long long t0 = clock64();
+        int spins = 0;
+        do {
+          if (++spins > 8) __nanosleep(32);
+          v = ld_relaxed_u64(src);
+          if (clock64() - t0 > ptx::kWaitCycles) {
+            mine = false;
+            break;
+          }
+        } while ((uint32_t)(v >> 32) != (uint32_t)(t + 1));
+      }
+      sbits[tid] = (uint32_t)v & 0xFFFFu;
+    }
+    ok = __syncthreads_and(mine ? 1 : 0) != 0;
+    if (!ok) break;
+    // field of this warp's row: groups g = lane + 32 k, spins 4 g .. 4 g + 3 = bits 4 (g % 4) ..
+    // of CTA g / 4's word; sign -1 where the bit is set
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kPersistGroups; ++k) {
+      const int g = lane + 32 * k;
+      if (g < ng) {
+        const uint32_t nib = sbits[g >> 2] >> (4 * (g & 3));
+        const float4 jv = jr[k];
+        acc = __fmaf_rn(jv.x, (nib & 1u) ? -1.0f : 1.0f, acc);
+        acc = __fmaf_rn(jv.y, (nib & 2u) ? -1.0f : 1.0f, acc);
+        acc = __fmaf_rn(jv.z, (nib & 4u) ? -1.0f : 1.0f, acc);
+        acc = __fmaf_rn(jv.w, (nib & 8u) ? -1.0f : 1.0f, acc);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (have) sb_update(acc, hv, pump, a.c0, a.dt, a.dta0, x, y);
+    publish(t + 1);  // its barrier also ends this step's reads of sbits
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
+    return;
+  }
+  if (have && lane == 0 && SB_BOUNDS(k_xy < (size_t)a.R * a.xp, a.status)) {
+    a.x_out[k_xy] = x;
+    a.y[k_xy] = y;
+  }
+}
+
 }  // namespace
 
 template <typename K>
@@ -645,6 +767,35 @@ cudaError_t launch_plain_step(const PlainStep &a0, cudaStream_t st) {
     default:
       return cudaErrorInvalidValue;
   }
+}
+
+int plain_persist_ctas(int n, int R, int jp) {
+  if (n < 1 || R < 1 || jp < 4 || jp % 4 || jp > kPersistMaxJp) return 0;
+  const int G = (n + kPersistRows - 1) / kPersistRows;
+  if (jp / 4 > 4 * G) return 0;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plain_persist_kernel, kPersistThreads, 0) !=
+          cudaSuccess)
+    return 0;
+  const long long ctas = (long long)G * R;
+  return ctas <= (long long)sms * per_sm ? (int)ctas : 0;
+}
+
+cudaError_t launch_plain_persist(const PlainPersist &a, cudaStream_t st) {
+  if (plain_persist_ctas(a.n, a.R, a.jp) == 0 || a.xp < a.jp || a.steps < 0) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)((a.n + kPersistRows - 1) / kPersistRows), (unsigned)a.R);
+  cfg.blockDim = dim3(kPersistThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // every CTA waits on every other one's words
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, plain_persist_kernel, a);
 }
 
 cudaError_t launch_plain_energy(const PlainEnergy &a0, bool fp64, cudaStream_t st) {

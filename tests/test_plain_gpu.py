@@ -1,4 +1,5 @@
-"""Plain fused FP32 kernel (one launch per step) against the CPU oracle, through the C ABI."""
+"""Plain FP32 kernels (one launch per step, and the one-launch dSB form) against the CPU oracle,
+through the C ABI."""
 import os
 import subprocess
 
@@ -38,6 +39,33 @@ def test_dsb_fp32_bit_exact(ctx, n, R, steps, h):
     assert res.energy_check_ok and res.best_energy_i64 == res.best_energy == e.min()
     s = np.where(x[res.best_replica] > 0, 1, -1).astype(np.int8)
     np.testing.assert_array_equal(res.best_spins, s)
+
+
+@pytest.mark.parametrize("n,R,steps,persist", [(2048, 1, 50, True), (1000, 2, 40, True), (257, 5, 30, True),
+                                               (2049, 1, 10, False), (2000, 2, 10, False)])
+def test_dsb_one_launch_equals_per_step(ctx, n, R, steps, persist, monkeypatch):
+    """Plain FP32 dSB whose rows fit one co-resident grid (pitch <= 2048, ceil(n / 16) R CTAs) runs
+    the whole solve in one cooperative launch, exchanging signs through tagged words; it is bit
+    for bit the oracle's and the per-step kernel's (SB_PLAIN_PERSIST=0). Larger shapes keep one
+    launch per step."""
+    J = instances.erdos_renyi(n, 0.5, seed=n + 1, jmax=2, allow_zero=True)
+    hv = np.random.default_rng(n).integers(-2, 3, n).astype(np.float32)
+    prob, res, x, y, _ = run_dsb(ctx, J, hv, R, steps, seed=29)
+    np.testing.assert_array_equal(res.final_x, x)
+    np.testing.assert_array_equal(res.final_y, y)
+    assert res.steps_per_launch == (steps if persist else 1)
+    assert res.kernel_launches == (3 if persist else steps + 2)
+    monkeypatch.setenv("SB_PLAIN_PERSIST", "0")
+    ctx2 = sb.Context(0)
+    try:
+        prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=29, field_mode=sb.FIELD_FP32)
+        r2 = ctx2.solve(prob, prm, want_state=True)
+    finally:
+        ctx2.close()
+    assert r2.steps_per_launch == 1
+    np.testing.assert_array_equal(r2.final_x, res.final_x)
+    np.testing.assert_array_equal(r2.final_y, res.final_y)
+    np.testing.assert_array_equal(r2.replica_energies, res.replica_energies)
 
 
 def test_dsb_trace_matches_oracle(ctx):
@@ -103,8 +131,11 @@ def test_profile_mode_reports_kernel_time(ctx):
     J = instances.complete_pm1(512, seed=7)
     prob = sb.Problem.from_dense(J)
     prm = sb.Params.default(sb.DSB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1)
-    r = ctx.solve(prob, prm)
-    assert r.kernel_ms_avg > 0 and r.kernel_launches >= 22
+    r = ctx.solve(prob, prm)  # the one-launch form: one timed launch of 20 steps
+    assert r.kernel_ms_avg > 0 and r.steps_per_launch == 20 and r.kernel_launches == 3
+    prm = sb.Params.default(sb.ASB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1)
+    r = ctx.solve(prob, prm)  # one launch per step, each timed
+    assert r.kernel_ms_avg > 0 and r.steps_per_launch == 1 and r.kernel_launches >= 22
 
 
 def test_cli_drop_in(tmp_path):
