@@ -69,6 +69,8 @@ NCU_TRAFFIC = {
     "batched-dsb": (19.58e6, "profiles/tc_fp4_kernel_batched_dsb_n2000_r1024.md"),
     # plain dSB, N=2000, R=1: bytes per launch (ncu runs the launch with cold caches)
     "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
+    # the same in one cooperative launch per solve: DRAM read + write per launch (J read once)
+    "plain-dsb-persist": (31.17e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
     # batched bSB, N=8192, R=256, BF16 hi+lo: bytes per SB step (8-step capture: 2.278 GB; 4 steps:
     # 1.146 GB), times the launch's steps
     "batched-bsb": (2.278e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
