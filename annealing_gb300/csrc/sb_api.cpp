@@ -51,7 +51,7 @@ struct sb_plan {
   double *denergy = nullptr;
   uint32_t *dstatus = nullptr;
   float *dpump = nullptr;  // [steps] a0 - a(t), the schedule every kernel reads
-  // plain FP32 dSB that fits one cooperative launch: the sign words of PlainPersist
+  // plain FP32 SB that fits one cooperative launch: the exchange lines of PlainPersist
   unsigned long long *dwords = nullptr;
   size_t words_bytes = 0;
   float *dxk = nullptr;    // [kTopK][xp] rows of the best candidates (real-valued J)
@@ -290,9 +290,9 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->denergy, energy_slots(*prm) * (size_t)pl->R * sizeof(double));
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
   PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
-  // plain FP32 dSB whose rows fit one co-resident grid runs every step in one launch, unless
+  // plain FP32 SB whose rows fit one co-resident grid runs every step in one launch, unless
   // SB_PLAIN_PERSIST=0 keeps the one-launch-per-step kernel
-  if (mode == SB_FIELD_FP32 && prm->variant == SB_DSB && !needs_trace(*prm) && prm->steps > 0) {
+  if (mode == SB_FIELD_FP32 && !needs_trace(*prm) && prm->steps > 0) {
     const char *env = getenv("SB_PLAIN_PERSIST");
     const int ctas = (env && env[0] == '0') ? 0 : sbk::plain_persist_ctas(pl->n, pl->R, pl->jp);
     if (ctas > 0) {
@@ -371,12 +371,13 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
     return cudaSuccess;
   }
   if (pl->dwords) {
-    // plain FP32 dSB in one cooperative launch (same fields and updates as the per-step kernel)
+    // plain FP32 SB in one cooperative launch (same fields and updates as the per-step kernel)
     if (p.steps > 0) {
       cudaError_t e = cudaMemsetAsync(pl->dwords, 0, pl->words_bytes, st);
       if (e != cudaSuccess) return e;
       sbk::PlainPersist a;
       memset(&a, 0, sizeof(a));
+      a.variant = p.variant;
       a.n = pl->n;
       a.R = R;
       a.jp = pl->jp;
@@ -390,6 +391,11 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
       a.c0 = pl->c0;
       a.dt = p.dt;
       a.dta0 = pl->dta0;
+      a.coeff = pl->coeff;
+      a.mts_dt = p.mts_dt;
+      a.detune = p.detune;
+      a.kerr = p.kerr;
+      a.m = p.mts_m;
       a.steps = p.steps;
       a.words = pl->dwords;
       a.status = pl->dstatus;

@@ -47,19 +47,22 @@ struct PlainStep {
   int stages;              // set by launch_plain_step
 };
 
-// Plain FP32 dSB, the whole solve in one cooperative launch (sb_plain.cu): CTA (c, r) keeps rows
+// Plain FP32 SB, the whole solve in one cooperative launch (sb_plain.cu): CTA (c, r) keeps rows
 // [16 c, 16 c + 16) of J in registers (one row per warp; a lane holds the float4 groups g = lane +
-// 32 k, which is the per-step kernel's summation order) and replica r's x, y of those rows; a step
-// exchanges only the signs: CTA (c, r) publishes one word (step tag << 32 | 16 sign bits) in
-// words[parity][r][c] and reads the G words of its replica. Eligible when jp <= kPersistMaxJp and
-// G R CTAs (G = ceil(n / 16)) are co-resident.
+// 32 k, which is the per-step kernel's summation order) and replica r's x, y of those rows. A step
+// exchanges through one 128-byte line per CTA at words[parity][r][c]: dSB one word (step tag << 32 |
+// 16 sign bits), bSB / aSB sixteen (step tag << 32 | bits of x). Eligible when jp <= kPersistMaxJp
+// and G R CTAs (G = ceil(n / 16)) are co-resident.
 struct PlainPersist {
+  int variant;                // 0 aSB, 1 bSB (x exchanged), 2 dSB (signs exchanged)
   int n, R, jp, xp;
   const float *J, *h;         // J [n][jp], h [n] or null
   const float *x_in;          // x(0) [R][xp]
   float *x_out, *y;           // x(steps) (may alias x_in), y in place
   const float *pumps;         // [steps] a0 - a(t)
   float c0, dt, dta0;
+  float coeff, mts_dt, detune, kerr;  // aSB kick and local sub-steps
+  int m;
   int steps;
   unsigned long long *words;  // [2][R][G] words, one per 128-byte line (16 x 8 bytes), zero on entry
   uint32_t *status;

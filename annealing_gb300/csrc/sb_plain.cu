@@ -590,8 +590,13 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned l
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+template <int VARIANT>
 __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(PlainPersist a) {
-  __shared__ uint32_t sbits[kPersistMaxJp / kPersistRows];  // the G words' sign bits of this step
+  // dSB exchanges signs: one word per CTA (tag << 32 | 16 sign bits). bSB / aSB exchange x: the 16
+  // words of a CTA's line are its rows' (tag << 32 | bits of x), one written by each warp.
+  constexpr bool kSigns = VARIANT == 2;
+  __shared__ uint32_t sbits[kPersistMaxJp / kPersistRows];  // dSB: the G words' sign bits
+  __shared__ __align__(16) float xs[kPersistMaxJp];          // bSB / aSB: x(t) of every spin
   __shared__ uint32_t sout[kPersistRows];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c = blockIdx.x, r = blockIdx.y, G = gridDim.x;
@@ -618,21 +623,56 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
     y = a.y[k_xy];
   }
   const float hv = (have && a.h) ? a.h[row] : 0.0f;
-  // one 128-byte line per word: a CTA's store and the other CTAs' polls of it share no line with
-  // any other CTA's word
+  // one 128-byte line per CTA: its store(s) and the other CTAs' polls share no line with any other
+  // CTA's words
   constexpr int kLine = 16;                                       // words per line
   unsigned long long *wr = a.words + (size_t)r * G * kLine;      // parity 0 of replica r
   const size_t par = (size_t)a.R * G * kLine;                     // parity stride
-  // rows past n publish sign -1 (x = 0), as the per-step kernel reads padding spins
-  auto publish = [&](int t) {  // sign(x(t)) with tag t + 1
-    if (lane == 0) sout[warp] = (!have || !(x > 0.0f)) ? 1u : 0u;  // sgn: x > 0 -> +1, else -1
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t b = 0;
-      for (int w = 0; w < kPersistRows; ++w) b |= sout[w] << w;
-      st_relaxed_u64(wr + (size_t)(t & 1) * par + (size_t)c * kLine,
-                     ((unsigned long long)(uint32_t)(t + 1) << 32) | b);
+  // rows past n publish x = 0 (sign -1), as the per-step kernel reads padding spins
+  auto publish = [&](int t) {  // x(t) or its signs, with tag t + 1
+    const unsigned long long tag = (unsigned long long)(uint32_t)(t + 1) << 32;
+    unsigned long long *line = wr + (size_t)(t & 1) * par + (size_t)c * kLine;
+    if constexpr (kSigns) {
+      if (lane == 0) sout[warp] = (!have || !(x > 0.0f)) ? 1u : 0u;  // sgn: x > 0 -> +1, else -1
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t b = 0;
+        for (int w = 0; w < kPersistRows; ++w) b |= sout[w] << w;
+        st_relaxed_u64(line, tag | b);
+      }
+    } else {
+      if (lane == 0) st_relaxed_u64(line + warp, tag | __float_as_uint(have ? x : 0.0f));
+      __syncthreads();
     }
+  };
+  // one word with tag t + 1 into v: a first load, then bounded polling; false when it gave up
+  auto poll = [&](const unsigned long long *src, int t, unsigned long long &v) -> bool {
+    v = ld_relaxed_u64(src);
+    if ((uint32_t)(v >> 32) == (uint32_t)(t + 1)) return true;
+    const long long t0 = clock64();
+    int spins = 0;
+    do {
+      if (++spins > 8) __nanosleep(32);
+      v = ld_relaxed_u64(src);
+      if (clock64() - t0 > ptx::kWaitCycles) return false;
+    } while ((uint32_t)(v >> 32) != (uint32_t)(t + 1));
+    return true;
+  };
+  // thread q < G: CTA q's word(s) of step t into shared memory; false when a wait gave up
+  auto gather = [&](int t) -> bool {
+    if (tid >= G) return true;
+    const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
+    unsigned long long v;
+    if constexpr (kSigns) {
+      if (!poll(src, t, v)) return false;
+      sbits[tid] = (uint32_t)v & 0xFFFFu;
+    } else {
+      for (int w = 0; w < kPersistRows; ++w) {
+        if (!poll(src + w, t, v)) return false;
+        xs[tid * kPersistRows + w] = __uint_as_float((uint32_t)v);
+      }
+    }
+    return true;
   };
   publish(0);
   bool ok = true;
@@ -640,46 +680,44 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   for (int t = 0; t < a.steps && ok; ++t) {
     const float pump = pump_next;
     if (t + 1 < a.steps) pump_next = a.pumps[t + 1];  // off the step's critical path
-    // gather sign(x(t)): thread q < G waits for CTA q's word of step t
-    bool mine = true;
-    if (tid < G) {
-      const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
-      unsigned long long v = ld_relaxed_u64(src);
-      if ((uint32_t)(v >> 32) != (uint32_t)(t + 1)) {
-        const long long t0 = clock64();
-        int spins = 0;
-        do {
-          if (++spins > 8) __nanosleep(32);
-          v = ld_relaxed_u64(src);
-          if (clock64() - t0 > ptx::kWaitCycles) {
-            mine = false;
-            break;
-          }
-        } while ((uint32_t)(v >> 32) != (uint32_t)(t + 1));
-      }
-      sbits[tid] = (uint32_t)v & 0xFFFFu;
-    }
-    ok = __syncthreads_and(mine ? 1 : 0) != 0;
+    ok = __syncthreads_and(gather(t) ? 1 : 0) != 0;
     if (!ok) break;
-    // field of this warp's row: groups g = lane + 32 k, spins 4 g .. 4 g + 3 = bits 4 (g % 4) ..
-    // of CTA g / 4's word; sign -1 where the bit is set
+    // field of this warp's row over groups g = lane + 32 k (spins 4 g .. 4 g + 3)
     float acc = 0.0f;
 #pragma unroll
     for (int k = 0; k < kPersistGroups; ++k) {
       const int g = lane + 32 * k;
       if (g < ng) {
-        const uint32_t nib = sbits[g >> 2] >> (4 * (g & 3));
         const float4 jv = jr[k];
-        acc = __fmaf_rn(jv.x, (nib & 1u) ? -1.0f : 1.0f, acc);
-        acc = __fmaf_rn(jv.y, (nib & 2u) ? -1.0f : 1.0f, acc);
-        acc = __fmaf_rn(jv.z, (nib & 4u) ? -1.0f : 1.0f, acc);
-        acc = __fmaf_rn(jv.w, (nib & 8u) ? -1.0f : 1.0f, acc);
+        if constexpr (kSigns) {
+          // bits 4 (g % 4) .. of CTA g / 4's word; sign -1 where the bit is set
+          const uint32_t nib = sbits[g >> 2] >> (4 * (g & 3));
+          acc = __fmaf_rn(jv.x, (nib & 1u) ? -1.0f : 1.0f, acc);
+          acc = __fmaf_rn(jv.y, (nib & 2u) ? -1.0f : 1.0f, acc);
+          acc = __fmaf_rn(jv.z, (nib & 4u) ? -1.0f : 1.0f, acc);
+          acc = __fmaf_rn(jv.w, (nib & 8u) ? -1.0f : 1.0f, acc);
+        } else {
+          const float4 xv = reinterpret_cast<const float4 *>(xs)[g];
+          acc = __fmaf_rn(jv.x, xv.x, acc);
+          acc = __fmaf_rn(jv.y, xv.y, acc);
+          acc = __fmaf_rn(jv.z, xv.z, acc);
+          acc = __fmaf_rn(jv.w, xv.w, acc);
+        }
       }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (have) sb_update(acc, hv, pump, a.c0, a.dt, a.dta0, x, y);
-    publish(t + 1);  // its barrier also ends this step's reads of sbits
+    if (have) {
+      if constexpr (VARIANT == 0) {
+        // aSB: the coupling kick, then the next step's local sub-steps (none after the last)
+        y = __fmaf_rn(a.coeff, acc, y);
+        if (t + 1 < a.steps)
+          asb_local(x, y, __fdiv_rn((float)(t + 1), (float)a.steps), a.m, a.mts_dt, a.detune, a.kerr);
+      } else {
+        sb_update(acc, hv, pump, a.c0, a.dt, a.dta0, x, y);
+      }
+    }
+    publish(t + 1);  // its barrier also ends this step's reads of sbits / xs
   }
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
@@ -773,12 +811,18 @@ int plain_persist_ctas(int n, int R, int jp) {
   if (n < 1 || R < 1 || jp < 4 || jp % 4 || jp > kPersistMaxJp) return 0;
   const int G = (n + kPersistRows - 1) / kPersistRows;
   if (jp / 4 > 4 * G) return 0;
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, per_sm = 1 << 30;
   if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, plain_persist_kernel, kPersistThreads, 0) !=
-          cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
+  // the variants differ in registers: the least co-resident one decides
+  const void *ks[3] = {(const void *)plain_persist_kernel<0>, (const void *)plain_persist_kernel<1>,
+                       (const void *)plain_persist_kernel<2>};
+  for (const void *k : ks) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kPersistThreads, 0) != cudaSuccess) return 0;
+    per_sm = b < per_sm ? b : per_sm;
+  }
   const long long ctas = (long long)G * R;
   return ctas <= (long long)sms * per_sm ? (int)ctas : 0;
 }
@@ -795,7 +839,12 @@ cudaError_t launch_plain_persist(const PlainPersist &a, cudaStream_t st) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, plain_persist_kernel, a);
+  switch (a.variant) {
+    case 0: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<0>, a);
+    case 1: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<1>, a);
+    case 2: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<2>, a);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_plain_energy(const PlainEnergy &a0, bool fp64, cudaStream_t st) {

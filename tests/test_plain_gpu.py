@@ -68,6 +68,31 @@ def test_dsb_one_launch_equals_per_step(ctx, n, R, steps, persist, monkeypatch):
     np.testing.assert_array_equal(r2.replica_energies, res.replica_energies)
 
 
+@pytest.mark.parametrize("variant,n,R,steps", [(sb.BSB, 2000, 1, 60), (sb.BSB, 300, 3, 40), (sb.ASB, 2048, 1, 30),
+                                               (sb.ASB, 130, 2, 25)])
+def test_bsb_asb_one_launch_equals_per_step(ctx, variant, n, R, steps, monkeypatch):
+    """bSB and aSB (the reference's update) in one cooperative launch exchange x itself (16 tagged
+    words on a CTA's line): bit for bit the one-launch-per-step kernel's trajectories and energies."""
+    J = instances.complete_pm1(n, seed=n) if variant == sb.ASB else instances.gaussian(n, seed=n)[0]
+    prob = sb.Problem.from_dense(J)
+    prm = sb.Params.default(variant, steps=steps, replicas=R, seed=11, field_mode=sb.FIELD_FP32)
+    res = ctx.solve(prob, prm, want_state=True)
+    assert res.steps_per_launch == steps
+    monkeypatch.setenv("SB_PLAIN_PERSIST", "0")
+    ctx2 = sb.Context(0)
+    try:
+        r2 = ctx2.solve(prob, prm, want_state=True)
+    finally:
+        ctx2.close()
+    assert r2.steps_per_launch == 1
+    np.testing.assert_array_equal(r2.final_x, res.final_x)
+    np.testing.assert_array_equal(r2.final_y, res.final_y)
+    # real couplings: the FP64 energy pass adds its per-CTA partial sums with atomics (order not
+    # fixed, last bits may differ between runs); integer couplings: exact
+    np.testing.assert_allclose(r2.replica_energies, res.replica_energies, rtol=1e-12, atol=0)
+    assert res.energy_check_ok
+
+
 def test_dsb_trace_matches_oracle(ctx):
     J = instances.complete_pm1(300, seed=3)
     prob, res, x, y, (tr, tra) = run_dsb(ctx, J, None, 5, 40, seed=2, trace=1, trace_all=1)
@@ -133,8 +158,8 @@ def test_profile_mode_reports_kernel_time(ctx):
     prm = sb.Params.default(sb.DSB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1)
     r = ctx.solve(prob, prm)  # the one-launch form: one timed launch of 20 steps
     assert r.kernel_ms_avg > 0 and r.steps_per_launch == 20 and r.kernel_launches == 3
-    prm = sb.Params.default(sb.ASB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1)
-    r = ctx.solve(prob, prm)  # one launch per step, each timed
+    prm = sb.Params.default(sb.ASB, steps=20, replicas=2, field_mode=sb.FIELD_FP32, profile=1, trace=1)
+    r = ctx.solve(prob, prm)  # with a trace: one launch per step, each timed
     assert r.kernel_ms_avg > 0 and r.steps_per_launch == 1 and r.kernel_launches >= 22
 
 
