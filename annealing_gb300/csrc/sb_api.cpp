@@ -360,6 +360,8 @@ cudaError_t enqueue_loop(sb_plan *pl, cudaStream_t st, std::vector<cudaEvent_t> 
   int64_t nl = 0;
   if (pl->mode == SB_FIELD_TC) {
     if (p.steps > 0) {
+      sbk::tc_set_waits(pl->tc, (long long)pl->ctx->wait_cycles, pl->ctx->debug_skip_step);
+      pl->ctx->debug_skip_step = -1;
       if (evs) cudaEventRecord((*evs)[0], st);
       cudaError_t e = sbk::tc_run(pl->tc, p.steps, pl->dpump, pl->dx[0], pl->dy, pl->dh, pl->c0, p.dt,
                                   pl->dta0, tr ? pl->denergy : nullptr, pl->dstatus, st);
@@ -716,6 +718,20 @@ sb_status sb_destroy(sb_ctx *ctx) {
   sbh::nmfa_cache_free(ctx->nmfa);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
+  return SB_OK;
+}
+
+sb_status sb_set_wait_limit(sb_ctx *ctx, int64_t cycles) {
+  if (!ctx || cycles < 0) return SB_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->wait_cycles = cycles;
+  return SB_OK;
+}
+
+sb_status sb_debug_skip_publish(sb_ctx *ctx, int32_t step) {
+  if (!ctx || step < 0) return SB_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->debug_skip_step = step;
   return SB_OK;
 }
 

@@ -24,4 +24,6 @@ struct sb_ctx {
   sb_plan *cached = nullptr;  // most recent sb_solve plan, reused when the shape matches
   sbs::Server *server = nullptr;
   NmfaCache *nmfa = nullptr;  // device buffers of the last NMFA shape
+  int64_t wait_cycles = 0;    // bounded-wait limit of the tensor-core kernels (0: the default)
+  int32_t debug_skip_step = -1;  // sb_debug_skip_publish: consumed by the next tensor-core solve
 };

@@ -119,23 +119,30 @@ int tc_replica_tile(const TcEngine *e);
 cudaError_t tc_energy(TcEngine *e, int t, const float *x, const float *h, double *energy,
                       uint32_t *status, cudaStream_t st);
 int tc_dtype(const TcEngine *e);
+// Limit of every bounded wait in the engine's kernels (SM clock cycles; <= 0: the default, about
+// one second), and the fault injection for the timeout path: skip_step >= 0 makes unit 0 leave
+// out its step-skip_step flag, so its column's waits run out (skip_step < 0: off).
+void tc_set_waits(TcEngine *e, long long wait_cycles, int skip_step);
 
-// dSB on FP8 operands over buffers the caller provides; allocates nothing.
+// dSB on E2M1 or FP8 operands over buffers the caller provides; allocates nothing.
 struct TcExternal {
   const float *J;   // device couplings, row pitch jp floats
   int jp;
   const float *h;   // device fields or null
   int n, R, xp;
   float *x, *y;     // device state [R][xp]: initial in, final out
-  uint8_t *a;       // FP8 J operand, tc_external_sizes() a_bytes
+  bool fp4;         // packed E2M1 operands (integers |J| <= 4, tc_fp4_fits) instead of FP8
+  uint8_t *a;       // J operand, tc_external_sizes() a_bytes
   uint8_t *v0, *v1; // operand buffers, v_bytes each, zero on entry
-  uint32_t *flags, *status;    // one flag word per unit (<= 512 bytes), one status word
+  uint32_t *flags;  // flags_bytes (cleared by the solve itself)
+  uint32_t *status; // one status word, outside the flag bytes
   const float *pumps;          // [steps]
   int steps;
   float c0, dt, dta0;
   double *energy;   // [R] final energies, zero on entry
 };
-void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes);
-cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st);
+// Buffer sizes of the external dSB solve; false when the shape has no single-pass kernel.
+bool tc_external_sizes(int n, int R, bool fp4, size_t *a_bytes, size_t *v_bytes, size_t *flags_bytes);
+cudaError_t tc_dsb_external(const TcExternal &ext, cudaStream_t st);
 
 }  // namespace sbk

@@ -16,6 +16,12 @@
 // call before any stream capture. Every call shares the one array and the array keeps the last
 // call's contents: the parts that must start at zero are cleared by each call, and calls that
 // overlap on the GPU (different streams or threads at the same time) race on it.
+//
+// The call is synchronous: it reads the coupling scan back before the solve (couplings that no
+// operand type holds exactly are rejected without running a step) and the device status after it,
+// waiting for `stream` each time. Integer couplings with |J| <= 4 run on packed E2M1 operands when
+// the kernel that keeps J in shared memory fits the shape, others (|J| <= 16) on FP8; both give the
+// same bits as sb_solve's tensor-core dSB.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -32,17 +38,24 @@ namespace {
 constexpr int kMaxN = 2048;
 constexpr int kMaxReplicas = 1024;
 constexpr int kMaxSteps = 16384;
-// FP8 J operand (2048 x 2048) + two operand buffers (1024 x 2048) + pump table + control words.
+// J operand (FP8 2048 x 2048; packed E2M1 needs half) + two operand buffers (1024 x 2048) + pump
+// table + control words: [0, 2048) per-unit step flags (the solve clears what it uses), then the
+// status word and the coupling-scan word.
 constexpr size_t kOffA = 0;
 constexpr size_t kOffV0 = kOffA + (size_t)kMaxN * kMaxN;
 constexpr size_t kOffV1 = kOffV0 + (size_t)kMaxReplicas * kMaxN;
 constexpr size_t kOffPump = kOffV1 + (size_t)kMaxReplicas * kMaxN;
 constexpr size_t kOffCtl = kOffPump + (size_t)kMaxSteps * sizeof(float);
-constexpr size_t kNoAllocScratchBytes = kOffCtl + 1024;
+constexpr size_t kFlagBytes = 2048;
+constexpr size_t kCtlBytes = 4096;
+constexpr size_t kNoAllocScratchBytes = kOffCtl + kCtlBytes;
+static_assert(kNoAllocScratchBytes == 8458240, "the size stated in sb.h");
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr uint32_t kErrNotFp8Exact = 0x100u;  // a coupling is not an integer with |J| <= 16
+// coupling-scan bits
+constexpr uint32_t kNotFp8Exact = 1u;   // a coupling is not an integer with |J| <= 16
+constexpr uint32_t kNotE2m1Exact = 2u;  // a coupling is not an integer with |J| <= 4
 
 std::mutex g_mu;
 void *g_scratch_ptr[64] = {nullptr};
@@ -55,16 +68,21 @@ __global__ void noalloc_pumps_kernel(float *pumps, float a0, int steps) {
   pumps[t] = __fsub_rn(a0, __double2float_rn(a));
 }
 
-// FP8 E4M3 holds the couplings exactly only when each is an integer with |J| <= 16.
-__global__ void noalloc_check_kernel(const float *J, size_t count, uint32_t *status) {
+// Which operand types hold the couplings exactly: FP8 E4M3 every integer |J| <= 16, E2M1 every
+// integer |J| <= 4.
+__global__ void noalloc_scan_kernel(const float *J, size_t count, uint32_t *scan) {
+  uint32_t bits = 0;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < count;
        k += (size_t)gridDim.x * blockDim.x) {
-    const float v = J[k];
-    if (!(fabsf(v) <= 16.0f) || v != truncf(v)) {
-      atomicOr(status, kErrNotFp8Exact);
-      return;
+    const float v = J[k], a = fabsf(v);
+    if (!(a <= 16.0f) || v != truncf(v)) {
+      bits = kNotFp8Exact | kNotE2m1Exact;
+      break;
     }
+    if (a > 4.0f) bits |= kNotE2m1Exact;
   }
+  bits = __reduce_or_sync(0xffffffffu, bits);
+  if ((threadIdx.x & 31) == 0 && bits) atomicOr(scan, bits);
 }
 
 sb_status fail(sb_status s, const std::string &msg) {
@@ -108,29 +126,40 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
   }
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t *sc = (uint8_t *)base;
-  int nr = 0;
-  size_t a_bytes = 0, v_bytes = 0;
-  sbk::tc_external_sizes(n, replicas, &nr, &a_bytes, &v_bytes);
-  if (nr == 0 || a_bytes > kOffV0 - kOffA || v_bytes > kOffV1 - kOffV0)
-    return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: shape does not fit the scratch tiling");
-  uint32_t *ctl = (uint32_t *)(sc + kOffCtl);  // [0, 128): per-unit step flags, [192]: status
-  uint32_t *status = ctl + 192;
+  uint32_t *flags = (uint32_t *)(sc + kOffCtl);
+  uint32_t *status = (uint32_t *)(sc + kOffCtl + kFlagBytes);
+  uint32_t *scan = status + 1;
   float *pumps = (float *)(sc + kOffPump);
   cudaError_t e;
   std::string where;
+  uint32_t scan_bits = 0, hstatus = 0;
+  bool fp4 = false;
+  size_t a_bytes = 0, v_bytes = 0, f_bytes = 0;
 #define NA_CUDA(call)                       \
   if ((e = (call)) != cudaSuccess) {        \
     where = #call;                          \
     goto cuda_fail;                         \
   }
-  // what must start at zero: control words, both operand buffers (their padding is never
-  // written), the caller's energy accumulators
-  NA_CUDA(cudaMemsetAsync(ctl, 0, 1024, st));
+  // The coupling scan comes first, so that couplings no operand type holds exactly are rejected
+  // before any solve work; it also picks the operand type (packed E2M1 when every coupling allows
+  // it and the kernel that keeps J in shared memory fits this shape, else FP8).
+  NA_CUDA(cudaMemsetAsync(sc + kOffCtl, 0, kCtlBytes, st));
+  noalloc_scan_kernel<<<152, 256, 0, st>>>(d_J, (size_t)n * n, scan);
+  NA_CUDA(cudaGetLastError());
+  NA_CUDA(cudaMemcpyAsync(&scan_bits, scan, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  NA_CUDA(cudaStreamSynchronize(st));
+  if (scan_bits & kNotFp8Exact)
+    return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: couplings must be integers with |J| <= 16");
+  fp4 = !(scan_bits & kNotE2m1Exact) && sbk::tc_external_sizes(n, replicas, true, &a_bytes, &v_bytes, &f_bytes);
+  if (!fp4 && !sbk::tc_external_sizes(n, replicas, false, &a_bytes, &v_bytes, &f_bytes))
+    return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: no single-pass tensor-core kernel for this shape");
+  if (a_bytes > kOffV0 - kOffA || v_bytes > kOffV1 - kOffV0 || f_bytes > kFlagBytes)
+    return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: shape does not fit the scratch tiling");
+  // what must start at zero: both operand buffers (their padding is never written) and the
+  // caller's energy accumulators; the solve clears its own flags
   NA_CUDA(cudaMemsetAsync(sc + kOffV0, 0, v_bytes, st));
   NA_CUDA(cudaMemsetAsync(sc + kOffV1, 0, v_bytes, st));
   NA_CUDA(cudaMemsetAsync(d_energies, 0, (size_t)replicas * sizeof(double), st));
-  noalloc_check_kernel<<<152, 256, 0, st>>>(d_J, (size_t)n * n, status);
-  NA_CUDA(cudaGetLastError());
   if (steps > 0) {
     noalloc_pumps_kernel<<<(steps + 255) / 256, 256, 0, st>>>(pumps, a0, steps);
     NA_CUDA(cudaGetLastError());
@@ -146,10 +175,11 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
     ext.xp = n;
     ext.x = d_x;
     ext.y = d_y;
+    ext.fp4 = fp4;
     ext.a = sc + kOffA;
     ext.v0 = sc + kOffV0;
     ext.v1 = sc + kOffV1;
-    ext.flags = ctl;
+    ext.flags = flags;
     ext.status = status;
     ext.pumps = pumps;
     ext.steps = steps;
@@ -157,17 +187,12 @@ extern "C" sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, in
     ext.dt = dt;
     ext.dta0 = dt * a0;
     ext.energy = d_energies;
-    NA_CUDA(sbk::tc_dsb_fp8_external(ext, st));
+    NA_CUDA(sbk::tc_dsb_external(ext, st));
   }
-  {
-    uint32_t hstatus = 0;
-    NA_CUDA(cudaMemcpyAsync(&hstatus, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    NA_CUDA(cudaStreamSynchronize(st));
-    if (hstatus & kErrNotFp8Exact)
-      return fail(SB_ERR_UNSUPPORTED, "sb_dsb_solve_noalloc: couplings must be integers with |J| <= 16");
-    if (hstatus & sbk::kErrWaitTimeout) return fail(SB_ERR_TIMEOUT, "sb_dsb_solve_noalloc: a device wait timed out");
-    if (hstatus) return fail(SB_ERR_CUDA, "sb_dsb_solve_noalloc: " + sbh::device_status_text(hstatus));
-  }
+  NA_CUDA(cudaMemcpyAsync(&hstatus, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  NA_CUDA(cudaStreamSynchronize(st));
+  if (hstatus & sbk::kErrWaitTimeout) return fail(SB_ERR_TIMEOUT, "sb_dsb_solve_noalloc: a device wait timed out");
+  if (hstatus) return fail(SB_ERR_CUDA, "sb_dsb_solve_noalloc: " + sbh::device_status_text(hstatus));
 #undef NA_CUDA
   return SB_OK;
 cuda_fail:

@@ -447,34 +447,57 @@ void sbh::problem_scan(sb_problem *p) {
     int bad = 0;
     float m = 0.0f;
     int64_t e = 0;
-    double a1 = 0.0, a2 = 0.0;
+    int64_t a1 = 0, a2 = 0;
     for (int i = t; i < n; i += nt) {
       const float *Ji = p->J + (size_t)i * n;
-      int rb = 0;
-      float rm = 0.0f;
-      double r1 = 0.0, r2 = 0.0;  // exact for the integer couplings they are kept for
+      // integrality and the largest |J| of the row, in a form the compiler vectorises: |w| < 2^23
+      // is an integer exactly when adding and subtracting 2^23 gives it back, larger floats all
+      // are, NaN is not; the maximum runs on the bit patterns of |w| (monotonic for non-negative
+      // floats; NaN counts as 0)
+      uint32_t rb = 0, rm = 0;
       for (int j = 0; j < n; ++j) {
-        const float w = Ji[j];
-        rb |= (w != floorf(w)) ? 1 : 0;  // NaN is not integral
-        const float a = fabsf(w);
-        rm = a > rm ? a : rm;
-        r1 += (double)w;
-        r2 += (double)w * (double)w;
+        const float a = fabsf(Ji[j]);
+        const float r = (a + 8388608.0f) - 8388608.0f;
+        rb |= (uint32_t)((r != a) & (a < 8388608.0f)) | (uint32_t)(a != a);
+        uint32_t u;
+        memcpy(&u, &a, sizeof(u));
+        u &= (a == a) ? 0xFFFFFFFFu : 0u;
+        rm = u > rm ? u : rm;
       }
-      const double dg = (double)Ji[i];  // the diagonal does not count
-      a1 += r1 - dg;
-      a2 += r2 - dg * dg;
+      float rmax;
+      memcpy(&rmax, &rm, sizeof(rmax));
+      // the off-diagonal sums of J and J^2, kept only for integer couplings: exact integer sums
+      // (a row sum of |J| < 2^15 stays below 2^31 for n <= 65536)
+      if (rb == 0 && rmax < 32768.0f) {
+        int32_t s1 = 0;
+        int64_t s2 = 0;
+        for (int j = 0; j < n; ++j) {
+          const int32_t v = (int32_t)Ji[j];
+          s1 += v;
+          s2 += (int64_t)(v * v);
+        }
+        const int64_t dg = (int64_t)Ji[i];  // the diagonal does not count
+        a1 += (int64_t)s1 - dg;
+        a2 += s2 - dg * dg;
+      } else if (rb == 0 && rmax < 2147483648.0f) {
+        for (int j = 0; j < n; ++j) {
+          if (j == i) continue;
+          const int64_t v = (int64_t)Ji[j];  // integral and below 2^31
+          a1 += v;
+          a2 += v * v;
+        }
+      }
       int64_t re = 0;
       for (int j = i + 1; j < n; ++j) re += Ji[j] != 0.0f ? 1 : 0;
-      bad |= rb;
-      m = rm > m ? rm : m;
+      bad |= rb != 0 ? 1 : 0;
+      m = rmax > m ? rmax : m;
       e += re;
     }
     nonint[t] = bad;
     mx[t] = m;
     ed[t] = e;
-    sj[t] = a1;
-    sj2[t] = a2;
+    sj[t] = (double)a1;
+    sj2[t] = (double)a2;
   };
   if (nt == 1) {
     rows(0);

@@ -48,12 +48,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // Bounded wait for the phase with the given parity to complete. false = gave up.
 // After a short burst of immediate retries the waiting thread sleeps between polls, so a waiting
 // producer or MMA lane does not take issue slots from the warps doing work.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = kWaitCycles) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   int spins = 0;
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
     if (++spins > 16) __nanosleep(32);
   }
   return true;

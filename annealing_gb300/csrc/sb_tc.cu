@@ -219,6 +219,77 @@ int choose_nr_nmfa(int n, int R, int sms) {
 // one counter per unit (per unit and replica half for the E2M1 kernel)
 size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * 2 * sizeof(uint32_t) + 255) / 256 * 256; }
 
+namespace {
+
+// Tile geometry of an engine: the setup, the replica tile and the padded extents that follow.
+void set_geometry(TcEngine *e, const TcSetup &s, int nr) {
+  e->s = s;
+  e->nr = nr;
+  if (s.dtype == kTcFp4) e->threads = kFp4Threads;
+  e->Np = (s.n + kBM - 1) / kBM * kBM;
+  e->Kp = kp_for(s.dtype, s.n);
+  e->Rp = (s.R + nr - 1) / nr * nr;
+  e->n_mtiles = e->Np / kBM;
+  e->n_rtiles = e->Rp / nr;
+  e->units = e->n_mtiles * e->n_rtiles;
+}
+
+int elem_bytes(const TcEngine *e) { return (e->s.dtype == kTcFp8 || e->s.dtype == kTcFp4) ? 1 : 2; }
+// operand row length in tensor-map elements: bytes of E2M1 pairs, else K elements
+uint64_t row_elems(const TcEngine *e) { return e->s.dtype == kTcFp4 ? (uint64_t)e->Kp / 2 : (uint64_t)e->Kp; }
+int a_parts(const TcEngine *e) { return e->s.dtype == kTcBf16Split ? 2 : 1; }
+int b_parts(const TcEngine *e) {
+  return ((e->s.dtype == kTcBf16Split && e->s.variant == 1) || e->s.variant == 3) ? 2 : 1;
+}
+size_t a_part_bytes(const TcEngine *e) { return (size_t)e->Np * row_elems(e) * elem_bytes(e); }
+size_t v_part_bytes(const TcEngine *e) { return (size_t)e->Rp * row_elems(e) * elem_bytes(e); }
+
+// Tensor maps, kernel arguments and the shared-memory attribute of an engine whose operand and
+// flag buffers are in place. Returns null, or the name of the call that failed (its CUDA error in
+// *ce, cudaSuccess when the call is a tensor-map encoding).
+const char *bind(TcEngine *e, cudaError_t *ce) {
+  *ce = cudaSuccess;
+  const bool fp4 = e->s.dtype == kTcFp4;
+  const int elem = elem_bytes(e), nr = e->nr;
+  // V boxes: the whole replica tile, or one replica half for the E2M1 kernel
+  const uint32_t vrows = fp4 ? (uint32_t)(nr >= 64 ? nr / 2 : nr) : (uint32_t)nr;
+  const uint64_t rowe = row_elems(e);
+  TcArgs &g = e->args;
+  memset(&g, 0, sizeof(g));
+  for (int a = 0; a < a_parts(e); ++a)
+    if (!encode_2d(&g.tmA[a], e->a[a], elem, rowe, (uint64_t)e->Np, kBM)) return "cuTensorMapEncodeTiled(J)";
+  for (int b = 0; b < 2; ++b)
+    for (int pp = 0; pp < b_parts(e); ++pp) {
+      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, rowe, (uint64_t)e->Rp, vrows))
+        return "cuTensorMapEncodeTiled(V)";
+      g.v[b][pp] = e->v[b][pp];
+    }
+  // the unit's V tile: 128 spins = 128 elements, or 64 bytes of E2M1 pairs
+  for (int b = 0; b < 2; ++b)
+    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, rowe, (uint64_t)e->Rp, vrows, true, fp4 ? kBM / 2 : kBM))
+      return "cuTensorMapEncodeTiled(V store)";
+  g.flags = e->flags;
+  g.n = e->s.n;
+  g.R = e->s.R;
+  g.xp = e->s.xp;
+  g.Kp = e->Kp;
+  g.Rp = e->Rp;
+  g.n_mtiles = e->n_mtiles;
+  g.n_rtiles = e->n_rtiles;
+  g.k_chunks = (int)(rowe * elem / kChunkBytes);
+  g.wait_cycles = ptx::kWaitCycles;
+  g.skip_unit = -1;
+  g.skip_step = -1;
+  for (int m = 0; m < 3; ++m)
+    if (e->kernel[m] &&
+        (*ce = cudaFuncSetAttribute(e->kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem)) !=
+            cudaSuccess)
+      return "cudaFuncSetAttribute";
+  return nullptr;
+}
+
+}  // namespace
+
 bool tc_fp4_fits(int n, int R) {
   const int nr = choose_nr(n, R, sm_count());
   const void *k = nullptr;
@@ -262,70 +333,30 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     return SB_ERR_UNSUPPORTED;
   }
   TcEngine *e = new TcEngine();
-  e->s = s;
-  e->nr = nr;
   if (!pick(e, s.dtype, s.variant, nr, s.n)) {
     delete e;
     err = "no kernel for this dtype / variant / size";
     return SB_ERR_UNSUPPORTED;
   }
-  const bool fp4 = s.dtype == kTcFp4;
-  const int elem = (s.dtype == kTcFp8 || fp4) ? 1 : 2;
-  // V boxes: the whole replica tile, or one replica half for the E2M1 kernel
-  const uint32_t vrows = fp4 ? (uint32_t)(nr >= 64 ? nr / 2 : nr) : (uint32_t)nr;
-  if (fp4) e->threads = kFp4Threads;
-  e->Np = (s.n + kBM - 1) / kBM * kBM;
-  e->Kp = kp_for(s.dtype, s.n);
-  const uint64_t row_elems = fp4 ? (uint64_t)e->Kp / 2 : (uint64_t)e->Kp;  // operand row: bytes (E2M1 pairs) or elements
-  e->Rp = (s.R + nr - 1) / nr * nr;
-  e->n_mtiles = e->Np / kBM;
-  e->n_rtiles = e->Rp / nr;
-  e->units = e->n_mtiles * e->n_rtiles;
-  const int ap = s.dtype == kTcBf16Split ? 2 : 1;
-  const int bp = ((s.dtype == kTcBf16Split && s.variant == 1) || s.variant == 3) ? 2 : 1;
+  set_geometry(e, s, nr);
   auto fail = [&](const char *what, cudaError_t ce) {
     err = std::string(what) + (ce != cudaSuccess ? std::string(": ") + cudaGetErrorString(ce) : "");
     tc_destroy(e);
     return ce == cudaErrorMemoryAllocation ? SB_ERR_OOM : SB_ERR_CUDA;
   };
   cudaError_t ce;
-  const size_t abytes = (size_t)e->Np * row_elems * elem, vbytes = (size_t)e->Rp * row_elems * elem;
-  for (int a = 0; a < ap; ++a)
+  const size_t abytes = a_part_bytes(e), vbytes = v_part_bytes(e);
+  for (int a = 0; a < a_parts(e); ++a)
     if ((ce = cudaMalloc(&e->a[a], abytes)) != cudaSuccess) return fail("cudaMalloc(J operand)", ce);
   for (int b = 0; b < 2; ++b)
-    for (int pp = 0; pp < bp; ++pp) {
+    for (int pp = 0; pp < b_parts(e); ++pp) {
       if ((ce = cudaMalloc(&e->v[b][pp], vbytes)) != cudaSuccess) return fail("cudaMalloc(V operand)", ce);
       if ((ce = cudaMemsetAsync(e->v[b][pp], 0, vbytes, st)) != cudaSuccess) return fail("memset", ce);
     }
   if ((ce = cudaMalloc(&e->flags, flag_bytes(e))) != cudaSuccess) return fail("cudaMalloc(flags)", ce);
   if ((ce = tc_reload(e, dJ, jp, st)) != cudaSuccess) return fail("convert_j_kernel", ce);
-  TcArgs &g = e->args;
-  memset(&g, 0, sizeof(g));
-  for (int a = 0; a < ap; ++a)
-    if (!encode_2d(&g.tmA[a], e->a[a], elem, row_elems, (uint64_t)e->Np, kBM)) return fail("cuTensorMapEncodeTiled(J)", cudaSuccess);
-  for (int b = 0; b < 2; ++b)
-    for (int pp = 0; pp < bp; ++pp) {
-      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, row_elems, (uint64_t)e->Rp, vrows))
-        return fail("cuTensorMapEncodeTiled(V)", cudaSuccess);
-      g.v[b][pp] = e->v[b][pp];
-    }
-  // the unit's V tile: 128 spins = 128 elements, or 64 bytes of E2M1 pairs
-  for (int b = 0; b < 2; ++b)
-    if (!encode_2d(&g.tmS[b], e->v[b][0], elem, row_elems, (uint64_t)e->Rp, vrows, true, fp4 ? kBM / 2 : kBM))
-      return fail("cuTensorMapEncodeTiled(V store)", cudaSuccess);
-  g.flags = e->flags;
-  g.n = s.n;
-  g.R = s.R;
-  g.xp = s.xp;
-  g.Kp = e->Kp;
-  g.Rp = e->Rp;
-  g.n_mtiles = e->n_mtiles;
-  g.n_rtiles = e->n_rtiles;
-  g.k_chunks = (int)(row_elems * elem / kChunkBytes);
-  for (int m = 0; m < 3; ++m)
-    if (e->kernel[m] &&
-        (ce = cudaFuncSetAttribute(e->kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem)) != cudaSuccess)
-      return fail("cudaFuncSetAttribute", ce);
+  const char *what = bind(e, &ce);
+  if (what) return fail(what, ce);
   *out = e;
   return SB_OK;
 }
@@ -352,6 +383,12 @@ cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st) {
 }
 
 int tc_dtype(const TcEngine *e) { return e ? e->s.dtype : 0; }
+
+void tc_set_waits(TcEngine *e, long long wait_cycles, int skip_step) {
+  e->args.wait_cycles = wait_cycles > 0 ? wait_cycles : ptx::kWaitCycles;
+  e->args.skip_unit = skip_step >= 0 ? 0 : -1;
+  e->args.skip_step = skip_step;
+}
 int tc_units(const TcEngine *e) { return e ? e->units : 0; }
 int tc_replica_tile(const TcEngine *e) { return e ? e->nr : 0; }
 
@@ -467,58 +504,31 @@ cudaError_t tc_energy_signs(TcEngine *e, const float *x, const float *h, double 
   return cudaLaunchKernelExC(&cfg, k, params);
 }
 
-void tc_external_sizes(int n, int R, int *nr, size_t *a_bytes, size_t *v_bytes) {
-  const int r = choose_nr(n, R, sm_count());
-  const size_t Np = (size_t)(n + kBM - 1) / kBM * kBM, Kp = (size_t)(n + 127) / 128 * 128;
-  const size_t Rp = r > 0 ? (size_t)(R + r - 1) / r * r : 0;
-  *nr = r;
-  *a_bytes = Np * Kp;
-  *v_bytes = Rp * Kp;
+bool tc_external_sizes(int n, int R, bool fp4, size_t *a_bytes, size_t *v_bytes, size_t *flags_bytes) {
+  const int nr = choose_nr(n, R, sm_count());
+  *a_bytes = *v_bytes = *flags_bytes = 0;
+  if (nr == 0 || (fp4 && !tc_fp4_fits(n, R))) return false;
+  TcEngine e;
+  set_geometry(&e, TcSetup{2, fp4 ? kTcFp4 : kTcFp8, n, R, n}, nr);
+  *a_bytes = a_part_bytes(&e);
+  *v_bytes = v_part_bytes(&e);
+  *flags_bytes = flag_bytes(&e);
+  return true;
 }
 
-cudaError_t tc_dsb_fp8_external(const TcExternal &ext, cudaStream_t st) {
+cudaError_t tc_dsb_external(const TcExternal &ext, cudaStream_t st) {
   TcEngine e;  // on the stack: every buffer below belongs to the caller
-  e.s = TcSetup{2, kTcFp8, ext.n, ext.R, ext.xp};
-  e.nr = choose_nr(ext.n, ext.R, sm_count());
-  if (e.nr == 0 || !pick(&e, kTcFp8, 2, e.nr, ext.n)) return cudaErrorInvalidValue;
-  e.Np = (ext.n + kBM - 1) / kBM * kBM;
-  e.Kp = (ext.n + 127) / 128 * 128;
-  e.Rp = (ext.R + e.nr - 1) / e.nr * e.nr;
-  e.n_mtiles = e.Np / kBM;
-  e.n_rtiles = e.Rp / e.nr;
-  e.units = e.n_mtiles * e.n_rtiles;
+  const int dt = ext.fp4 ? kTcFp4 : kTcFp8;
+  const int nr = choose_nr(ext.n, ext.R, sm_count());
+  if (nr == 0 || (ext.fp4 && !tc_fp4_fits(ext.n, ext.R)) || !pick(&e, dt, 2, nr, ext.n)) return cudaErrorInvalidValue;
+  set_geometry(&e, TcSetup{2, dt, ext.n, ext.R, ext.xp}, nr);
   e.a[0] = ext.a;
   e.v[0][0] = ext.v0;
   e.v[1][0] = ext.v1;
   e.flags = ext.flags;
-  TcArgs &g = e.args;
-  memset(&g, 0, sizeof(g));
-  if (!encode_2d(&g.tmA[0], e.a[0], 1, (uint64_t)e.Kp, (uint64_t)e.Np, kBM) ||
-      !encode_2d(&g.tmB[0][0], e.v[0][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr) ||
-      !encode_2d(&g.tmB[1][0], e.v[1][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr))
-    return cudaErrorInvalidValue;
-  if (!encode_2d(&g.tmS[0], e.v[0][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr, true) ||
-      !encode_2d(&g.tmS[1], e.v[1][0], 1, (uint64_t)e.Kp, (uint64_t)e.Rp, (uint32_t)e.nr, true))
-    return cudaErrorInvalidValue;
-  g.v[0][0] = e.v[0][0];
-  g.v[1][0] = e.v[1][0];
-  g.flags = e.flags;
-  g.n = ext.n;
-  g.R = ext.R;
-  g.xp = ext.xp;
-  g.Kp = e.Kp;
-  g.Rp = e.Rp;
-  g.n_mtiles = e.n_mtiles;
-  g.n_rtiles = e.n_rtiles;
-  g.k_chunks = e.Kp / kChunkBytes;
   cudaError_t ce = cudaSuccess;
-  for (int m = 0; m < 3; ++m)
-    if (e.kernel[m] &&
-        (ce = cudaFuncSetAttribute(e.kernel[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem)) != cudaSuccess)
-      return ce;
-  convert_j_kernel<<<grid_1d((size_t)e.Np * e.Kp), 256, 0, st>>>(ext.J, ext.n, ext.jp, e.a[0], nullptr, e.Np, e.Kp,
-                                                                 kTcFp8);
-  if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+  if (bind(&e, &ce)) return ce != cudaSuccess ? ce : cudaErrorInvalidValue;
+  if ((ce = tc_reload(&e, ext.J, ext.jp, st)) != cudaSuccess) return ce;
   if ((ce = tc_prepare(&e, ext.x, st)) != cudaSuccess) return ce;
   if ((ce = tc_run(&e, ext.steps, ext.pumps, ext.x, ext.y, ext.h, ext.c0, ext.dt, ext.dta0, nullptr, ext.status,
                    st)) != cudaSuccess)

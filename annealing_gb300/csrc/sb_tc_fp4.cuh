@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
   uint8_t *ring = smem;                                   // [STAGES][NH][128] V chunks
   uint8_t *jres = smem + STAGES * kBTile;                  // [k_chunks][128][128] resident J
   uint8_t *vtile = jres + (size_t)p.k_chunks * kFp4ATile;  // [NR][64] next V tile (half h: rows h NH ..)
-  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], a_bar, accf_bar[H], acce_bar[H], pub_bar[H];
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], a_bar, accf_bar[H], acce_bar[H], pub_bar[H],
+      drain_bar;
   __shared__ uint32_t tmem_base_sh;
   __shared__ float ered[4][NR];
 
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
       ptx::mbar_init(&empty_bar[s], 1);
     }
     ptx::mbar_init(&a_bar, 1);
+    ptx::mbar_init(&drain_bar, 1);
     for (int h = 0; h < H; ++h) {
       ptx::mbar_init(&accf_bar[h], 1);
       ptx::mbar_init(&acce_bar[h], kEpiWarps);
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
       for (int kc = 0; kc < p.k_chunks; ++kc)
         ptx::tma_load_2d(jres + (size_t)kc * kFp4ATile, &p.tmA[0], kc * kChunkBytes, m0, &a_bar);
     }
-    uint32_t g = 0;
+    uint32_t g = 0, issued = 0;  // chunks walked / V loads issued (lane 0)
     for (int ls = 0; ls < nsteps && ok; ++ls) {
       const int buf = (p.buf0 + ls) & 1;
       for (int h = 0; h < H && ok; ++h) {
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           const uint32_t *hf = p.flags + (size_t)(rt * H + h) * p.n_mtiles;
           for (int u0 = 0; u0 < p.n_mtiles && ok; u0 += 32) {
             const int u = u0 + lane;
-            const bool fl = u < p.n_mtiles ? wait_flag(hf + u, (uint32_t)ls) : true;
+            const bool fl = u < p.n_mtiles ? wait_flag(hf + u, (uint32_t)ls, p.wait_cycles) : true;
             if (!__all_sync(0xffffffffu, fl)) ok = false;
           }
           ptx::fence_proxy_async_global();
@@ -165,31 +167,39 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           if (lane == 0) {
             const int s = g % STAGES;
             const uint32_t use = g / STAGES;
-            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1, p.wait_cycles)) {
               ok = false;
             } else {
               ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)kBTile);
               ptx::tma_load_2d(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes, r0 + h * NH, &full_bar[s]);
+              ++issued;
             }
           }
           ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
         }
       }
     }
+    if (!ok && lane == 0) {
+      // a wait gave up: let the copies this CTA started land before it exits (each stage's last
+      // issued load, and the resident J)
+      for (int s = 0; s < STAGES; ++s)
+        if (issued > (uint32_t)s) ptx::mbar_wait(&full_bar[s], ((issued - 1 - s) / STAGES) & 1, p.wait_cycles);
+      ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
+    }
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      ok = ptx::mbar_wait(&a_bar, 0);
+      ok = ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
       uint32_t g = 0;
       for (int ls = 0; ls < nsteps && ok; ++ls) {
         for (int h = 0; h < H && ok; ++h) {
-          if (ls >= 1 && !ptx::mbar_wait(&acce_bar[h], (uint32_t)(ls - 1) & 1)) { ok = false; break; }
+          if (ls >= 1 && !ptx::mbar_wait(&acce_bar[h], (uint32_t)(ls - 1) & 1, p.wait_cycles)) { ok = false; break; }
           ptx::tc_fence_after();
           const uint32_t t_acc = tmem + h * NH;
           for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
             const int s = g % STAGES;
             const uint32_t use = g / STAGES;
-            if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+            if (!ptx::mbar_wait(&full_bar[s], use & 1, p.wait_cycles)) { ok = false; break; }
             ptx::tc_fence_after();
             const uint32_t sa = ptx::smem_u32(jres + (size_t)kc * kFp4ATile);
             const uint32_t sb = ptx::smem_u32(ring + s * kBTile);
@@ -203,6 +213,11 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           ptx::mma_commit(&accf_bar[h]);
         }
       }
+      if (!ok) {
+        // a wait gave up: the MMAs already issued finish before TMEM is freed
+        ptx::mma_commit(&drain_bar);
+        ptx::mbar_wait(&drain_bar, 0, p.wait_cycles);
+      }
     }
   } else if (warp == 2 + kEpiWarps) {
     // ---------------- publisher: half tile -> global (TMA store), then the flag ----------------
@@ -210,12 +225,13 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
       for (int ls = 0; ls < nsteps && ok; ++ls) {
         const int buf = (p.buf0 + ls) & 1;
         for (int h = 0; h < H; ++h) {
-          if (!ptx::mbar_wait(&pub_bar[h], (uint32_t)ls & 1)) { ok = false; break; }
+          if (!ptx::mbar_wait(&pub_bar[h], (uint32_t)ls & 1, p.wait_cycles)) { ok = false; break; }
           ptx::tma_store_2d(&p.tmS[buf ^ 1], vtile + (size_t)h * NH * kVRow, m0 / 2, r0 + h * NH);
           ptx::bulk_commit();
           ptx::bulk_wait_all();             // the half tile is in global memory
           ptx::fence_proxy_async_global();  // the bulk store's writes, then the flag (release)
-          if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status))
+          if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status) &&
+              !((int)blockIdx.x == p.skip_unit && ls == p.skip_step))
             st_release(p.flags + (size_t)(rt * H + h) * p.n_mtiles + mt, (uint32_t)(ls + 1));
         }
       }
@@ -250,7 +266,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
       const float pump = pump_next;
       if (!kEOnly && ls + 1 < nsteps) pump_next = p.pumps[t + 1];
       for (int h = 0; h < H; ++h) {
-        const bool got = ptx::mbar_wait(&accf_bar[h], (uint32_t)ls & 1);
+        const bool got = ptx::mbar_wait(&accf_bar[h], (uint32_t)ls & 1, p.wait_cycles);
         if (!epi_all(got)) { ok = false; break; }
         ptx::tc_fence_after();
         const int c_lo = h * NH + sub * F::kWarpCols;

@@ -72,6 +72,10 @@ struct alignas(64) TcArgs {
   float c0, dt, dta0;
   uint32_t *rng;           // NMFA: [5][R][xp] XORWOW words of each (sample, spin)
   float noise, keep, mix;  // NMFA: sigma, 1 - alpha, alpha
+  long long wait_cycles;   // limit of every bounded wait (SM clock cycles)
+  // host-side fault injection for the timeout path: unit skip_unit does not publish its flag(s)
+  // of step skip_step (skip_step < 0: every unit publishes)
+  int skip_unit, skip_step;
 };
 
 template <int DT>
@@ -172,11 +176,11 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
 // Bounded wait until a unit's published step counter reaches `target`. Polls with relaxed loads
 // (an acquire load per poll would order, and slow, everything else on this SM) and backs off;
 // the acquire fence is taken once the flag is seen.
-__device__ __forceinline__ bool wait_flag(const uint32_t *flag, uint32_t target) {
+__device__ __forceinline__ bool wait_flag(const uint32_t *flag, uint32_t target, long long limit) {
   if (ld_relaxed(flag) < target) {
     const long long t0 = clock64();
     while (ld_relaxed(flag) < target) {
-      if (clock64() - t0 > ptx::kWaitCycles) return false;
+      if (clock64() - t0 > limit) return false;
       __nanosleep(64);
     }
   }
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2];
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2], drain_bar;
   __shared__ uint32_t tmem_base_sh;
   __shared__ float ered[4][NR];
 
@@ -238,6 +242,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       ptx::mbar_init(&accf_bar[b], 1);
       ptx::mbar_init(&acce_bar[b], kEpiWarps);
     }
+    ptx::mbar_init(&drain_bar, 1);
     ptx::fence_mbar_init();
     for (int a = 0; a < C::kAParts; ++a) ptx::prefetch_tmap(&p.tmA[a]);
     for (int b = 0; b < C::kBParts; ++b) {
@@ -263,6 +268,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
     // lane that gives up on a wait never strands the rest.
     uint32_t g = 0;  // chunks issued so far (the MMA lane counts identically)
     int pre = 0;     // chunks of the coming step whose J part is already in flight
+    uint32_t armed = 0;  // stage uses whose barrier lane 0 has armed (loads in flight or landed)
     for (int ls = 0; ls < nsteps && ok; ++ls) {
       const int buf = (p.buf0 + ls) & 1;
       int ready = ls == 0 ? p.n_mtiles : 0;  // units of this column known to have published V(ls)
@@ -271,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         if (kx / kBM >= ready) {
           // poll the next 32 units of the column at once (one L2 round trip for all of them)
           const int u = ready + lane;
-          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls) : true;
+          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls, p.wait_cycles) : true;
           if (!__all_sync(0xffffffffu, fl)) ok = false;
           ready = ready + 32 < p.n_mtiles ? ready + 32 : p.n_mtiles;
           ptx::fence_proxy_async_global();
@@ -282,13 +288,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           uint8_t *st = smem + s * kStage;
           bool issue = true;
           if (kc >= pre) {
-            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1, p.wait_cycles)) {
               ok = false;
               issue = false;
             } else {
               ptx::mbar_arrive_expect_tx(&full_bar[s], kTx);
               for (int a = 0; a < C::kAParts; ++a)
                 ptx::tma_load_2d(st + a * kATile, &p.tmA[a], kx, m0, &full_bar[s]);
+              armed = g + 1;
             }
           }
           if (issue)
@@ -305,7 +312,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           const uint32_t gg = g + kc;
           const int s = gg % STAGES;
           const uint32_t use = gg / STAGES;
-          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+          if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1, p.wait_cycles)) {
             ok = false;
             break;
           }
@@ -313,11 +320,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           for (int a = 0; a < C::kAParts; ++a)
             ptx::tma_load_2d(smem + s * kStage + a * kATile, &p.tmA[a], kc * (kChunkBytes / C::kElem), m0,
                              &full_bar[s]);
+          armed = gg + 1;
           ++pre;
         }
       }
       pre = __shfl_sync(0xffffffffu, pre, 0);
       ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    }
+    if (!ok && lane == 0) {
+      // a wait gave up: let the copies this CTA started land before it exits (each stage's last
+      // armed use; a use whose J part alone was started never completes its phase, and the
+      // bounded wait then outlasts those loads)
+      for (int s = 0; s < STAGES; ++s)
+        if (armed > (uint32_t)s) ptx::mbar_wait(&full_bar[s], ((armed - 1 - s) / STAGES) & 1, p.wait_cycles);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -326,12 +341,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       for (int ls = 0; ls < nsteps && ok; ++ls) {
         const int ab = ls & 1;
         const uint32_t t_acc = tmem + ab * NR;
-        if (ls >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((ls >> 1) - 1) & 1)) { ok = false; break; }
+        if (ls >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((ls >> 1) - 1) & 1, p.wait_cycles)) { ok = false; break; }
         ptx::tc_fence_after();
         for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
           const int s = g % STAGES;
           const uint32_t use = g / STAGES;
-          if (!ptx::mbar_wait(&full_bar[s], use & 1)) { ok = false; break; }
+          if (!ptx::mbar_wait(&full_bar[s], use & 1, p.wait_cycles)) { ok = false; break; }
           ptx::tc_fence_after();
           const uint32_t sa = ptx::smem_u32(smem + s * kStage);
           const uint32_t sb = sa + C::kAParts * kATile;
@@ -356,7 +371,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
           }
           ptx::mma_commit(&empty_bar[s]);
         }
+        if (!ok) break;
         ptx::mma_commit(&accf_bar[ab]);
+      }
+      if (!ok) {
+        // a wait gave up: the MMAs already issued finish before TMEM is freed
+        ptx::mma_commit(&drain_bar);
+        ptx::mbar_wait(&drain_bar, 0, p.wait_cycles);
       }
     }
   } else {
@@ -429,7 +450,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       const int buf = (p.buf0 + ls) & 1;
       const int ab = ls & 1;
       const uint32_t t_acc = tmem + ab * NR;
-      const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1);
+      const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1, p.wait_cycles);
       if (!epi_all(got)) { ok = false; break; }
       ptx::tc_fence_after();
       // the schedule value was fetched one step ahead (a global load on the critical path otherwise)
@@ -534,7 +555,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         }
         ptx::fence_proxy_async_global();
         __threadfence();
-        if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status))
+        if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status) &&
+            !((int)blockIdx.x == p.skip_unit && ls == p.skip_step))
           st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
       }
       // NMFA: the next stage's noise, while the column's units finish this sweep and the next

@@ -309,6 +309,8 @@ _SIGS = {
     "sb_batch_destroy": (C.c_int, [C.c_void_p]),
     "sb_solve_batch": (C.c_int, [C.c_void_p, C.POINTER(ProblemStruct), C.c_int32, C.POINTER(Params),
                                  C.POINTER(ResultStruct)]),
+    "sb_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64]),
+    "sb_debug_skip_publish": (C.c_int, [C.c_void_p, C.c_int32]),
     "sb_dsb_solve_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -655,6 +657,14 @@ class Context:
 
     def cancel(self, ticket: int) -> None:
         _check(lib().sb_cancel(self.h, ticket), self.h)
+
+    def set_wait_limit(self, cycles: int) -> None:
+        """Limit of every bounded wait in the tensor-core kernels, in SM clock cycles (0: default)."""
+        _check(lib().sb_set_wait_limit(self.h, cycles), self.h)
+
+    def debug_skip_publish(self, step: int) -> None:
+        """Test hook: the next tensor-core solve runs with unit 0 leaving out its step `step` flag."""
+        _check(lib().sb_debug_skip_publish(self.h, step), self.h)
 
     def serving_stats(self) -> dict:
         s = ServingStats()

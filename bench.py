@@ -1,23 +1,31 @@
 """Benchmark: SB spin-updates/s on the batched dSB workload (and the other workloads on request).
 
 Default workload (one GB300): complete graph N = 2000 with J_ij iid in {-1, +1}, R = 1024
-replicas, 2000 SB steps, dSB with the field J*sign(x) on the tensor cores (FP8 E4M3 operands,
-FP32 accumulation, bit-exact), x and y in FP32. One bench "step" is one full solve (init, 2000 SB
-steps, final energies, best spins back to the host).
+replicas, 2000 SB steps, dSB with the field J*sign(x) on the tensor cores (packed E2M1 operands,
+FP32 accumulation, bit-exact; FP8 E4M3 with --operand fp8), x and y in FP32. One bench "step" is
+one full solve (init, 2000 SB steps, final energies, best spins back to the host).
 
   value  spin-updates/s = N * R * sb_steps / solve time, J resident in HBM (sb_plan_run), device
          time from CUDA events on the solver's stream; L2 is flushed (256 MB write) between solves
-  e2e    the same metric through sb_solve from pinned host memory: H2D of J and D2H of the
-         results inside the timed region
+  e2e    the same metric through the public call a user makes: sb_problem_wrap of pinned host
+         memory (its O(N^2) coupling scan decides the operand type and c0) and sb_solve (H2D of J,
+         the solve, D2H of the results), all inside the timed region
   roofline  the persistent tensor-core kernel: algorithmic FLOPs (2 N^2 R per SB step) per launch
-         over its event-timed launch duration, against 2x the measured dense BF16 peak (FP8 rate)
+         over its event-timed launch duration, against the E2M1 rate (6 x the measured dense BF16
+         burst, the nominal 13.5 / 2.25 ratio; 2 x for FP8), and as a fraction of the BF16 burst
+  latency  a bounded serving run after the timed region: Poisson requests of the serving
+         workload's distribution through sb_submit / sb_poll, p50 / p99 latency and served rate
   cpu_baseline  the multithreaded FP32 CPU port of the same step loop (oracle/sb_cpu_baseline.c)
          on this host's cores, on a bounded sample of the workload
 
 Multi-GPU: the path shards by replicas / instances only; each rank runs its own solve (weak
 scaling) and the value is the total over ranks divided by the slowest rank's time.
 `--impl reference` times the CPU port of the reference step loop (the reference has no CPU
-implementation of its own) on the same workload and prints its line.
+implementation of its own) on the same workload and prints its line; each bench step is a bounded
+sample (its wall time is the line's ms_per_step, its SB steps config.sb_steps_timed). The line also
+carries the reference SB program itself on the GPU (its kernels compiled from its sources by
+oracle/build_ref.py, with cuBLAS SGEMV for the field, as m2_opt.cu runs them), untimed by the
+line's value.
 """
 from __future__ import annotations
 
@@ -195,6 +203,33 @@ def cpu_sample(name, J, h, budget_s=12.0, threads=None, max_steps=None):
             "seconds": dt, "steps": k}
 
 
+def reference_gpu_plain(sb_steps=1000):
+    """The reference SB program on this GPU, as the plain method: m2_opt.cu's kernels (compiled from
+    its sources into oracle/_ref/m2_opt.cubin by oracle/build_ref.py) and cuBLAS SGEMV, driven as its
+    main loop does (m2_opt.cu:152-187) on the default instance (2000 spins, padded to its N = 2048,
+    one trial = one replica). Returns None when the cubin was not built (no reference checkout)."""
+    from annealing_gb300 import instances
+    from oracle import ref_gpu
+
+    if not os.path.exists(ref_gpu.M2OPT_CUBIN):
+        return None
+    spins, N = 2000, 2048
+    Jh = np.zeros((N, N), np.float32)
+    Jh[:spins, :spins] = instances.complete_pm1(spins, seed=1234)
+    ref = ref_gpu.M2opt(Jh)
+    try:
+        prog_ms, dev_ms = ref.time_steps(sb_steps)
+    finally:
+        ref.close()
+    return {"instance": f"complete +-1 graph, {spins} spins (the program's N = {N}, zero padding), 1 replica, "
+                        f"{sb_steps} SB steps (aSB, the reference's update)",
+            "ms_per_sb_step_as_program": prog_ms, "ms_per_sb_step_device_only": dev_ms,
+            "spin_updates_per_s_as_program": spins / (prog_ms * 1e-3),
+            "spin_updates_per_s_device_only": spins / (dev_ms * 1e-3),
+            "note": "as_program: an event pair and an event synchronize around every step, as m2_opt.cu:159-185 "
+                    "(host wall time); device_only: the same launches back to back under one event pair"}
+
+
 def run_reference(args, rank, world):
     """The CPU port of the reference step loop, timed per bench step on a bounded sample."""
     if rank != 0:
@@ -205,29 +240,41 @@ def run_reference(args, rank, world):
         return run_reference_nmfa(args, world)
     J, h = make_problem(args.workload)
     variant, n, R, steps, field, desc = WORKLOADS[args.workload]
-    budget = args.cpu_budget or max(2.0, min(12.0, 60.0 / max(1, args.steps + args.warmup)))
+    budget = args.cpu_budget or max(1.0, min(12.0, 40.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_sample(args.workload, J, h, budget_s=budget / 4)
-    vals, samples = [], []
+    samples = []
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        s = cpu_sample(args.workload, J, h, budget_s=budget)
-        vals.append(s["value"])
-        samples.append(s)
-    value = float(statistics.median(vals))
-    ms_per_step = 1e3 * n * R * steps / value  # time for one full solve at this rate
+        samples.append(cpu_sample(args.workload, J, h, budget_s=budget))
+    wall = time.perf_counter() - t0
+    value = float(sum(n * R * s["steps"] for s in samples) / sum(s["seconds"] for s in samples))
     line = {
         "impl": "reference", "metric": "SB spin-updates/s", "value": value, "unit": "spin-updates/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        # the wall time of one timed bench step: one bounded sample of the workload
+        "ms_per_step": 1e3 * sum(s["seconds"] for s in samples) / len(samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": desc, "n": n, "replicas": R, "sb_steps": steps},
+        "data": "synthetic",
+        "config": {"workload": desc, "n": n, "replicas": R, "sb_steps": steps, "variant": variant,
+                   "field": "f32", "parallelism": f"replicas-only x{world}",
+                   "l2": "host CPU (no device caches)",
+                   "sb_steps_timed": int(statistics.median(s["steps"] for s in samples))},
         "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": samples[0]["cores"],
                          "kind": "port", "sample": samples[0]["sample"]},
         "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "timed_wall_s": wall,
         "note": "the reference ships no CPU implementation of the SB step loop; this is the C port "
                 "of its loop (UpdateTwice + dense matrix-vector field, and the bSB/dSB update) with "
-                "POSIX threads, each bench step a bounded sample of the workload",
+                "POSIX threads; each bench step is a bounded sample of the workload (all replicas, "
+                "config.sb_steps_timed SB steps), value = the samples' spin-updates over their time",
     }
+    if variant == "dsb" and not args.no_reference_gpu:
+        try:
+            line["reference_gpu_plain"] = reference_gpu_plain()
+        except Exception as exc:  # the GPU leg is informational; the CPU line stands
+            line["reference_gpu_plain"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
 
 
@@ -355,19 +402,23 @@ def run_ours(args, rank, world, local_rank):
                 "traffic_source": traffic[1], "kernel": kernel, "launch_ms": rp.kernel_ms_avg,
                 "sb_steps_per_launch": spl, "peak_source": f"{src} HBM copy", "note": note}
 
-    # ---- e2e: host buffers through sb_solve ----
+    # ---- e2e: host buffers through the public calls: sb_problem_wrap (the coupling scan that
+    # decides the operand type and c0) and sb_solve (H2D of J, the solve, D2H of the results) ----
     Jp = torch.from_numpy(J).pin_memory()
     hp = torch.from_numpy(h).pin_memory() if h is not None else None
-    pw = sb.Problem.wrap(n, Jp.data_ptr(), hp.data_ptr() if hp is not None else 0, keepalive=(Jp, hp))
+
+    def wrap():
+        return sb.Problem.wrap(n, Jp.data_ptr(), hp.data_ptr() if hp is not None else 0, keepalive=(Jp, hp))
+
     for k in range(max(1, args.warmup)):
-        ctx.solve(pw, prm)
+        ctx.solve(wrap(), prm)
     barrier()
     e2e_ms = []
     for k in range(args.steps):
         flush.fill_(float(k))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        r = ctx.solve(pw, prm)  # H2D of J, solve, D2H of spins / energies; returns when done
+        r = ctx.solve(wrap(), prm)  # scan, H2D of J, solve, D2H of spins / energies; returns when done
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_total = reduce_max(float(sum(e2e_ms)), world)
     e2e_value = weak_scaling_value(float(n) * R * sb_steps, world, args.steps, e2e_total)
@@ -391,9 +442,11 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": desc, "n": n, "replicas": R, "sb_steps": sb_steps,
                    "variant": variant, "field": results[0].field_dtype,
                    "parallelism": f"replicas-only x{world}",
-                   "l2": "flushed between timed solves (256 MB write outside the timed events)"},
+                   "l2": "flushed between timed solves (256 MB write outside the timed events)",
+                   "sb_steps_timed": sb_steps},
         "e2e": {"value": e2e_value, "unit": "spin-updates/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_total / args.steps},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_total / args.steps,
+                "includes": "sb_problem_wrap of pinned host J (coupling scan), sb_solve (H2D, solve, D2H)"},
         "gpu_launches": int(launches),
         "roofline": roof,
         "clocks": clk.summary(),
@@ -408,8 +461,20 @@ def run_ours(args, rank, world, local_rank):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(args.workload, J, h).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
-    print(json.dumps(line), flush=True)
     plan.close()
+    if args.workload == "batched-dsb" and world == 1 and not args.no_latency:
+        # latency: a bounded run of the serving workload's request stream, after the timed region
+        lat_ctx = sb.Context(local_rank)
+        try:
+            out = serve_stream(sb, lat_ctx, count=200, rate=200.0, pool_size=16, R=32, seed=4321,
+                               device=local_rank, warmup=2)
+            line["latency"] = {k: v for k, v in out.items() if not k.startswith("_")}
+            line["latency"]["workload"] = ("serving stream, bounded: 200 Poisson requests at 200/s, N log-uniform "
+                                           "in [128,16384], density ~ U[0.01,1], J ~ U{-8..8}, R=32, step budget "
+                                           "~ U[500,4000]; couplings from a pool of 16 distinct instances")
+        finally:
+            lat_ctx.close()
+    print(json.dumps(line), flush=True)
     ctx.close()
 
 
@@ -491,12 +556,20 @@ def run_batch(args, rank, world, local_rank):
             "kernel": "grouped_kernel (one launch per SB step)",
             "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
             "peak_source": f"{src} HBM copy"}
-    # e2e: sb_solve_batch from host buffers every step (upload, convert, run, results back)
+    # e2e: from host couplings every step through the public calls: sb_problem_wrap of each
+    # instance (its coupling scan), then the batch (upload, convert, run, results back)
+    import ctypes
+
+    def addr(ptr):
+        return ctypes.cast(ptr, ctypes.c_void_p).value or 0
+
+    host = [(p.n, addr(p.s.J), addr(p.s.h)) for p in probs]
     e2e_ms = []
     for k in range(args.steps):
         torch.cuda.synchronize(dev)
         t1 = time.perf_counter()
-        ctx.batch(probs, prm).run(seed=200 + k)
+        wrapped = [sb.Problem.wrap(n_, j_, h_, keepalive=probs) for n_, j_, h_ in host]
+        ctx.batch(wrapped, prm).run(seed=200 + k)
         e2e_ms.append(1e3 * (time.perf_counter() - t1))
     e2e_total = reduce_max(float(sum(e2e_ms)), world)
     if rank != 0:
@@ -514,41 +587,43 @@ def run_batch(args, rank, world, local_rank):
         "e2e": {"value": world * updates * args.steps / (e2e_total * 1e-3), "unit": "spin-updates/s",
                 "h2d_bytes_per_step": int(np_kp),  # couplings packed on the host, then copied
                 "d2h_bytes_per_step": int(sum(p.n + 8 * R for p in probs)),
-                "ms_per_step": e2e_total / args.steps},
+                "ms_per_step": e2e_total / args.steps,
+                "includes": "sb_problem_wrap of every instance's host couplings (coupling scan), batch "
+                            "creation (packing, upload), the run, results back"},
         "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary(),
         "quality": {"energy_check_ok": all(quality)}, "setup_s": setup_s,
     }
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args, rank, world, local_rank):
+def serve_stream(sb, ctx, count, rate, pool_size, R, seed, device, warmup=2):
+    """The serving workload's request stream through sb_submit / sb_poll: Poisson arrivals at
+    `rate`, N log-uniform in [128, 16384], density U[0.01, 1], J ~ U{-8..8}, R replicas, step budget
+    U[500, 4000]. A pool of distinct instances drawn from the same size distribution stands in for
+    the couplings (each request takes the pool instance nearest its own N), which keeps host memory
+    bounded. Latency = submit to result (the library's per-request total_ms). The stream's HBM
+    fraction counts the algorithmic bytes the resident requests' steps read and write (FP8 couplings
+    Np x Kp per step, x and y read and written and the next sign operand, 17 B per spin and replica)
+    over the worker's busy time."""
     import threading as th
 
-    import torch
-
-    import annealing_gb300 as sb
     from annealing_gb300 import instances
 
-    torch.cuda.set_device(local_rank)
-    variant, _, R, _, field, desc = WORKLOADS[args.workload]
-    count = args.requests
-    stream = instances.serving_stream(count=count, seed=1234 + rank)
-    # a pool of distinct instances drawn from the request-size distribution; each request takes
-    # the pool instance nearest its own N (the pool keeps host memory bounded)
+    stream = instances.serving_stream(count=count, rate=rate, seed=seed)
     rng = np.random.default_rng(99)
-    pool_n = sorted(set(int(v) for v in np.exp(rng.uniform(np.log(128), np.log(16384), size=args.pool))))
+    pool_n = sorted(set(int(v) for v in np.exp(rng.uniform(np.log(128), np.log(16384), size=pool_size))))
     pool = [sb.Problem.random(n, float(rng.uniform(0.01, 1.0)), 8, 0, seed=5000 + i) for i, n in enumerate(pool_n)]
     pool_arr = np.array(pool_n)
-    ctx = sb.Context(local_rank)
     # warm-up: a few requests through the server (kernels, allocator)
-    for k in range(args.warmup):
+    for k in range(warmup):
         p = pool[0]
         prm = sb.Params.default(sb.DSB, steps=100, replicas=R, seed=k, field_mode=sb.FIELD_TC)
         ctx.poll(ctx.submit(p, prm), p.n, prm, wait_ms=-1)
+    stats0 = ctx.serving_stats()
     reqs = []
-    for (arr, n, dens, steps, seed) in stream:
+    for (arr, n, dens, steps, sd) in stream:
         i = int(np.argmin(np.abs(pool_arr - n)))
-        reqs.append((arr, pool[i], sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed,
+        reqs.append((arr, pool[i], sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=sd,
                                                      field_mode=sb.FIELD_TC)))
     tickets = [None] * len(reqs)
     t_start = time.perf_counter()
@@ -560,36 +635,75 @@ def run_serving(args, rank, world, local_rank):
                 time.sleep(arr - now)
             tickets[k] = ctx.submit(p, prm)
 
-    with ClockSampler(local_rank) as clk:
+    with ClockSampler(device) as clk:
         pt = th.Thread(target=producer)
         pt.start()
         results = [None] * len(reqs)
+        done_at = np.zeros(len(reqs))
         for k in range(len(reqs)):
             while tickets[k] is None:
                 time.sleep(0.001)
             arr, p, prm = reqs[k]
             results[k] = ctx.poll(tickets[k], p.n, prm, wait_ms=-1)
+            done_at[k] = time.perf_counter() - t_start
         pt.join()
         makespan = time.perf_counter() - t_start
     lat = np.array([r.total_ms for r in results])
     updates = float(sum(p.n * R * prm.steps for _, p, prm in reqs))
     stats = ctx.serving_stats()
+    busy_ms = stats["busy_ms"] - stats0["busy_ms"]
+    algo_bytes = float(sum((((p.n + 127) // 128 * 128) ** 2 + 17.0 * p.n * R) * prm.steps for _, p, prm in reqs))
+    hbm, _, src = peaks()
+    span = reqs[-1][0]
+    # a queue that keeps up finishes the last request about one latency after its arrival; a
+    # growing queue shows as latency rising along the stream
+    half = len(reqs) // 2
+    return {"requests": len(reqs), "offered_rate_per_s": rate, "arrival_span_s": span,
+            "served_rate_per_s": len(reqs) / makespan, "makespan_s": makespan,
+            "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "p50_ms_first_half": float(np.percentile(lat[:half], 50)),
+            "p50_ms_second_half": float(np.percentile(lat[half:], 50)),
+            "spin_updates_per_s": updates / makespan, "busy_ms": busy_ms,
+            "admit_ms": stats["admit_ms"] - stats0["admit_ms"],
+            "hbm_fraction": (algo_bytes / (busy_ms * 1e-3) / 1e9) / hbm if busy_ms > 0 else None,
+            "hbm_bytes": algo_bytes, "peak_source": f"{src} HBM copy",
+            "pool_instances": len(pool), "replicas": R,
+            "energy_check_ok": all(r.energy_check_ok for r in results), "clocks": clk.summary(),
+            "_updates": updates, "_results": results, "_reqs": reqs, "_stats": stats}
+
+
+def run_serving(args, rank, world, local_rank):
+    import torch
+
+    import annealing_gb300 as sb
+
+    torch.cuda.set_device(local_rank)
+    variant, _, R, _, field, desc = WORKLOADS[args.workload]
+    ctx = sb.Context(local_rank)
+    out = serve_stream(sb, ctx, count=args.requests, rate=args.rate, pool_size=args.pool, R=R, seed=1234 + rank,
+                       device=local_rank, warmup=args.warmup)
+    reqs, results, updates, stats = out.pop("_reqs"), out.pop("_results"), out.pop("_updates"), out.pop("_stats")
+    makespan = out["makespan_s"]
     if rank != 0:
+        ctx.close()
         return
+    if args.rate != 200.0:
+        desc = desc.replace("at 200/s", f"at {args.rate:g}/s")
     line = {
         "metric": "SB spin-updates/s (serving stream)", "value": updates / makespan,
         "unit": "spin-updates/s", "n_gpus": world, "steps": len(reqs), "warmup": args.warmup,
         "ms_per_step": 1e3 * makespan / len(reqs), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp8e4m3 field (f32 accumulate), f32 state",
         "data": "synthetic (seeded Poisson stream; sizes from a pool of distinct instances)",
-        "config": {"workload": desc, "requests": len(reqs), "rate_per_s": 200.0,
-                   "pool_instances": len(pool), "replicas": R},
-        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
-                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
-        "makespan_s": makespan, "arrival_span_s": reqs[-1][0],
+        "config": {"workload": desc, "requests": len(reqs), "rate_per_s": args.rate,
+                   "pool_instances": out["pool_instances"], "replicas": R},
+        "latency_ms": {"p50": out["p50_ms"], "p90": out["p90_ms"], "p99": out["p99_ms"], "max": out["max_ms"]},
+        "latency": {k: v for k, v in out.items() if k != "clocks"},
+        "makespan_s": makespan, "arrival_span_s": out["arrival_span_s"],
         "requests_per_s": len(reqs) / makespan, "serving": stats,
-        "quality": {"energy_check_ok": all(r.energy_check_ok for r in results)},
-        "clocks": clk.summary(),
+        "quality": {"energy_check_ok": out["energy_check_ok"]},
+        "clocks": out["clocks"],
         "e2e": {"value": updates / makespan, "unit": "spin-updates/s",
                 # couplings packed to FP8 on the host before the copy
                 "h2d_bytes_per_step": int(np.mean([((p.n + 127) // 128 * 128) ** 2 for _, p, _ in reqs])),
@@ -631,17 +745,19 @@ def run_reference_sqa(args, world):
         sqa_cpu_sample(J, SQA_TROTTER, budget_s=budget / 4)
     samples = [sqa_cpu_sample(J, SQA_TROTTER, budget_s=budget) for _ in range(args.steps)]
     value = float(statistics.median(s["value"] for s in samples))
-    updates = float(R) * SQA_TROTTER * (n + SQA_TROTTER - 1) * steps
     line = {
         "impl": "reference", "metric": "SQA spin-updates/s", "value": value, "unit": "spin-updates/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * updates / value,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(s["seconds"] for s in samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int",
         "data": "synthetic", "config": {"workload": desc, "n": n, "trotter": SQA_TROTTER, "replicas": R,
-                                        "anneal_steps": steps},
+                                        "anneal_steps": steps, "rng": "hash", "parallelism": f"replicas-only x{world}",
+                                        "l2": "host CPU (no device caches)"},
         "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": 1, "kind": "port",
                          "sample": samples[0]["sample"]},
         "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the C restatement of pre_calculate.cu's wavefront (oracle/sqa_oracle.c), one thread",
+        "note": "the C restatement of pre_calculate.cu's wavefront (oracle/sqa_oracle.c), one thread; each "
+                "bench step is a bounded sample (whole annealing steps of one replica)",
     }
     print(json.dumps(line), flush=True)
 
@@ -745,18 +861,48 @@ def run_reference_nmfa(args, world):
         nmfa_cpu_sample(J, budget_s=budget / 4)
     samples = [nmfa_cpu_sample(J, budget_s=budget) for _ in range(args.steps)]
     value = float(statistics.median(s["value"] for s in samples))
-    updates = float(n) * R * 2 * stages
     line = {
         "impl": "reference", "metric": "NMFA spin-updates/s", "value": value, "unit": "spin-updates/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * updates / value,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(s["seconds"] for s in samples),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": desc, "n": n, "samples": R, "stages": stages},
+        "data": "synthetic", "config": {"workload": desc, "n": n, "samples": R, "stages": stages,
+                                        "sweeps_per_stage": 2, "parallelism": f"samples-only x{world}",
+                                        "l2": "host CPU (no device caches)"},
         "cpu_baseline": {"value": value, "unit": "spin-updates/s", "cores": 1, "kind": "port",
                          "sample": samples[0]["sample"]},
         "e2e": {"value": value, "unit": "spin-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the C restatement of NMFA/CUDA_GPU/src/nmfa.cu (oracle/nmfa_oracle.c), one thread",
+        "note": "the C restatement of NMFA/CUDA_GPU/src/nmfa.cu (oracle/nmfa_oracle.c), one thread; each "
+                "bench step is a bounded sample (whole anneals of one sample)",
     }
+    if not args.no_reference_gpu:
+        try:
+            line["reference_gpu_kernel"] = reference_gpu_nmfa(J, R, stages)
+        except Exception as exc:  # the GPU leg is informational; the CPU line stands
+            line["reference_gpu_kernel"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_nmfa(J, samples, stages):
+    """The reference NMFA kernel on this GPU (gpu_nmfa_kernel of NMFA/CUDA_GPU/src/nmfa.cu, compiled
+    from its sources into oracle/_ref/nmfa_states_n{N}.cubin by oracle/build_ref.py), launched as
+    gpu_nmfa does on the workload's instance and schedule: event time of the one launch, best of 3.
+    Returns None when the cubin was not built."""
+    from oracle import ref_gpu
+
+    n = J.shape[0]
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", f"nmfa_states_n{n}.cubin")):
+        return None
+    k = ref_gpu.NmfaKernel(n)
+    betas = ref_gpu.nmfa_schedule(stages)
+    try:
+        k.run(J, betas, 8)  # warm-up
+        ms = min(k.run(J, betas, samples, timed=True)[1] for _ in range(3))
+    finally:
+        k.close()
+    return {"samples": samples, "stages": stages, "ms_per_anneal": ms,
+            "spin_updates_per_s": float(n) * samples * 2 * stages / (ms * 1e-3),
+            "note": "one launch anneals every sample (one CTA of N threads each); event-timed, best of 3"}
 
 
 def run_nmfa(args, rank, world, local_rank):
@@ -856,6 +1002,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched-dsb")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip the reference program's GPU timing")
+    ap.add_argument("--no-latency", action="store_true",
+                    help="default workload: skip the bounded serving run that reports latency")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving workload: offered requests per second")
     ap.add_argument("--requests", type=int, default=2000, help="serving workload: stream length")
     ap.add_argument("--cpu-budget", type=float, default=0.0,
                     help="seconds of CPU work per reference-arm step (default: fit the run in ~1 min)")

@@ -259,6 +259,18 @@ sb_status sb_time_to_target(const double *energies, const double *times_ms, int3
 sb_status sb_create(sb_ctx **out, const sb_device_opts *opts);
 sb_status sb_destroy(sb_ctx *ctx);
 const char *sb_last_error(sb_ctx *ctx);
+/* Bounded device waits. Every wait inside the persistent tensor-core kernels (a dataflow flag of
+ * another unit, an mbarrier of a copy or a contraction) gives up after `cycles` SM clock cycles;
+ * the kernel then lets the copies and contractions it started finish, frees its tensor memory,
+ * returns, and the call returns SB_ERR_TIMEOUT with the context still usable. 0 restores the
+ * default (2e9 cycles, about one second at the maximum SM clock). Replaces the reference's
+ * gpuErrchk, which ends the program on any CUDA error (m2_opt.cu:24-36). */
+sb_status sb_set_wait_limit(sb_ctx *ctx, int64_t cycles);
+/* Test hook for the timeout path above, a host-side fault injection: the next tensor-core solve of
+ * this context runs with unit 0 (spins 0..127 of the first replica tile) leaving out its
+ * published flag of SB step `step`, so the units of its replica column wait for a flag that
+ * nothing sets and give up at the wait limit. Nothing faults; no counterpart in the reference. */
+sb_status sb_debug_skip_publish(sb_ctx *ctx, int32_t step);
 
 /* One blocking solve from host buffers: upload J, run, copy results back. */
 sb_status sb_solve(sb_ctx *ctx, const sb_problem *p, const sb_params *params, sb_result *res);
@@ -366,13 +378,16 @@ sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *p, const sb_sqa_params *pa
  * device memory budget (and hands out buffers from its own pool), or that must not pay the
  * implicit synchronisation, latency or out-of-memory risk of cudaMalloc / cudaFree in the middle
  * of its work. It runs the same solve as sb_solve with variant SB_DSB on the tensor-core path
- * with FP8 operands (uniform initial state from `seed`, schedule a(t) = a0 t / steps), on device
- * buffers the caller owns: d_J [n*n] row-major (symmetric, zero diagonal, integers |J| <= 16),
- * d_h [n] or NULL, outputs d_x, d_y [replicas*n] (final state, replica-major) and
- * d_energies [replicas] (final energies), all on `stream` (a cudaStream_t, NULL = legacy default
- * stream) of the current device. c0 must be given (> 0; sb_default_c0 on the host problem gives
- * the usual value). The call returns when the work has finished.
- * Scratch is one fixed array of 8,455,168 bytes in the library's device memory, held by every GPU
+ * (packed E2M1 operands when every coupling is an integer with |J| <= 4 and the shape fits the
+ * kernel that keeps J in shared memory, else FP8; the same bits either way), with a uniform initial
+ * state from `seed` and the schedule a(t) = a0 t / steps, on device buffers the caller owns:
+ * d_J [n*n] row-major (symmetric, zero diagonal, integers |J| <= 16), d_h [n] or NULL, outputs
+ * d_x, d_y [replicas*n] (final state, replica-major) and d_energies [replicas] (final energies),
+ * all on `stream` (a cudaStream_t, NULL = legacy default stream) of the current device. c0 must be
+ * given (> 0; sb_default_c0 on the host problem gives the usual value). The call is synchronous:
+ * it waits for `stream` once after scanning the couplings (other couplings return
+ * SB_ERR_UNSUPPORTED before any step runs) and again when the solve has finished.
+ * Scratch is one fixed array of 8,458,240 bytes in the library's device memory, held by every GPU
  * that loads the library until the process exits; hence the limits n <= 2048, replicas <= 1024,
  * steps <= 16384 (larger sizes return SB_ERR_INVALID_ARG). The first call on a device looks up
  * the array's device address; make that first call before any stream capture. All calls share the

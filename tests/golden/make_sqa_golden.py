@@ -103,4 +103,6 @@ def main(out_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "gpurun_out/golden")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <out_dir>")
+    main(sys.argv[1])
