@@ -18,7 +18,8 @@
 //     accumulator, x and y with tcgen05.ld, apply the SB update with the exact operation order of
 //     the CPU oracle, write x and y back to TMEM and the next step's operand V (sign as FP8/BF16,
 //     or x as BF16 hi + lo) to global memory; the accumulator is double-buffered in TMEM so the
-//     next contraction can start while the epilogue drains;
+//     next contraction can start while the epilogue drains (split operands instead accumulate K in
+//     segments, each folded by the epilogue into an FP32 sum rounded to nearest);
 //   * steps are ordered by per-unit release/acquire flags instead of a grid barrier: a unit
 //     publishes its V(t+1) chunk and the units of its replica column wait only for the chunks they
 //     load (bounded spins).
@@ -31,6 +32,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -278,6 +280,13 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
   g.n_rtiles = e->n_rtiles;
   g.k_chunks = (int)(rowe * elem / kChunkBytes);
   g.wait_cycles = ptx::kWaitCycles;
+  // split operands: 8 chunks (512 spins of K) per accumulation segment; SB_SPLIT_SEG_CHUNKS
+  // overrides it (shorter segments take fewer roundings each and cost more hand-offs)
+  g.seg_chunks = 8;
+  if (const char *sc = getenv("SB_SPLIT_SEG_CHUNKS")) {
+    const int v = atoi(sc);
+    if (v > 0) g.seg_chunks = v;
+  }
   g.skip_unit = -1;
   g.skip_step = -1;
   for (int m = 0; m < 3; ++m)

@@ -18,7 +18,8 @@
 //     accumulator, x and y with tcgen05.ld, apply the SB update with the exact operation order of
 //     the CPU oracle, write x and y back to TMEM and the next step's operand V (sign as FP8/BF16,
 //     or x as BF16 hi + lo) to global memory; the accumulator is double-buffered in TMEM so the
-//     next contraction can start while the epilogue drains;
+//     next contraction can start while the epilogue drains (split operands instead accumulate K in
+//     segments, each folded by the epilogue into an FP32 sum rounded to nearest);
 //   * steps are ordered by per-unit release/acquire flags instead of a grid barrier: a unit
 //     publishes its V(t+1) chunk and the units of its replica column wait only for the chunks they
 //     load (bounded spins).
@@ -73,6 +74,7 @@ struct alignas(64) TcArgs {
   uint32_t *rng;           // NMFA: [5][R][xp] XORWOW words of each (sample, spin)
   float noise, keep, mix;  // NMFA: sigma, 1 - alpha, alpha
   long long wait_cycles;   // limit of every bounded wait (SM clock cycles)
+  int seg_chunks;          // split operands: K chunks per accumulation segment
   // host-side fault injection for the timeout path: unit skip_unit does not publish its flag(s)
   // of step skip_step (skip_step < 0: every unit publishes)
   int skip_unit, skip_step;
@@ -215,6 +217,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   constexpr uint32_t kCols = kUsedCols <= 32 ? 32 : (kUsedCols <= 64 ? 64 : (kUsedCols <= 128 ? 128 : (kUsedCols <= 256 ? 256 : 512)));
   constexpr uint32_t kIdesc = make_idesc(DT, kBM, NR);
   constexpr int kHalf = NR / 2;               // columns per epilogue warp
+  // Split couplings (BF16 hi + lo, real-valued J): the tensor core rounds the sum of each MMA into
+  // its FP32 accumulator toward zero, a bias that grows with the number of MMAs one accumulator
+  // takes and with its magnitude. So the contraction over K runs in segments of p.seg_chunks chunks,
+  // each into a fresh accumulator (column block 0), and the epilogue warps, idle during the
+  // contraction, load each finished segment (the MMA lane waits only for that load) and add it into
+  // a running FP32 sum (round to nearest; column block 1). x and y keep blocks 2 and 3.
+  constexpr bool kSeg = DT == kTcBf16Split;
   static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
   static_assert(4 * NR <= 512, "two accumulators + x + y must fit TMEM");
 
@@ -261,6 +270,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   // columns: accumulators [0, NR) and [NR, 2NR), x [2NR, 3NR), y [3NR, 4NR); NMFA with the noise
   // drawn ahead: z0 [4NR, 5NR), y1 [5NR, 6NR) (stage k's z1 in y for even k, in y1 for odd k)
   const uint32_t t_x = tmem + 2 * NR, t_y = tmem + 3 * NR, t_z0 = tmem + 4 * NR, t_y1 = tmem + 5 * NR;
+  const uint32_t t_sum = tmem + NR;  // split operands: the running sum of the segments
+  const int nseg = kSeg ? (p.k_chunks + p.seg_chunks - 1) / p.seg_chunks : 1;
 
   if (warp == 0) {
     // ---------------- TMA producer (lane 0 issues; the warp polls the column's flags) ----------------
@@ -338,12 +349,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
       uint32_t g = 0;
+      uint32_t gs = 0;  // split operands: segments issued
       for (int ls = 0; ls < nsteps && ok; ++ls) {
         const int ab = ls & 1;
-        const uint32_t t_acc = tmem + ab * NR;
-        if (ls >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((ls >> 1) - 1) & 1, p.wait_cycles)) { ok = false; break; }
-        ptx::tc_fence_after();
+        if constexpr (!kSeg) {
+          if (ls >= 2 && !ptx::mbar_wait(&acce_bar[ab], (uint32_t)((ls >> 1) - 1) & 1, p.wait_cycles)) { ok = false; break; }
+          ptx::tc_fence_after();
+        }
+        int kin = 0;  // chunk index inside the current segment
         for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
+          const uint32_t t_acc = tmem + (kSeg ? 0 : ab) * NR;
+          if (kSeg && kin == 0) {
+            // the segment block is free once the epilogue has loaded the previous segment
+            if (gs >= 1 && !ptx::mbar_wait_spin(&acce_bar[0], (uint32_t)(gs - 1) & 1, p.wait_cycles)) { ok = false; break; }
+            ptx::tc_fence_after();
+          }
           const int s = g % STAGES;
           const uint32_t use = g / STAGES;
           if (!ptx::mbar_wait(&full_bar[s], use & 1, p.wait_cycles)) { ok = false; break; }
@@ -360,7 +380,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
               for (int k = 0; k < C::kMmaPerChunk; ++k) {
                 const uint64_t ad = ptx::smem_desc_sw128(sa + a * kATile + k * 32);
                 const uint64_t bd = ptx::smem_desc_sw128(sb + b * kBTile + k * 32);
-                const uint32_t acc = (kc > 0 || prod > 0 || k > 0) ? 1u : 0u;
+                const uint32_t acc = ((kSeg ? kin : kc) > 0 || prod > 0 || k > 0) ? 1u : 0u;
                 if constexpr (DT == kTcFp8)
                   ptx::mma_f8(t_acc, ad, bd, kIdesc, acc);
                 else
@@ -370,9 +390,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             }
           }
           ptx::mma_commit(&empty_bar[s]);
+          if constexpr (kSeg) {
+            if (++kin == p.seg_chunks || kc + 1 == p.k_chunks) {
+              ptx::mma_commit(&accf_bar[0]);
+              ++gs;
+              kin = 0;
+            }
+          }
         }
         if (!ok) break;
-        ptx::mma_commit(&accf_bar[ab]);
+        if constexpr (!kSeg) ptx::mma_commit(&accf_bar[ab]);
       }
       if (!ok) {
         // a wait gave up: the MMAs already issued finish before TMEM is freed
@@ -445,13 +472,56 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
       if (nsteps > 0 && (p.t0 & 1) == 0) draw_stage(c_lo, c_lo + kHalf, ((p.t0 >> 1) & 1) ? t_y1 : t_y);
     }
     float pump_next = (!kEOnly && nsteps > 0) ? p.pumps[p.t0] : 0.0f;
+    uint32_t gs = 0;  // split operands: segments consumed
     for (int ls = 0; ls < nsteps; ++ls) {
       const int t = p.t0 + ls;
       const int buf = (p.buf0 + ls) & 1;
+      if constexpr (kSeg) {
+        // every segment, the step's last too: load it (then the MMA lane may start the next one into
+        // the same block, the next step's first included) and add it into the sum, which is the field
+        bool seg_ok = true;
+        for (int sg = 0; sg < nseg; ++sg, ++gs) {
+          const bool got_s = ptx::mbar_wait_spin(&accf_bar[0], gs & 1, p.wait_cycles);
+          if (!epi_all(got_s)) { seg_ok = false; break; }
+          ptx::tc_fence_after();
+          uint32_t va[kHalf];
+          if constexpr (kHalf == 64) {
+            ptx::tmem_ld64(tmem + lane_off + c_lo, *reinterpret_cast<uint32_t(*)[64]>(va));
+          } else {
+#pragma unroll
+            for (int i = 0; i < kHalf / 16; ++i)
+              ptx::tmem_ld16(tmem + lane_off + c_lo + 16 * i, *reinterpret_cast<uint32_t(*)[16]>(va + 16 * i));
+          }
+          ptx::tmem_ld_wait();
+          ptx::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&acce_bar[0]);
+#pragma unroll
+          for (int i = 0; i < kHalf / 16; ++i) {
+            uint32_t vs[16];
+            const uint32_t ts = t_sum + lane_off + c_lo + 16 * i;
+            if (sg > 0) {
+              ptx::tmem_ld16(ts, vs);
+              ptx::tmem_ld_wait();
+#pragma unroll
+              for (int j = 0; j < 16; ++j)
+                vs[j] = __float_as_uint(__fadd_rn(__uint_as_float(vs[j]), __uint_as_float(va[16 * i + j])));
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) vs[j] = va[16 * i + j];
+            }
+            ptx::tmem_st16(ts, vs);
+          }
+          ptx::tmem_st_wait();
+        }
+        if (!seg_ok) { ok = false; break; }
+      }
       const int ab = ls & 1;
-      const uint32_t t_acc = tmem + ab * NR;
-      const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1, p.wait_cycles);
-      if (!epi_all(got)) { ok = false; break; }
+      const uint32_t t_acc = kSeg ? t_sum : tmem + ab * NR;
+      if constexpr (!kSeg) {
+        const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(ls >> 1) & 1, p.wait_cycles);
+        if (!epi_all(got)) { ok = false; break; }
+      }
       ptx::tc_fence_after();
       // the schedule value was fetched one step ahead (a global load on the critical path otherwise)
       const float pump = pump_next;
@@ -540,10 +610,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         }
       }
       if constexpr (!kEOnly) ptx::tmem_st_wait();
-      // the accumulator may be overwritten from here on
+      // the accumulator may be overwritten from here on (split operands: released by the folds)
       ptx::tc_fence_before();
       __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(&acce_bar[ab]);
+      if (!kSeg && lane == 0) ptx::mbar_arrive(&acce_bar[ab]);
       // publish this unit's V(t+1) chunk to the replica column
       if constexpr (kStageV && !kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> TMA store
       epi_sync();

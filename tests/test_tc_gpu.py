@@ -161,43 +161,86 @@ def test_profile_reports_persistent_launch(ctx):
     assert r.steps_per_launch == 50 and r.kernel_ms_avg > 0
 
 
+def _fp64_bsb(torch, J, h, x0, y0, c0, K, dev):
+    """The published bSB update in FP64 on the GPU (J x in FP64), same initial state and schedule."""
+    Jd = torch.from_numpy(J).double().to(dev)
+    hd = torch.from_numpy(h).double().to(dev) if h is not None else 0.0
+    x = torch.from_numpy(x0).double().to(dev)
+    y = torch.from_numpy(y0).double().to(dev)
+    for t in range(K):
+        pump = float(sb.pump(1.0, t, K))
+        y = y + 1.25 * (-pump * x + c0 * (x @ Jd + hd))
+        x = x + 1.25 * y
+        wall = x.abs() > 1.0
+        x = torch.where(wall, torch.sign(x), x)
+        y = torch.where(wall, torch.zeros_like(y), y)
+    return x, y
+
+
+def test_split_field_error_unbiased_n1024():
+    """One bSB step from the uniform initial state (N=1024, J ~ N(0, 1/N), R=256): the field error of
+    the BF16 hi + lo path against FP64, read from y. The tensor core rounds each MMA's sum toward zero,
+    so a field accumulated in one FP32 accumulator is shrunk by a bias that dominates its error; the
+    kernel accumulates K in segments of 512 spins, each folded into an FP32 sum with round to nearest.
+    Stated bars: rms error <= 4e-7 (the hi + lo representation alone gives ~2e-7 here) and bias ratio
+    mean(dF sign F) / mean|dF| within +-0.45 (measured -0.32; -0.53 in one accumulator)."""
+    import torch
+
+    n, R, seed = 1024, 256, 3
+    J, h = instances.gaussian(n, seed=1234)
+    prob = sb.Problem.from_dense(J, h)
+    c0 = float(prob.default_c0())
+    dev = torch.device("cuda", 0)
+    x0, y0 = orc.init_uniform(n, R, seed)
+    ctx = sb.Context(0)
+    try:
+        res = ctx.solve(prob, sb.Params.default(sb.BSB, steps=1, replicas=R, seed=seed, field_mode=sb.FIELD_TC),
+                        want_state=True)
+    finally:
+        ctx.close()
+    assert res.field_dtype == "bf16x2"
+    _, y64 = _fp64_bsb(torch, J, h, x0, y0, c0, 1, dev)
+    F = torch.from_numpy(x0).double().to(dev) @ torch.from_numpy(J).double().to(dev)
+    dF = (torch.from_numpy(res.final_y).double().to(dev) - y64) / (1.25 * c0)
+    rms = float(dF.pow(2).mean().sqrt())
+    ratio = float((dF * torch.sign(F)).mean() / dF.abs().mean())
+    print(f"split-bf16 one-step field error: rms {rms:.3g}, bias ratio {ratio:.3f}")
+    assert rms <= 4e-7
+    assert abs(ratio) <= 0.45
+
+
 def test_config3_split_bf16_error_vs_fp64():
     """The batched bSB workload's shape (N=8192, J ~ N(0, 1/N), h ~ N(0, 0.1), R=256) against an FP64
     run of the same update (J x in FP64 on the GPU; the published bSB equations, same initial state,
-    schedule and c0). Stated tolerance: over the first 2 steps the BF16 hi+lo trajectory stays within
-    1e-4 of FP64. The tensor core's FP32 accumulation shrinks the field by a small biased amount per
-    MMA block (1536 blocks per field here), so later steps drift further than the FP32 path's (a
-    replica whose x sits at a wall can take the other branch); the 10-step figures are printed."""
+    schedule and c0). Stated tolerances: over the first 2 steps the BF16 hi + lo trajectory stays
+    within 1e-5 of FP64 (measured 5.2e-6); after 10 steps at most 8 of the 256 replicas are off by
+    more than 1e-2 (a replica whose x sits at the inelastic wall can take the other branch: measured 3,
+    and 33 before the field was accumulated in segments; the plain FP32 kernel has 0), and the 99th
+    percentile of |x - x_fp64| stays below 2e-4 (measured 8e-5)."""
     import torch
 
     n, R, seed = 8192, 256, 3
     J, h = instances.gaussian(n, seed=1234)
     prob = sb.Problem.from_dense(J, h)
     dev = torch.device("cuda", 0)
-    Jd = torch.from_numpy(J).double().to(dev)
-    hd = torch.from_numpy(h).double().to(dev)
-    c0, dt, a0 = float(prob.default_c0()), 1.25, 1.0
+    c0 = float(prob.default_c0())
     x0, y0 = orc.init_uniform(n, R, seed)
     ctx = sb.Context(0)
     try:
-        for K, tol in ((2, 1e-4), (10, None)):
+        for K in (2, 10):
             prm = sb.Params.default(sb.BSB, steps=K, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
             res = ctx.solve(prob, prm, want_state=True)
             assert res.field_dtype == "bf16x2"
-            x = torch.from_numpy(x0).double().to(dev)
-            y = torch.from_numpy(y0).double().to(dev)
-            for t in range(K):
-                pump = float(sb.pump(a0, t, K))
-                y = y + dt * (-pump * x + c0 * (x @ Jd + hd))
-                x = x + dt * a0 * y
-                wall = x.abs() > 1.0
-                x = torch.where(wall, torch.sign(x), x)
-                y = torch.where(wall, torch.zeros_like(y), y)
+            x, _ = _fp64_bsb(torch, J, h, x0, y0, c0, K, dev)
             d = (torch.from_numpy(res.final_x).to(dev).double() - x).abs()
             off = int((d.max(dim=1).values > 1e-2).sum())
+            p99 = float(d.flatten().kthvalue(int(0.99 * d.numel())).values)
             print(f"config-3 split-bf16 after {K} steps: max |x - x_fp64| = {float(d.max()):.3g}, "
-                  f"median {float(d.median()):.3g}, replicas off by > 1e-2: {off} of {R}")
-            if tol is not None:
-                assert float(d.max()) <= tol
+                  f"p99 {p99:.3g}, median {float(d.median()):.3g}, replicas off by > 1e-2: {off} of {R}")
+            if K == 2:
+                assert float(d.max()) <= 1e-5
+            else:
+                assert off <= 8
+                assert p99 <= 2e-4
     finally:
         ctx.close()
