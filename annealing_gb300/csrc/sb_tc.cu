@@ -49,7 +49,7 @@ namespace sbk {
 bool tc_kernel_fp8(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_bf16(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem);
-bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem);
+bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem, bool pair = false);
 
 namespace {
 using namespace tck;
@@ -169,6 +169,7 @@ struct TcEngine {
   const void *kernel[3] = {nullptr, nullptr, nullptr};  // by epilogue mode
   size_t smem = 0;
   int threads = kTcThreads;
+  bool pair = false;  // E2M1 kernel in CTA pairs (clusters of two, launched with that attribute)
 };
 
 namespace {
@@ -176,12 +177,12 @@ namespace {
 // Kp: K extent in spins (a multiple of 256 for packed E2M1 operands, of 128 otherwise).
 int kp_for(int dt, int n) { return dt == kTcFp4 ? (n + 255) / 256 * 256 : (n + 127) / 128 * 128; }
 
-bool pick(TcEngine *e, int dt, int variant, int nr, int n) {
+bool pick(TcEngine *e, int dt, int variant, int nr, int n, bool pair = false) {
   size_t smem = 0;
   for (int m = 0; m < 3; ++m) {
     const void *k = nullptr;
     bool ok;
-    if (dt == kTcFp4) ok = tc_kernel_fp4(variant, nr, m, kp_for(dt, n) / 256, &k, &smem);
+    if (dt == kTcFp4) ok = tc_kernel_fp4(variant, nr, m, kp_for(dt, n) / 256, &k, &smem, pair);
     else if (dt == kTcFp8) ok = tc_kernel_fp8(variant, nr, m, &k, &smem);
     else if (dt == kTcBf16) ok = tc_kernel_bf16(variant, nr, m, &k, &smem);
     else ok = tc_kernel_split(variant, nr, m, &k, &smem);
@@ -224,11 +225,13 @@ size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * 2 * sizeof(uin
 namespace {
 
 // Tile geometry of an engine: the setup, the replica tile and the padded extents that follow.
-void set_geometry(TcEngine *e, const TcSetup &s, int nr) {
+void set_geometry(TcEngine *e, const TcSetup &s, int nr, bool pair = false) {
   e->s = s;
   e->nr = nr;
+  e->pair = pair;
   if (s.dtype == kTcFp4) e->threads = kFp4Threads;
-  e->Np = (s.n + kBM - 1) / kBM * kBM;
+  // CTA pairs take spin tiles 2k and 2k + 1: an even number of them
+  e->Np = pair ? (s.n + 2 * kBM - 1) / (2 * kBM) * (2 * kBM) : (s.n + kBM - 1) / kBM * kBM;
   e->Kp = kp_for(s.dtype, s.n);
   e->Rp = (s.R + nr - 1) / nr * nr;
   e->n_mtiles = e->Np / kBM;
@@ -253,8 +256,10 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
   *ce = cudaSuccess;
   const bool fp4 = e->s.dtype == kTcFp4;
   const int elem = elem_bytes(e), nr = e->nr;
-  // V boxes: the whole replica tile, or one replica half for the E2M1 kernel
+  // V boxes: the whole replica tile, or one replica half for the E2M1 kernel (half of that for each
+  // CTA of a pair); stores: one replica half of the unit's own spins
   const uint32_t vrows = fp4 ? (uint32_t)(nr >= 64 ? nr / 2 : nr) : (uint32_t)nr;
+  const uint32_t vload = e->pair ? vrows / 2 : vrows;
   const uint64_t rowe = row_elems(e);
   TcArgs &g = e->args;
   memset(&g, 0, sizeof(g));
@@ -262,7 +267,7 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
     if (!encode_2d(&g.tmA[a], e->a[a], elem, rowe, (uint64_t)e->Np, kBM)) return "cuTensorMapEncodeTiled(J)";
   for (int b = 0; b < 2; ++b)
     for (int pp = 0; pp < b_parts(e); ++pp) {
-      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, rowe, (uint64_t)e->Rp, vrows))
+      if (!encode_2d(&g.tmB[b][pp], e->v[b][pp], elem, rowe, (uint64_t)e->Rp, vload))
         return "cuTensorMapEncodeTiled(V)";
       g.v[b][pp] = e->v[b][pp];
     }
@@ -299,6 +304,43 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
 
 }  // namespace
 
+namespace {
+// The CTA-pair E2M1 kernel runs this dSB shape when asked for (SB_TC_PAIR=1): the 128-replica
+// tile, its units (spin tiles rounded up to an even count) on distinct SMs, every pair co-resident
+// as a cluster of two. It is bit-identical to the single-CTA kernel and measured slower on the
+// batched dSB workload, so the single-CTA kernel is the default.
+bool pair_fits(const TcSetup &s, int nr, int sms) {
+  if (s.dtype != kTcFp4 || s.variant != 2 || nr != 128) return false;
+  const char *v = getenv("SB_TC_PAIR");
+  if (!v || v[0] != '1') return false;
+  const int mt = (s.n + 2 * kBM - 1) / (2 * kBM) * 2;
+  const int units = mt * ((s.R + nr - 1) / nr);
+  if (units > sms) return false;
+  const void *k = nullptr;
+  size_t smem = 0;
+  if (!tc_kernel_fp4(2, nr, kEmodeStep, kp_for(kTcFp4, s.n) / 256, &k, &smem, true)) return false;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)units);
+  cfg.blockDim = dim3((unsigned)kFp4Threads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return 2 * clusters >= units;
+}
+}  // namespace
+
 bool tc_fp4_fits(int n, int R) {
   const int nr = choose_nr(n, R, sm_count());
   const void *k = nullptr;
@@ -308,7 +350,7 @@ bool tc_fp4_fits(int n, int R) {
 
 int64_t tc_footprint(const TcSetup &s) {
   if (s.dtype == kTcFp4) {
-    const int64_t Np = (s.n + kBM - 1) / kBM * kBM, Kb = kp_for(kTcFp4, s.n) / 2;
+    const int64_t Np = (s.n + 2 * kBM - 1) / (2 * kBM) * (2 * kBM), Kb = kp_for(kTcFp4, s.n) / 2;
     const int64_t Rp = (s.R + 127) / 128 * 128;
     return Np * Kb + 2 * Rp * Kb + 4096;
   }
@@ -342,12 +384,13 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     return SB_ERR_UNSUPPORTED;
   }
   TcEngine *e = new TcEngine();
-  if (!pick(e, s.dtype, s.variant, nr, s.n)) {
+  const bool pair = pair_fits(s, nr, sms);
+  if (!pick(e, s.dtype, s.variant, nr, s.n, pair)) {
     delete e;
     err = "no kernel for this dtype / variant / size";
     return SB_ERR_UNSUPPORTED;
   }
-  set_geometry(e, s, nr);
+  set_geometry(e, s, nr, pair);
   auto fail = [&](const char *what, cudaError_t ce) {
     err = std::string(what) + (ce != cudaSuccess ? std::string(": ") + cudaGetErrorString(ce) : "");
     tc_destroy(e);
@@ -420,11 +463,15 @@ static cudaError_t launch(TcEngine *e, int emode, const TcArgs &a, cudaStream_t 
   cfg.blockDim = dim3((unsigned)e->threads);
   cfg.dynamicSmemBytes = e->smem;
   cfg.stream = st;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;
+  attr[1].val.clusterDim.x = 2;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = e->pair ? 2 : 1;
   void *params[1] = {const_cast<TcArgs *>(&a)};
   return cudaLaunchKernelExC(&cfg, e->kernel[emode], params);
 }

@@ -9,21 +9,24 @@ namespace {
 constexpr size_t kSmemLimit = 232448;
 constexpr size_t kStaticReserve = 4096;
 
-template <int NR>
+template <int NR, bool PAIR = false>
 bool lookup(int emode, int k_chunks, const void **k, size_t *smem) {
-  *smem = tck::fp4_smem<NR>(k_chunks);
+  *smem = tck::fp4_smem<NR, PAIR>(k_chunks);
   *k = nullptr;
   if (*smem + kStaticReserve > kSmemLimit) return false;
-  if (emode == tck::kEmodeStep) *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeStep>);
-  if (emode == tck::kEmodeStepTrace) *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeStepTrace>);
-  if (emode == tck::kEmodeEnergy) *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeEnergy>);
+  if (emode == tck::kEmodeStep) *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeStep, PAIR>);
+  if (emode == tck::kEmodeStepTrace)
+    *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeStepTrace, PAIR>);
+  if (emode == tck::kEmodeEnergy) *k = reinterpret_cast<const void *>(&tck::tc_fp4_kernel<NR, tck::kEmodeEnergy, PAIR>);
   return *k != nullptr;
 }
 }  // namespace
 
 // k_chunks: 256-spin chunks of K (Kp / 256); false when the unit's J rows do not fit shared memory.
-bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem) {
+// pair: the CTA-pair form (clusters of two, 128-replica tile only).
+bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem, bool pair) {
   if (variant != 2 || k_chunks <= 0) return false;
+  if (pair) return nr == 128 && lookup<128, true>(emode, k_chunks, k, smem);
   switch (nr) {
     case 32: return lookup<32>(emode, k_chunks, k, smem);
     case 64: return lookup<64>(emode, k_chunks, k, smem);

@@ -47,12 +47,16 @@ __host__ __device__ constexpr uint32_t make_idesc_mxf4(int m, int n) {
 
 // Replica halves and pipeline depth per replica tile: each epilogue warp takes a multiple of 16
 // columns of a half.
-template <int NR>
+// PAIR: two CTAs (a cluster of two, spin tiles 2k and 2k + 1 of the same replica tile) run one
+// M = 256 MMA per K chunk (tcgen05 cta_group::2): each stages its own 128 J rows and half of the V
+// chunk's replicas, so a CTA streams half the V bytes per step.
+template <int NR, bool PAIR = false>
 struct Fp4Cfg {
   static constexpr int kHalves = NR >= 64 ? 2 : 1;
-  static constexpr int kNH = NR / kHalves;           // replicas per half: MMA N, V box rows
-  static constexpr int kBTile = kNH * kChunkBytes;   // one V chunk of one half
-  static constexpr int kStages = 8;
+  static constexpr int kNH = NR / kHalves;           // replicas per half: MMA N
+  static constexpr int kBRows = PAIR ? kNH / 2 : kNH;  // V box rows this CTA loads
+  static constexpr int kBTile = kBRows * kChunkBytes;  // this CTA's part of one V chunk of one half
+  static constexpr int kStages = PAIR ? 16 : 8;        // the same 64 KB ring
   static constexpr int kWarpCols = kNH / 2;          // columns of a half per epilogue warp
 };
 constexpr int kFp4Threads = kTcThreads + 32;  // + the publisher warp
@@ -61,12 +65,12 @@ constexpr int kFp4ATile = kBM * kChunkBytes;  // one J chunk: 128 spins x 256 sp
 // Shared memory of one CTA for k_chunks 128-byte chunks of K (256 spins each).
 // At least enough that no more CTAs share an SM than its 512 TMEM columns hold (a CTA waiting
 // in tcgen05.alloc would stall the flag-ordered grid).
-template <int NR>
+template <int NR, bool PAIR = false>
 constexpr size_t fp4_smem(int k_chunks) {
   constexpr int kCols = 3 * NR + 32 <= 128 ? 128 : (3 * NR + 32 <= 256 ? 256 : 512);
   constexpr size_t kFloor = 233472 / (512 / kCols + 1) + 1024;  // 228 KB of shared memory per SM
-  const size_t need = 1024 + (size_t)Fp4Cfg<NR>::kStages * Fp4Cfg<NR>::kBTile + (size_t)k_chunks * kFp4ATile +
-                      (size_t)NR * (kBM / 2);
+  const size_t need = 1024 + (size_t)Fp4Cfg<NR, PAIR>::kStages * Fp4Cfg<NR, PAIR>::kBTile +
+                      (size_t)k_chunks * kFp4ATile + (size_t)NR * (kBM / 2);
   return need > kFloor ? need : kFloor;
 }
 
@@ -74,15 +78,21 @@ constexpr size_t fp4_smem(int k_chunks) {
 // bytes); p.tmA loads 128-byte x 128-row J boxes, p.tmB 128-byte x NR/2-row V boxes (NR/2 = the
 // half's replicas; the whole NR when NR = 32), p.tmS stores one half tile (64 bytes x NR/2 rows).
 // p.flags[(rt * halves + h) * n_mtiles + mt] = steps whose half h this unit has published.
-template <int NR, int EMODE>
+// PAIR (a cluster of two CTAs): p.tmB boxes hold kBRows = NH / 2 rows; the first CTA of the pair
+// (rank 0) issues the MMAs and owns the copy barriers (full_bar, a_bar) that both CTAs' loads
+// complete, and the accumulator-free barrier (acce_bar) that both CTAs' epilogues arrive on; its
+// commits arrive on the same barrier of both CTAs. Every wait stays bounded; both CTAs meet at a
+// cluster barrier before freeing tensor memory and exiting.
+template <int NR, int EMODE, bool PAIR = false>
 __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_constant__ TcArgs p) {
-  using F = Fp4Cfg<NR>;
+  using F = Fp4Cfg<NR, PAIR>;
   constexpr int H = F::kHalves, NH = F::kNH, STAGES = F::kStages, kBTile = F::kBTile;
   constexpr int kVRow = kBM / 2;  // bytes of one replica row of the unit's V tile
   constexpr uint32_t kSf = 3 * NR;
   constexpr uint32_t kCols = kSf + 32 <= 128 ? 128 : (kSf + 32 <= 256 ? 256 : 512);
-  constexpr uint32_t kIdesc = make_idesc_mxf4(kBM, NH);
+  constexpr uint32_t kIdesc = make_idesc_mxf4(PAIR ? 2 * kBM : kBM, NH);
   static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128 && F::kWarpCols % 16 == 0, "replica tile");
+  static_assert(!PAIR || NR == 128, "CTA pairs run the 128-replica tile");
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -101,6 +111,10 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
   constexpr bool want_e = EMODE != kEmodeStep;
   const int nsteps = kEOnly ? 1 : p.steps;
   bool ok = true;
+  const uint32_t crank = PAIR ? ptx::cluster_rank() : 0u;  // 0: the pair's MMA issuer
+  const bool issuer = crank == 0;
+  // shared::cluster address of the issuer's J-load barrier, which both CTAs' loads complete
+  const uint32_t a_bar_c = PAIR ? ptx::mapa(ptx::smem_u32(&a_bar), 0) : 0u;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -111,7 +125,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
     ptx::mbar_init(&drain_bar, 1);
     for (int h = 0; h < H; ++h) {
       ptx::mbar_init(&accf_bar[h], 1);
-      ptx::mbar_init(&acce_bar[h], kEpiWarps);
+      ptx::mbar_init(&acce_bar[h], PAIR ? 2 * kEpiWarps : kEpiWarps);
       ptx::mbar_init(&pub_bar[h], kEpiWarps);
     }
     ptx::fence_mbar_init();
@@ -120,8 +134,13 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
     ptx::prefetch_tmap(&p.tmB[1][0]);
   }
   if (warp == 1) {
-    ptx::tmem_alloc(&tmem_base_sh, kCols);
-    ptx::tmem_relinquish();
+    if constexpr (PAIR) {
+      ptx::tmem_alloc_pair(&tmem_base_sh, kCols);
+      ptx::tmem_relinquish_pair();
+    } else {
+      ptx::tmem_alloc(&tmem_base_sh, kCols);
+      ptx::tmem_relinquish();
+    }
   }
   ptx::tc_fence_before();
   __syncthreads();
@@ -138,15 +157,24 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
     ptx::tmem_st_wait();
   }
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (PAIR)
+    ptx::cluster_sync();  // both CTAs' barriers initialised and scale columns written
+  else
+    __syncthreads();
   ptx::tc_fence_after();
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      ptx::mbar_arrive_expect_tx(&a_bar, (uint32_t)(p.k_chunks * kFp4ATile));
-      for (int kc = 0; kc < p.k_chunks; ++kc)
-        ptx::tma_load_2d(jres + (size_t)kc * kFp4ATile, &p.tmA[0], kc * kChunkBytes, m0, &a_bar);
+      if constexpr (PAIR) {
+        if (issuer) ptx::mbar_arrive_expect_tx(&a_bar, (uint32_t)(2 * p.k_chunks * kFp4ATile));
+        for (int kc = 0; kc < p.k_chunks; ++kc)
+          ptx::tma_load_2d_pair(jres + (size_t)kc * kFp4ATile, &p.tmA[0], kc * kChunkBytes, m0, a_bar_c);
+      } else {
+        ptx::mbar_arrive_expect_tx(&a_bar, (uint32_t)(p.k_chunks * kFp4ATile));
+        for (int kc = 0; kc < p.k_chunks; ++kc)
+          ptx::tma_load_2d(jres + (size_t)kc * kFp4ATile, &p.tmA[0], kc * kChunkBytes, m0, &a_bar);
+      }
     }
     uint32_t g = 0, issued = 0;  // chunks walked / V loads issued (lane 0)
     for (int ls = 0; ls < nsteps && ok; ++ls) {
@@ -167,8 +195,16 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           if (lane == 0) {
             const int s = g % STAGES;
             const uint32_t use = g / STAGES;
-            if (use > 0 && !ptx::mbar_wait(&empty_bar[s], (use - 1) & 1, p.wait_cycles)) {
+            const bool freed = use == 0 || (PAIR ? ptx::mbar_wait_cluster(&empty_bar[s], (use - 1) & 1, p.wait_cycles)
+                                                  : ptx::mbar_wait(&empty_bar[s], (use - 1) & 1, p.wait_cycles));
+            if (!freed) {
               ok = false;
+            } else if constexpr (PAIR) {
+              // the issuer's full_bar[s] counts both CTAs' halves of the chunk
+              if (issuer) ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)(2 * kBTile));
+              ptx::tma_load_2d_pair(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes,
+                                    r0 + h * NH + (int)crank * F::kBRows, ptx::mapa(ptx::smem_u32(&full_bar[s]), 0));
+              ++issued;
             } else {
               ptx::mbar_arrive_expect_tx(&full_bar[s], (uint32_t)kBTile);
               ptx::tma_load_2d(ring + s * kBTile, &p.tmB[buf][0], kc * kChunkBytes, r0 + h * NH, &full_bar[s]);
@@ -182,38 +218,73 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
     if (!ok && lane == 0) {
       // a wait gave up: let the copies this CTA started land before it exits (each stage's last
       // issued load, and the resident J)
-      for (int s = 0; s < STAGES; ++s)
-        if (issued > (uint32_t)s) ptx::mbar_wait(&full_bar[s], ((issued - 1 - s) / STAGES) & 1, p.wait_cycles);
-      ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
+      if constexpr (PAIR) {
+        // this CTA's loads complete barriers of the issuer, which it cannot wait on: a bounded pause
+        // far longer than any copy, then the issuer's own bounded waits
+        const long long t0 = clock64();
+        while (clock64() - t0 < (p.wait_cycles < 2000000LL ? p.wait_cycles : 2000000LL)) __nanosleep(1000);
+        if (issuer) {
+          for (int s = 0; s < STAGES; ++s)
+            if (issued > (uint32_t)s) ptx::mbar_wait_cluster(&full_bar[s], ((issued - 1 - s) / STAGES) & 1, p.wait_cycles);
+          ptx::mbar_wait_cluster(&a_bar, 0, p.wait_cycles);
+        }
+      } else {
+        for (int s = 0; s < STAGES; ++s)
+          if (issued > (uint32_t)s) ptx::mbar_wait(&full_bar[s], ((issued - 1 - s) / STAGES) & 1, p.wait_cycles);
+        ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
+      }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && issuer) {
       // ---------------- MMA issuer ----------------
-      ok = ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
+      ok = PAIR ? ptx::mbar_wait_cluster(&a_bar, 0, p.wait_cycles) : ptx::mbar_wait(&a_bar, 0, p.wait_cycles);
       uint32_t g = 0;
       for (int ls = 0; ls < nsteps && ok; ++ls) {
         for (int h = 0; h < H && ok; ++h) {
-          if (ls >= 1 && !ptx::mbar_wait(&acce_bar[h], (uint32_t)(ls - 1) & 1, p.wait_cycles)) { ok = false; break; }
+          if (ls >= 1 && !(PAIR ? ptx::mbar_wait_cluster(&acce_bar[h], (uint32_t)(ls - 1) & 1, p.wait_cycles)
+                                : ptx::mbar_wait(&acce_bar[h], (uint32_t)(ls - 1) & 1, p.wait_cycles))) {
+            ok = false;
+            break;
+          }
           ptx::tc_fence_after();
           const uint32_t t_acc = tmem + h * NH;
           for (int kc = 0; kc < p.k_chunks; ++kc, ++g) {
             const int s = g % STAGES;
             const uint32_t use = g / STAGES;
-            if (!ptx::mbar_wait(&full_bar[s], use & 1, p.wait_cycles)) { ok = false; break; }
+            if (!(PAIR ? ptx::mbar_wait_cluster(&full_bar[s], use & 1, p.wait_cycles)
+                       : ptx::mbar_wait(&full_bar[s], use & 1, p.wait_cycles))) {
+              ok = false;
+              break;
+            }
             ptx::tc_fence_after();
             const uint32_t sa = ptx::smem_u32(jres + (size_t)kc * kFp4ATile);
             const uint32_t sb = ptx::smem_u32(ring + s * kBTile);
 #pragma unroll
-            for (int k = 0; k < kChunkBytes / 32; ++k)
-              ptx::mma_mxf4(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
-                            tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
-            ptx::mma_commit(&empty_bar[s]);
+            for (int k = 0; k < kChunkBytes / 32; ++k) {
+              if constexpr (PAIR)
+                ptx::mma_mxf4_pair(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
+                                   tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
+              else
+                ptx::mma_mxf4(t_acc, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32), kIdesc,
+                              tmem + kSf, tmem + kSf + 16, (kc > 0 || k > 0) ? 1u : 0u);
+            }
+            if constexpr (PAIR)
+              ptx::mma_commit_pair(&empty_bar[s]);
+            else
+              ptx::mma_commit(&empty_bar[s]);
           }
           if (!ok) break;
-          ptx::mma_commit(&accf_bar[h]);
+          if constexpr (PAIR)
+            ptx::mma_commit_pair(&accf_bar[h]);
+          else
+            ptx::mma_commit(&accf_bar[h]);
         }
       }
-      if (!ok) {
+      if constexpr (PAIR) {
+        // both CTAs wait on drain_bar before freeing tensor memory: the MMAs issued are done
+        ptx::mma_commit_pair(&drain_bar);
+        ptx::mbar_wait_cluster(&drain_bar, 0, p.wait_cycles);
+      } else if (!ok) {
         // a wait gave up: the MMAs already issued finish before TMEM is freed
         ptx::mma_commit(&drain_bar);
         ptx::mbar_wait(&drain_bar, 0, p.wait_cycles);
@@ -266,7 +337,8 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
       const float pump = pump_next;
       if (!kEOnly && ls + 1 < nsteps) pump_next = p.pumps[t + 1];
       for (int h = 0; h < H; ++h) {
-        const bool got = ptx::mbar_wait(&accf_bar[h], (uint32_t)ls & 1, p.wait_cycles);
+        const bool got = PAIR ? ptx::mbar_wait_cluster(&accf_bar[h], (uint32_t)ls & 1, p.wait_cycles)
+                              : ptx::mbar_wait(&accf_bar[h], (uint32_t)ls & 1, p.wait_cycles);
         if (!epi_all(got)) { ok = false; break; }
         ptx::tc_fence_after();
         const int c_lo = h * NH + sub * F::kWarpCols;
@@ -339,7 +411,10 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
         if constexpr (!kEOnly) ptx::fence_proxy_async_shared();  // tile writes -> the publisher's TMA store
         __syncwarp();
         if (lane == 0) {
-          ptx::mbar_arrive(&acce_bar[h]);
+          if constexpr (PAIR)
+            ptx::mbar_arrive_cluster(ptx::mapa(ptx::smem_u32(&acce_bar[h]), 0));
+          else
+            ptx::mbar_arrive(&acce_bar[h]);
           if constexpr (!kEOnly) ptx::mbar_arrive(&pub_bar[h]);
         }
         // the next step rewrites this half tile only after its accumulator, which needs this
@@ -380,9 +455,19 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
   if (!ok) atomicOr(p.status, kErrWaitTimeout);
   ptx::tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) {
+    // the pair's second CTA: the issuer's MMAs write this CTA's tensor memory and read its shared
+    // memory; once this CTA's own work is done, wait for their completion (the issuer's last commit)
+    if (!issuer && warp == 1 && lane == 0 && !ptx::mbar_wait_cluster(&drain_bar, 0, p.wait_cycles))
+      atomicOr(p.status, kErrWaitTimeout);
+    ptx::cluster_sync();  // neither CTA leaves while the other may still touch its memory
+  }
   if (warp == 1) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, kCols);
+    if constexpr (PAIR)
+      ptx::tmem_dealloc_pair(tmem, kCols);
+    else
+      ptx::tmem_dealloc(tmem, kCols);
   }
 }
 
