@@ -600,11 +600,6 @@ cudaError_t Grouped::energy_pass_for(const std::vector<int> &idx, int tick) {
 
 // ---- autotuning: replica tile and item order, timed on the batch itself ----
 
-namespace {
-std::mutex g_tune_mu;
-std::map<std::string, std::pair<int, int>> g_tune_cache;
-}  // namespace
-
 std::string Grouped::tune_key() const {
   int64_t chunks = 0;
   int rmax = 0;

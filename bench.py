@@ -77,8 +77,9 @@ NCU_TRAFFIC = {
     "batched-dsb": (19.58e6, "profiles/tc_fp4_kernel_batched_dsb_n2000_r1024.md"),
     # plain dSB, N=2000, R=1: bytes per launch (ncu runs the launch with cold caches)
     "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
-    # the same in one cooperative launch per solve: DRAM read + write per launch (J read once)
-    "plain-dsb-persist": (31.17e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
+    # the same in one cooperative launch per solve: DRAM read + write per launch from a one-pass
+    # capture (J read once; 16.06 MB read, 15.9 KB written)
+    "plain-dsb-persist": (16.08e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
     # batched bSB, N=8192, R=256, BF16 hi+lo: bytes per SB step (8-step capture: 2.278 GB; 4 steps:
     # 1.146 GB), times the launch's steps
     "batched-bsb": (2.278e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
@@ -387,12 +388,22 @@ def run_ours(args, rank, world, local_rank):
         spl = max(1, rp.steps_per_launch)
         bytes_per_launch = (4.0 * n * n + 16.0 * n * R) * spl
         achieved = bytes_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e9
+        limiter = None
         if spl > 1:
             traffic = NCU_TRAFFIC.get("plain-dsb-persist", (None, None)) if n == 2000 and R == 1 else (None, None)
             kernel = "plain_persist_kernel (one cooperative launch per solve)"
-            note = ("J lives in registers for the whole launch (read from HBM once); an SB step moves one "
-                    "tagged sign word per CTA through L2, so the fraction of HBM above 1 is on-chip reuse "
-                    "and the step is bound by that exchange's latency")
+            note = ("achieved counts the algorithmic 4 N^2 bytes of J per SB step, but J lives in registers for "
+                    "the whole launch and is read from HBM once (traffic); the kernel is not HBM-bound, see "
+                    "limiter")
+            us = 1e3 * rp.kernel_ms_avg / spl
+            limiter = {"kind": "latency of the per-step sign exchange through L2",
+                       "us_per_sb_step": us,
+                       "serial_l2_trips_per_step": 2,
+                       "us_per_l2_trip": us / 2,
+                       "exchange": "each CTA stores one tagged sign word on its own 128-byte line; thread q of "
+                                   "every CTA polls CTA q's line until the tag of the step appears",
+                       "hbm_bytes_per_launch": 4.0 * n * n + 16.0 * n * R,
+                       "hbm_frac_of_launch": (4.0 * n * n + 16.0 * n * R) / (rp.kernel_ms_avg * 1e-3) / 1e9 / hbm}
         else:
             traffic = NCU_TRAFFIC["plain-dsb"] if n == 2000 and R == 1 else (None, None)
             kernel = "plain_step_kernel"
@@ -401,6 +412,8 @@ def run_ours(args, rank, world, local_rank):
                 "frac": achieved / hbm, "traffic": traffic[0],
                 "traffic_source": traffic[1], "kernel": kernel, "launch_ms": rp.kernel_ms_avg,
                 "sb_steps_per_launch": spl, "peak_source": f"{src} HBM copy", "note": note}
+        if limiter:
+            roof["limiter"] = limiter
 
     # ---- e2e: host buffers through the public calls: sb_problem_wrap (the coupling scan that
     # decides the operand type and c0) and sb_solve (H2D of J, the solve, D2H of the results) ----
