@@ -24,7 +24,7 @@ CHECKED = os.path.join(PKG, "_checked")
 ORACLE = os.path.join(ROOT, "oracle")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["sb_plain.cu", "sb_tc.cu", "sb_tc_fp8.cu", "sb_tc_bf16.cu", "sb_tc_split.cu", "sb_tc_fp4.cu", "sb_grouped.cu", "sb_noalloc.cu",
+LIB_SOURCES = ["sb_plain.cu", "sb_tc.cu", "sb_tc_fp8.cu", "sb_tc_bf16.cu", "sb_tc_split.cu", "sb_tc_split16.cu", "sb_tc_fp4.cu", "sb_grouped.cu", "sb_noalloc.cu",
                "sb_api.cpp", "sb_batch.cpp", "sb_problem.cpp", "sb_serve.cpp", "sb_analysis.cpp", "sb_sqa.cu",
                "sb_nmfa.cpp"]
 

@@ -121,7 +121,7 @@ sb_status resolve_mode(const sb_problem *p, const sb_params *prm, int &mode, int
     return SB_ERR_UNSUPPORTED;
   }
   const int want = prm->operand_dtype;
-  if (want < SB_OPERAND_AUTO || want > SB_OPERAND_FP4) {
+  if (want < SB_OPERAND_AUTO || want > SB_OPERAND_FP16X2) {
     err = "unknown operand_dtype";
     return SB_ERR_INVALID_ARG;
   }
@@ -148,11 +148,11 @@ sb_status resolve_mode(const sb_problem *p, const sb_params *prm, int &mode, int
       dtype = want;  // sb_operand_dtype and TcDtype share their codes
     }
   } else {
-    if (want != SB_OPERAND_AUTO && want != SB_OPERAND_BF16X2) {
-      err = "bSB on tensor cores runs the BF16 hi+lo operands only";
+    if (want != SB_OPERAND_AUTO && want != SB_OPERAND_BF16X2 && want != SB_OPERAND_FP16X2) {
+      err = "bSB on tensor cores runs split operands only (BF16 or FP16 hi + lo)";
       return SB_ERR_UNSUPPORTED;
     }
-    dtype = sbk::kTcBf16Split;
+    dtype = want == SB_OPERAND_FP16X2 ? sbk::kTcFp16Split : sbk::kTcBf16Split;
     if (prm->trace || prm->trace_all) {
       err = "per-step energy traces of bSB are produced by the plain FP32 path only";
       return SB_ERR_UNSUPPORTED;
@@ -327,12 +327,12 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
 // request; rows: replicas in x (x has R rows unless given).
 cudaError_t enqueue_energy(sb_plan *pl, const float *x, double *slot, cudaStream_t st, int t, bool fp64 = false,
                            int rows = -1) {
-  if (pl->tc && pl->dtype != sbk::kTcBf16Split && pl->prm.variant == SB_DSB && t >= 0)
+  if (pl->tc && !sbk::tc_split(pl->dtype) && pl->prm.variant == SB_DSB && t >= 0)
     return sbk::tc_energy(pl->tc, t, x, pl->dh, slot, pl->dstatus, st);
   // split couplings (bSB, real-valued dSB): the final pass on the tensor cores too (FP32 sums of the
   // hi and lo products: exact for integer couplings, and for real ones it ranks the replicas whose
   // best kTopK are recomputed in FP64 below); FP64 passes stay on the plain kernel
-  if (pl->tc && pl->dtype == sbk::kTcBf16Split && t >= 0 && !fp64 && (pl->split_exact || !pl->integral))
+  if (pl->tc && sbk::tc_split(pl->dtype) && t >= 0 && !fp64 && (pl->split_exact || !pl->integral))
     return sbk::tc_energy_signs(pl->tc, x, pl->dh, slot, pl->dstatus, st);
   sbk::PlainEnergy a;
   const int R = rows > 0 ? rows : pl->R;

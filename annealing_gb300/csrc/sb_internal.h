@@ -125,7 +125,13 @@ cudaError_t launch_pad_rows_f32(const float *src, float *dst, int n, int jp, cud
 
 // ---------------------------------------------------------------------------------------------
 // Tensor-core (tcgen05) path. See sb_tc.cu.
-enum TcDtype : int { kTcFp8 = 1, kTcBf16 = 2, kTcBf16Split = 3, kTcFp4 = 4 };
+enum TcDtype : int { kTcFp8 = 1, kTcBf16 = 2, kTcBf16Split = 3, kTcFp4 = 4, kTcFp16Split = 5 };
+// Operands split in a high and a low part (real-valued couplings): BF16 hi + lo, or FP16 hi + lo
+// with power-of-two scaling.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+constexpr bool tc_split(int dt) { return dt == kTcBf16Split || dt == kTcFp16Split; }
 
 struct TcPlanInfo;  // opaque, defined in sb_tc.cu
 }  // namespace sbk

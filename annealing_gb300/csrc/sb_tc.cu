@@ -35,6 +35,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <string>
 
@@ -49,6 +51,7 @@ namespace sbk {
 bool tc_kernel_fp8(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_bf16(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_split(int variant, int nr, int emode, const void **k, size_t *smem);
+bool tc_kernel_split16(int variant, int nr, int emode, const void **k, size_t *smem);
 bool tc_kernel_fp4(int variant, int nr, int emode, int k_chunks, const void **k, size_t *smem, bool pair = false);
 
 namespace {
@@ -56,14 +59,20 @@ using namespace tck;
 
 // ---- operand preparation ----
 
+// jscale: FP16 hi + lo, the power of two that brings max |J| into [2^12, 2^13)
 __global__ void convert_j_kernel(const float *J, int n, int jp, uint8_t *a0, uint8_t *a1, int Np,
-                                 int Kp, int dt) {
+                                 int Kp, int dt, float jscale) {
   const size_t total = (size_t)Np * Kp;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
        k += (size_t)gridDim.x * blockDim.x) {
     const size_t i = k / Kp, j = k % Kp;
     const float v = (i < (size_t)n && j < (size_t)n) ? J[i * jp + j] : 0.0f;
-    if (dt == kTcFp8) {
+    if (dt == kTcFp16Split) {
+      const float vs = __fmul_rn(v, jscale);
+      const __half hi = __float2half_rn(vs);
+      reinterpret_cast<__half *>(a0)[k] = hi;
+      reinterpret_cast<__half *>(a1)[k] = __float2half_rn(__fsub_rn(vs, __half2float(hi)));
+    } else if (dt == kTcFp8) {
       a0[k] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
     } else {
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
@@ -75,7 +84,7 @@ __global__ void convert_j_kernel(const float *J, int n, int jp, uint8_t *a0, uin
 }
 
 __global__ void prepare_v_kernel(const float *x, int n, int R, int xp, uint8_t *v0, uint8_t *v1,
-                                 int Kp, int dt, int variant) {
+                                 int Kp, int dt, int variant, float xscale) {
   const size_t total = (size_t)n * R;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
        k += (size_t)gridDim.x * blockDim.x) {
@@ -85,7 +94,13 @@ __global__ void prepare_v_kernel(const float *x, int n, int R, int xp, uint8_t *
     if (dt == kTcFp8) {
       v0[idx] = xv > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
     } else if ((dt == kTcBf16 && variant != 3) || variant == 2) {
-      reinterpret_cast<uint16_t *>(v0)[idx] = xv > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80;
+      reinterpret_cast<uint16_t *>(v0)[idx] =
+          dt == kTcFp16Split ? one16<kTcFp16Split>(!(xv > 0.0f)) : one16<kTcBf16>(!(xv > 0.0f));
+    } else if (dt == kTcFp16Split) {
+      const float xs = __fmul_rn(xv, xscale);
+      const __half hi = __float2half_rn(xs);
+      reinterpret_cast<__half *>(v0)[idx] = hi;
+      reinterpret_cast<__half *>(v1)[idx] = __float2half_rn(__fsub_rn(xs, __half2float(hi)));
     } else {
       const __nv_bfloat16 hi = __float2bfloat16_rn(xv);
       reinterpret_cast<__nv_bfloat16 *>(v0)[idx] = hi;
@@ -115,6 +130,20 @@ __global__ void prepare_v_fp4_kernel(const float *x, int n, int R, int xp, uint8
     const uint32_t c1 = i + 1 < (size_t)n ? (x[r * xp + i + 1] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
     v[k] = (uint8_t)(c0 | (c1 << 4));
   }
+}
+
+// max |J| over the n x n couplings, as the bits of a non-negative float (NaN ignored)
+__global__ void absmax_kernel(const float *J, int n, int jp, unsigned int *out) {
+  unsigned int m = 0;
+  const size_t total = (size_t)n * n;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const float a = fabsf(J[(k / n) * jp + k % n]);
+    const unsigned int u = __float_as_uint(a);
+    if (a == a && u > m) m = u;
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 int grid_1d(size_t total) {
@@ -170,6 +199,7 @@ struct TcEngine {
   size_t smem = 0;
   int threads = kTcThreads;
   bool pair = false;  // E2M1 kernel in CTA pairs (clusters of two, launched with that attribute)
+  float jscale = 1.0f, jinv = 1.0f;  // FP16 hi + lo: the coupling scale (a power of two) and its inverse
 };
 
 namespace {
@@ -185,6 +215,7 @@ bool pick(TcEngine *e, int dt, int variant, int nr, int n, bool pair = false) {
     if (dt == kTcFp4) ok = tc_kernel_fp4(variant, nr, m, kp_for(dt, n) / 256, &k, &smem, pair);
     else if (dt == kTcFp8) ok = tc_kernel_fp8(variant, nr, m, &k, &smem);
     else if (dt == kTcBf16) ok = tc_kernel_bf16(variant, nr, m, &k, &smem);
+    else if (dt == kTcFp16Split) ok = tc_kernel_split16(variant, nr, m, &k, &smem);
     else ok = tc_kernel_split(variant, nr, m, &k, &smem);
     e->kernel[m] = ok ? k : nullptr;
   }
@@ -242,10 +273,8 @@ void set_geometry(TcEngine *e, const TcSetup &s, int nr, bool pair = false) {
 int elem_bytes(const TcEngine *e) { return (e->s.dtype == kTcFp8 || e->s.dtype == kTcFp4) ? 1 : 2; }
 // operand row length in tensor-map elements: bytes of E2M1 pairs, else K elements
 uint64_t row_elems(const TcEngine *e) { return e->s.dtype == kTcFp4 ? (uint64_t)e->Kp / 2 : (uint64_t)e->Kp; }
-int a_parts(const TcEngine *e) { return e->s.dtype == kTcBf16Split ? 2 : 1; }
-int b_parts(const TcEngine *e) {
-  return ((e->s.dtype == kTcBf16Split && e->s.variant == 1) || e->s.variant == 3) ? 2 : 1;
-}
+int a_parts(const TcEngine *e) { return tc_split(e->s.dtype) ? 2 : 1; }
+int b_parts(const TcEngine *e) { return ((tc_split(e->s.dtype) && e->s.variant == 1) || e->s.variant == 3) ? 2 : 1; }
 size_t a_part_bytes(const TcEngine *e) { return (size_t)e->Np * row_elems(e) * elem_bytes(e); }
 size_t v_part_bytes(const TcEngine *e) { return (size_t)e->Rp * row_elems(e) * elem_bytes(e); }
 
@@ -284,6 +313,8 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
   g.n_mtiles = e->n_mtiles;
   g.n_rtiles = e->n_rtiles;
   g.k_chunks = (int)(rowe * elem / kChunkBytes);
+  g.jinv = e->jinv;
+  g.xscale = e->s.dtype == kTcFp16Split ? 16384.0f : 1.0f;  // |x| <= 1 -> [-2^14, 2^14]
   g.wait_cycles = ptx::kWaitCycles;
   // split operands: 8 chunks (512 spins of K) per accumulation segment; SB_SPLIT_SEG_CHUNKS
   // overrides it (shorter segments take fewer roundings each and cost more hand-offs)
@@ -357,8 +388,8 @@ int64_t tc_footprint(const TcSetup &s) {
   const int elem = s.dtype == kTcFp8 ? 1 : 2;
   const int64_t Np = (s.n + kBM - 1) / kBM * kBM, Kp = (s.n + 127) / 128 * 128;
   const int64_t Rp = (s.R + 127) / 128 * 128;
-  const int ap = s.dtype == kTcBf16Split ? 2 : 1;
-  const int bp = ((s.dtype == kTcBf16Split && s.variant == 1) || s.variant == 3) ? 2 : 1;
+  const int ap = tc_split(s.dtype) ? 2 : 1;
+  const int bp = ((tc_split(s.dtype) && s.variant == 1) || s.variant == 3) ? 2 : 1;
   return Np * Kp * elem * ap + 2 * Rp * Kp * elem * bp + 4096;
 }
 
@@ -373,8 +404,8 @@ sb_status tc_create(TcEngine **out, const TcSetup &s, const float *dJ, int jp, s
     err = "NMFA on tensor cores needs BF16 operands (integer couplings)";
     return SB_ERR_UNSUPPORTED;
   }
-  if (s.variant == 1 && s.dtype != kTcBf16Split) {
-    err = "bSB on tensor cores needs the BF16 hi+lo operands";
+  if (s.variant == 1 && !tc_split(s.dtype)) {
+    err = "bSB on tensor cores needs split (hi + lo) operands";
     return SB_ERR_UNSUPPORTED;
   }
   const int sms = sm_count();
@@ -424,13 +455,31 @@ void tc_destroy(TcEngine *e) {
 }
 
 cudaError_t tc_reload(TcEngine *e, const float *dJ, int jp, cudaStream_t st) {
+  if (e->s.dtype == kTcFp16Split) {
+    // the scale that brings max |J| into [2^12, 2^13): the flag words serve as the reduction's cell
+    cudaError_t ce = cudaMemsetAsync(e->flags, 0, sizeof(unsigned int), st);
+    if (ce != cudaSuccess) return ce;
+    absmax_kernel<<<grid_1d((size_t)e->s.n * e->s.n), 256, 0, st>>>(dJ, e->s.n, jp, e->flags);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+    unsigned int bits = 0;
+    if ((ce = cudaMemcpyAsync(&bits, e->flags, sizeof(bits), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return ce;
+    if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return ce;
+    float m;
+    memcpy(&m, &bits, sizeof(m));
+    int ex = 0;
+    if (m > 0.0f && m < 3.0e38f) frexpf(m, &ex);  // m = f 2^ex, f in [0.5, 1)
+    const int sj = m > 0.0f ? std::max(-100, std::min(100, 13 - ex)) : 0;
+    e->jscale = ldexpf(1.0f, sj);
+    e->jinv = ldexpf(1.0f, -sj);
+    e->args.jinv = e->jinv;
+  }
   if (e->s.dtype == kTcFp4) {
     const int Kb = e->Kp / 2;
     convert_j_fp4_kernel<<<grid_1d((size_t)e->Np * Kb), 256, 0, st>>>(dJ, e->s.n, jp, e->a[0], e->Np, Kb);
     return cudaGetLastError();
   }
   convert_j_kernel<<<grid_1d((size_t)e->Np * e->Kp), 256, 0, st>>>(dJ, e->s.n, jp, e->a[0], e->a[1], e->Np, e->Kp,
-                                                                   e->s.dtype);
+                                                                   e->s.dtype, e->jscale);
   return cudaGetLastError();
 }
 
@@ -451,7 +500,7 @@ cudaError_t tc_prepare(TcEngine *e, const float *x, cudaStream_t st) {
     return cudaGetLastError();
   }
   prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(x, e->s.n, e->s.R, e->s.xp, e->v[0][0], e->v[0][1], e->Kp,
-                                                                      e->s.dtype, e->s.variant);
+                                                                      e->s.dtype, e->s.variant, e->args.xscale);
   return cudaGetLastError();
 }
 
@@ -527,13 +576,15 @@ cudaError_t tc_energy_signs(TcEngine *e, const float *x, const float *h, double 
   // per replica into energy
   const void *k = nullptr;
   size_t smem = 0;
-  const bool have = e->s.dtype == kTcBf16 ? tc_kernel_bf16(2, e->nr, kEmodeEnergy, &k, &smem)
-                    : e->s.dtype == kTcBf16Split ? tc_kernel_split(2, e->nr, kEmodeEnergy, &k, &smem) : false;
+  const bool have = e->s.dtype == kTcBf16        ? tc_kernel_bf16(2, e->nr, kEmodeEnergy, &k, &smem)
+                    : e->s.dtype == kTcBf16Split ? tc_kernel_split(2, e->nr, kEmodeEnergy, &k, &smem)
+                    : e->s.dtype == kTcFp16Split ? tc_kernel_split16(2, e->nr, kEmodeEnergy, &k, &smem)
+                                                 : false;
   if (!have) return cudaErrorInvalidValue;
   cudaError_t ce = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (ce != cudaSuccess) return ce;
   prepare_v_kernel<<<grid_1d((size_t)e->s.n * e->s.R), 256, 0, st>>>(x, e->s.n, e->s.R, e->s.xp, e->v[0][0], nullptr,
-                                                                      e->Kp, e->s.dtype, 2);
+                                                                      e->Kp, e->s.dtype, 2, 1.0f);
   if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
   TcArgs a = e->args;
   a.x = const_cast<float *>(x);

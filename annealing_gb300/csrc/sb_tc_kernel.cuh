@@ -37,6 +37,7 @@
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -75,6 +76,7 @@ struct alignas(64) TcArgs {
   float noise, keep, mix;  // NMFA: sigma, 1 - alpha, alpha
   long long wait_cycles;   // limit of every bounded wait (SM clock cycles)
   int seg_chunks;          // split operands: K chunks per accumulation segment
+  float jinv, xscale;      // FP16 hi + lo: J was scaled by 1 / jinv and x is scaled by xscale (powers of two)
   // host-side fault injection for the timeout path: unit skip_unit does not publish its flag(s)
   // of step skip_step (skip_step < 0: every unit publishes)
   int skip_unit, skip_step;
@@ -94,6 +96,10 @@ template <>
 struct DtTraits<kTcBf16Split> {
   static constexpr int kElem = 2, kParts = 2;
 };
+template <>
+struct DtTraits<kTcFp16Split> {
+  static constexpr int kElem = 2, kParts = 2;
+};
 
 template <int DT, int VARIANT>
 struct Cfg {
@@ -101,16 +107,23 @@ struct Cfg {
   static constexpr int kAParts = DtTraits<DT>::kParts;
   // V = sign(x) needs one part even when J is split; bSB's x is split with J; NMFA's state is split
   // against exact (integer) BF16 couplings.
-  static constexpr int kBParts = ((DT == kTcBf16Split && VARIANT == 1) || VARIANT == 3) ? 2 : 1;
+  static constexpr int kBParts = ((tc_split(DT) && VARIANT == 1) || VARIANT == 3) ? 2 : 1;
   static constexpr int kKPerMma = 32 / kElem;  // 32 bytes of K per instruction
   static constexpr int kMmaPerChunk = kChunkBytes / 32;
 };
 
 __host__ __device__ constexpr uint32_t make_idesc(int dt, int m, int n) {
-  // D = F32 (bits 4-5 = 1); A/B format: E4M3 = 0 (kind::f8f6f4) or BF16 = 1 (kind::f16);
+  // D = F32 (bits 4-5 = 1); A/B format: E4M3 = 0 (kind::f8f6f4), F16 = 0 or BF16 = 1 (kind::f16);
   // both K-major; N >> 3 at bits 17-22; M >> 4 at bits 24-28.
-  return (1u << 4) | ((dt == kTcFp8 ? 0u : 1u) << 7) | ((dt == kTcFp8 ? 0u : 1u) << 10) |
-         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+  return (1u << 4) | ((dt == kTcBf16 || dt == kTcBf16Split ? 1u : 0u) << 7) |
+         ((dt == kTcBf16 || dt == kTcBf16Split ? 1u : 0u) << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+// +1 / -1 in a 16-bit operand type
+template <int DT>
+__host__ __device__ constexpr uint16_t one16(bool neg) {
+  return DT == kTcFp16Split ? (neg ? (uint16_t)0xBC00 : (uint16_t)0x3C00) : (neg ? (uint16_t)0xBF80 : (uint16_t)0x3F80);
 }
 
 __device__ __forceinline__ float sgnf(float v) { return v > 0.0f ? 1.0f : -1.0f; }
@@ -128,13 +141,19 @@ __device__ __forceinline__ void sb_update(float f, float hv, float pump, float c
   }
 }
 
-// Write element (r, i) of the next operand.
+// Write element (r, i) of the next operand (FP16 hi + lo: x scaled by xscale, a power of two).
 template <int DT, int VARIANT>
-__device__ __forceinline__ void store_operand(uint8_t *const (&vb)[2], size_t idx, float x) {
+__device__ __forceinline__ void store_operand(uint8_t *const (&vb)[2], size_t idx, float x, float xscale) {
   if constexpr (DT == kTcFp8) {
     vb[0][idx] = x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;  // E4M3 +1 / -1
   } else if constexpr (Cfg<DT, VARIANT>::kBParts == 1) {
-    reinterpret_cast<uint16_t *>(vb[0])[idx] = x > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80;
+    reinterpret_cast<uint16_t *>(vb[0])[idx] = one16<DT>(!(x > 0.0f));
+  } else if constexpr (DT == kTcFp16Split) {
+    const float xs = __fmul_rn(x, xscale);
+    const __half hi = __float2half_rn(xs);
+    const __half lo = __float2half_rn(__fsub_rn(xs, __half2float(hi)));
+    reinterpret_cast<__half *>(vb[0])[idx] = hi;
+    reinterpret_cast<__half *>(vb[1])[idx] = lo;
   } else {
     const __nv_bfloat16 hi = __float2bfloat16_rn(x);
     const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(x, __bfloat162float(hi)));
@@ -223,7 +242,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   // each into a fresh accumulator (column block 0), and the epilogue warps, idle during the
   // contraction, load each finished segment (the MMA lane waits only for that load) and add it into
   // a running FP32 sum (round to nearest; column block 1). x and y keep blocks 2 and 3.
-  constexpr bool kSeg = DT == kTcBf16Split;
+  constexpr bool kSeg = tc_split(DT);
+  // FP16 hi + lo: the accumulated field is scaled back by an exact power of two
+  const float fscale = DT == kTcFp16Split ? (C::kBParts == 2 ? p.jinv / p.xscale : p.jinv) : 1.0f;
   static_assert(NR % 32 == 0 && NR >= 32 && NR <= 128, "replica tile");
   static_assert(4 * NR <= 512, "two accumulators + x + y must fit TMEM");
 
@@ -547,7 +568,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         for (int j = 0; j < 16; ++j) {
           const int r = r0 + c + j;
           const bool in = row < p.n && r < p.R;
-          const float f = __uint_as_float(va[j]);
+          const float f = DT == kTcFp16Split ? __fmul_rn(__uint_as_float(va[j]), fscale) : __uint_as_float(va[j]);
           float x, y;
           if constexpr (kEOnly) {
             x = in ? p.x[(size_t)r * p.xp + row] : 0.0f;
@@ -582,7 +603,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             }
             if constexpr (!kStageV)
               if (SB_BOUNDS((size_t)r * p.Kp + row < (size_t)p.Rp * p.Kp, p.status))
-                store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x);
+                store_operand<DT, VARIANT>(vnext, (size_t)r * p.Kp + row, x, p.xscale);
           }
           if constexpr (kStageV && !kEOnly) {
             // every element of the tile is written (zero outside the problem) so the padding stays 0
@@ -590,7 +611,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
             if constexpr (DT == kTcFp8)
               *dst = in ? (x > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8) : (uint8_t)0;
             else
-              *reinterpret_cast<uint16_t *>(dst) = in ? (x > 0.0f ? (uint16_t)0x3F80 : (uint16_t)0xBF80) : (uint16_t)0;
+              *reinterpret_cast<uint16_t *>(dst) = in ? one16<DT>(!(x > 0.0f)) : (uint16_t)0;
           }
           vx[j] = __float_as_uint(x);
           vy[j] = __float_as_uint(y);

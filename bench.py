@@ -319,7 +319,8 @@ def run_ours(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     ctx = sb.Context(local_rank, stream=stream.cuda_stream)
     prob = sb.Problem.from_dense(J, h)
-    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16}[args.operand]
+    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16,
+           "bf16x2": sb.OPERAND_BF16X2, "fp16x2": sb.OPERAND_FP16X2}[args.operand]
     prm = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=fmode, seed=1234 + rank, operand_dtype=odt)
     plan = ctx.plan(prob, prm)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -371,7 +372,7 @@ def run_ours(args, rank, world, local_rank):
         achieved = flops_per_launch / (rp.kernel_ms_avg * 1e-3) / 1e12
         if fdt == "fp4e2m1" and n == 2000 and R == 1024:
             traffic = NCU_TRAFFIC["batched-dsb"]
-        elif fdt == "bf16x2" and n == 8192 and R == 256:
+        elif fdt in ("bf16x2", "fp16x2") and n == 8192 and R == 256:
             traffic = (NCU_TRAFFIC["batched-bsb"][0] * rp.steps_per_launch, NCU_TRAFFIC["batched-bsb"][1])
         else:
             traffic = (None, None)
@@ -381,7 +382,7 @@ def run_ours(args, rank, world, local_rank):
                 "launch_ms": rp.kernel_ms_avg, "sb_steps_per_launch": rp.steps_per_launch,
                 "flops_per_launch": flops_per_launch, "peak_source": label.format(src),
                 "frac_of_bf16_burst": achieved / bf16}
-        if results[0].field_dtype == "bf16x2":
+        if results[0].field_dtype in ("bf16x2", "fp16x2"):
             roof["note"] = "split operands run 3 products per field; achieved counts the algorithmic 2N^2R"
     else:
         # algorithmic bytes of one SB step (J, and x, y read and written) x the steps of a launch
@@ -449,6 +450,7 @@ def run_ours(args, rank, world, local_rank):
         "dtype": {"fp4e2m1": "e2m1 x e2m1 field (f32 accumulate, exact for |J| <= 4), f32 state",
                   "fp8e4m3": "fp8e4m3 field (f32 accumulate), f32 state",
                   "bf16x2": "bf16 hi+lo field (f32 accumulate), f32 state",
+                  "fp16x2": "fp16 hi+lo field, power-of-two scaled (f32 accumulate), f32 state",
                   "bf16": "bf16 field (f32 accumulate), f32 state",
                   "f32": "f32"}[results[0].field_dtype],
         "data": "synthetic (seeded; the reference's WK2000_1.rud is not shipped)",
@@ -1026,7 +1028,7 @@ def main():
     ap.add_argument("--pool", type=int, default=64, help="serving workload: distinct instances")
     ap.add_argument("--sb-steps", type=int, default=0,
                     help="smaller case for profiling: SB steps per solve (default: the workload's)")
-    ap.add_argument("--operand", choices=["auto", "fp4", "fp8", "bf16"], default="auto",
+    ap.add_argument("--operand", choices=["auto", "fp4", "fp8", "bf16", "bf16x2", "fp16x2"], default="auto",
                     help="tensor-core operand type of the single-instance workloads (default: narrowest exact)")
     ap.add_argument("--instances", type=int, default=512,
                     help="uneven-batch workload: instance count (smaller cases for profiling)")

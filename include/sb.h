@@ -95,7 +95,8 @@ typedef enum sb_operand_dtype {
   SB_OPERAND_FP8 = 1,    /* E4M3, integer |J| <= 16 */
   SB_OPERAND_BF16 = 2,   /* integer |J| <= 256 */
   SB_OPERAND_BF16X2 = 3, /* BF16 hi + lo, real J */
-  SB_OPERAND_FP4 = 4     /* packed E2M1, integer |J| <= 4, single-instance dSB */
+  SB_OPERAND_FP4 = 4,    /* packed E2M1, integer |J| <= 4, single-instance dSB */
+  SB_OPERAND_FP16X2 = 5  /* FP16 hi + lo, real J scaled by powers of two: 22 bits per operand (opt-in) */
 } sb_operand_dtype;
 
 /* Initial x, y.
