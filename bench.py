@@ -80,9 +80,9 @@ NCU_TRAFFIC = {
     # the same in one cooperative launch per solve: DRAM read + write per launch from a one-pass
     # capture (J read once; 16.06 MB read, 15.9 KB written)
     "plain-dsb-persist": (16.08e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
-    # batched bSB, N=8192, R=256, BF16 hi+lo: bytes per SB step (8-step capture: 2.278 GB; 4 steps:
-    # 1.146 GB), times the launch's steps
-    "batched-bsb": (2.278e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
+    # batched bSB, N=8192, R=256, BF16 hi+lo with the field accumulated in K segments: bytes per SB
+    # step (8-step capture of the step launch: 2.587 GB; 4 steps: 1.146 GB), times the launch's steps
+    "batched-bsb": (2.587e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
     # uneven batch: measured bytes per algorithmic byte on a 48-instance batch (441.2 MB of
     # 451.8 MB); the launch of the full batch is scaled by its algorithmic bytes
     "uneven-batch": (441.2 / 451.8, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
@@ -578,14 +578,18 @@ def run_batch(args, rank, world, local_rank):
     def addr(ptr):
         return ctypes.cast(ptr, ctypes.c_void_p).value or 0
 
+    from concurrent.futures import ThreadPoolExecutor
+
     host = [(p.n, addr(p.s.J), addr(p.s.h)) for p in probs]
+    pool = ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4))  # the scans run in C, GIL released
     e2e_ms = []
     for k in range(args.steps):
         torch.cuda.synchronize(dev)
         t1 = time.perf_counter()
-        wrapped = [sb.Problem.wrap(n_, j_, h_, keepalive=probs) for n_, j_, h_ in host]
+        wrapped = list(pool.map(lambda a: sb.Problem.wrap(a[0], a[1], a[2], keepalive=probs), host))
         ctx.batch(wrapped, prm).run(seed=200 + k)
         e2e_ms.append(1e3 * (time.perf_counter() - t1))
+    pool.shutdown()
     e2e_total = reduce_max(float(sum(e2e_ms)), world)
     if rank != 0:
         return
@@ -603,8 +607,8 @@ def run_batch(args, rank, world, local_rank):
                 "h2d_bytes_per_step": int(np_kp),  # couplings packed on the host, then copied
                 "d2h_bytes_per_step": int(sum(p.n + 8 * R for p in probs)),
                 "ms_per_step": e2e_total / args.steps,
-                "includes": "sb_problem_wrap of every instance's host couplings (coupling scan), batch "
-                            "creation (packing, upload), the run, results back"},
+                "includes": "sb_problem_wrap of every instance's host couplings (coupling scans, 16 at a "
+                            "time), batch creation (packing, upload), the run, results back"},
         "gpu_launches": int(launches), "roofline": roof, "clocks": clk.summary(),
         "quality": {"energy_check_ok": all(quality)}, "setup_s": setup_s,
     }
