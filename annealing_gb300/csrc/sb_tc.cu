@@ -200,6 +200,7 @@ struct TcEngine {
   int threads = kTcThreads;
   bool pair = false;  // E2M1 kernel in CTA pairs (clusters of two, launched with that attribute)
   float jscale = 1.0f, jinv = 1.0f;  // FP16 hi + lo: the coupling scale (a power of two) and its inverse
+  int flag_stride = 1;  // words between consecutive units' step flags
 };
 
 namespace {
@@ -251,7 +252,9 @@ int choose_nr_nmfa(int n, int R, int sms) {
 }  // namespace
 
 // one counter per unit (per unit and replica half for the E2M1 kernel)
-size_t flag_bytes(const TcEngine *e) { return ((size_t)e->units * 2 * sizeof(uint32_t) + 255) / 256 * 256; }
+size_t flag_bytes(const TcEngine *e) {
+  return ((size_t)e->units * 2 * e->flag_stride * sizeof(uint32_t) + 255) / 256 * 256;
+}
 
 namespace {
 
@@ -268,6 +271,14 @@ void set_geometry(TcEngine *e, const TcSetup &s, int nr, bool pair = false) {
   e->n_mtiles = e->Np / kBM;
   e->n_rtiles = e->Rp / nr;
   e->units = e->n_mtiles * e->n_rtiles;
+  // the streamed-J kernel polls and publishes faster with each unit's flag on its own 128-byte line
+  // (FP8 dSB N=2000 R=1024: 24.7 -> 23.4 ms per solve); the E2M1 kernel is indifferent (its two
+  // halves' flags alternate) and keeps them packed. SB_FLAG_STRIDE overrides it (measurements).
+  e->flag_stride = s.dtype == kTcFp4 ? 1 : 32;
+  if (const char *fs = getenv("SB_FLAG_STRIDE")) {
+    const int v = atoi(fs);
+    if (v >= 1 && v <= 64) e->flag_stride = v;
+  }
 }
 
 int elem_bytes(const TcEngine *e) { return (e->s.dtype == kTcFp8 || e->s.dtype == kTcFp4) ? 1 : 2; }
@@ -305,6 +316,7 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
     if (!encode_2d(&g.tmS[b], e->v[b][0], elem, rowe, (uint64_t)e->Rp, vrows, true, fp4 ? kBM / 2 : kBM))
       return "cuTensorMapEncodeTiled(V store)";
   g.flags = e->flags;
+  g.flag_stride = e->flag_stride;
   g.n = e->s.n;
   g.R = e->s.R;
   g.xp = e->s.xp;
@@ -617,6 +629,7 @@ bool tc_external_sizes(int n, int R, bool fp4, size_t *a_bytes, size_t *v_bytes,
   if (nr == 0 || (fp4 && !tc_fp4_fits(n, R))) return false;
   TcEngine e;
   set_geometry(&e, TcSetup{2, fp4 ? kTcFp4 : kTcFp8, n, R, n}, nr);
+  e.flag_stride = 1;  // packed flags: the allocation-free caller's fixed control area
   *a_bytes = a_part_bytes(&e);
   *v_bytes = v_part_bytes(&e);
   *flags_bytes = flag_bytes(&e);
@@ -629,6 +642,7 @@ cudaError_t tc_dsb_external(const TcExternal &ext, cudaStream_t st) {
   const int nr = choose_nr(ext.n, ext.R, sm_count());
   if (nr == 0 || (ext.fp4 && !tc_fp4_fits(ext.n, ext.R)) || !pick(&e, dt, 2, nr, ext.n)) return cudaErrorInvalidValue;
   set_geometry(&e, TcSetup{2, dt, ext.n, ext.R, ext.xp}, nr);
+  e.flag_stride = 1;  // packed flags (tc_external_sizes)
   e.a[0] = ext.a;
   e.v[0][0] = ext.v0;
   e.v[1][0] = ext.v1;

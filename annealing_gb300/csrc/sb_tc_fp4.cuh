@@ -77,7 +77,7 @@ constexpr size_t fp4_smem(int k_chunks) {
 // Buffers as in tc_sb_kernel; p.k_chunks = Kp / 256 (Kp a multiple of 256, J and V rows of Kp / 2
 // bytes); p.tmA loads 128-byte x 128-row J boxes, p.tmB 128-byte x NR/2-row V boxes (NR/2 = the
 // half's replicas; the whole NR when NR = 32), p.tmS stores one half tile (64 bytes x NR/2 rows).
-// p.flags[(rt * halves + h) * n_mtiles + mt] = steps whose half h this unit has published.
+// p.flags[((rt * halves + h) * n_mtiles + mt) * p.flag_stride] = steps whose half h this unit has published.
 // PAIR (a cluster of two CTAs): p.tmB boxes hold kBRows = NH / 2 rows; the first CTA of the pair
 // (rank 0) issues the MMAs and owns the copy barriers (full_bar, a_bar) that both CTAs' loads
 // complete, and the accumulator-free barrier (acce_bar) that both CTAs' epilogues arrive on; its
@@ -183,10 +183,10 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
         if (ls > 0) {
           // half h of V(ls) complete: every unit of the replica column has published it (the warp
           // polls 32 units per L2 round trip)
-          const uint32_t *hf = p.flags + (size_t)(rt * H + h) * p.n_mtiles;
+          const uint32_t *hf = p.flags + (size_t)(rt * H + h) * p.n_mtiles * p.flag_stride;
           for (int u0 = 0; u0 < p.n_mtiles && ok; u0 += 32) {
             const int u = u0 + lane;
-            const bool fl = u < p.n_mtiles ? wait_flag(hf + u, (uint32_t)ls, p.wait_cycles) : true;
+            const bool fl = u < p.n_mtiles ? wait_flag(hf + (size_t)u * p.flag_stride, (uint32_t)ls, p.wait_cycles) : true;
             if (!__all_sync(0xffffffffu, fl)) ok = false;
           }
           ptx::fence_proxy_async_global();
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(kFp4Threads, 1) tc_fp4_kernel(const __grid_con
           ptx::fence_proxy_async_global();  // the bulk store's writes, then the flag (release)
           if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status) &&
               !((int)blockIdx.x == p.skip_unit && ls == p.skip_step))
-            st_release(p.flags + (size_t)(rt * H + h) * p.n_mtiles + mt, (uint32_t)(ls + 1));
+            st_release(p.flags + ((size_t)(rt * H + h) * p.n_mtiles + mt) * p.flag_stride, (uint32_t)(ls + 1));
         }
       }
     }

@@ -76,6 +76,7 @@ struct alignas(64) TcArgs {
   float noise, keep, mix;  // NMFA: sigma, 1 - alpha, alpha
   long long wait_cycles;   // limit of every bounded wait (SM clock cycles)
   int seg_chunks;          // split operands: K chunks per accumulation segment
+  int flag_stride;         // words between consecutive units' flags (32: one 128-byte line each)
   float jinv, xscale;      // FP16 hi + lo: J was scaled by 1 / jinv and x is scaled by xscale (powers of two)
   // host-side fault injection for the timeout path: unit skip_unit does not publish its flag(s)
   // of step skip_step (skip_step < 0: every unit publishes)
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
   constexpr bool kEOnly = EMODE == kEmodeEnergy;   // one contraction, energies only
   constexpr bool want_e = EMODE != kEmodeStep;      // per-replica energies of s(t)
   const int nsteps = kEOnly ? 1 : p.steps;
-  uint32_t *col_flags = p.flags + (size_t)rt * p.n_mtiles;
+  uint32_t *col_flags = p.flags + (size_t)rt * p.n_mtiles * p.flag_stride;
   bool ok = true;
 
   if (threadIdx.x == 0) {
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         if (kx / kBM >= ready) {
           // poll the next 32 units of the column at once (one L2 round trip for all of them)
           const int u = ready + lane;
-          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + u, (uint32_t)ls, p.wait_cycles) : true;
+          const bool fl = u < p.n_mtiles ? wait_flag(col_flags + (size_t)u * p.flag_stride, (uint32_t)ls, p.wait_cycles) : true;
           if (!__all_sync(0xffffffffu, fl)) ok = false;
           ready = ready + 32 < p.n_mtiles ? ready + 32 : p.n_mtiles;
           ptx::fence_proxy_async_global();
@@ -648,7 +649,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_sb_kernel(const __grid_const
         __threadfence();
         if (SB_BOUNDS(rt < p.n_rtiles && mt < p.n_mtiles, p.status) &&
             !((int)blockIdx.x == p.skip_unit && ls == p.skip_step))
-          st_release(p.flags + (size_t)rt * p.n_mtiles + mt, (uint32_t)(ls + 1));
+          st_release(p.flags + ((size_t)rt * p.n_mtiles + mt) * p.flag_stride, (uint32_t)(ls + 1));
       }
       // NMFA: the next stage's noise, while the column's units finish this sweep and the next
       // contraction streams in: its first chunk after this stage's first sweep (whose z0 is
