@@ -145,16 +145,42 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   } else {
     // ---------------- epilogue ----------------
+    // A thread updates its row's state 16 replica columns at a time. The state does not depend on
+    // the contraction, so the first group's x and y are loaded before the accumulator wait (their
+    // latency overlaps the MMA), and each next group's loads are issued before the current group's
+    // stores (two groups in flight).
+    constexpr int kGroup = 16;
+    constexpr int kSub = kGroup / 16;
+    constexpr int kGroups = kHalf / kGroup;
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     const int c_lo = half * kHalf;
     const uint32_t lane_off = (uint32_t)(32 * q) << 16;
     int li = 0;
+#pragma unroll 1
     for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++li) {
       const GItem w = items[it];
       const GInst *in = insts + w.inst;
       const int ab = li & 1;
       const uint32_t t_acc = tmem + ab * NR;
+      const int n = in->n, R = in->R, xp = in->xp, kb = in->kbytes;
+      const int row = w.m0 + 32 * q + lane;
+      // element (replica r, spin row) of x and y sits at r * xp + row: 32-bit offsets from the row's
+      // base (an instance's state is far below 2^32 elements) keep the group's addresses cheap
+      float *xs = in->x + row, *ys = in->y + row;
+      const uint32_t uxp = (uint32_t)xp;
+      float xv[kGroup], yv[kGroup];
+      auto load_group = [&](int g0, float (&ox)[kGroup], float (&oy)[kGroup]) {
+        const int rlim = row < n ? R - (w.r0 + g0) : 0;  // columns j < rlim are inside the instance
+        const uint32_t o0 = (uint32_t)(w.r0 + g0) * uxp;
+#pragma unroll
+        for (int j = 0; j < kGroup; ++j) {
+          const uint32_t o = o0 + (uint32_t)j * uxp;
+          ox[j] = j < rlim ? xs[o] : 0.0f;
+          if constexpr (!kEOnly) oy[j] = j < rlim ? ys[o] : 0.0f;
+        }
+      };
+      load_group(c_lo, xv, yv);
       const bool got = ptx::mbar_wait(&accf_bar[ab], (uint32_t)(li >> 1) & 1);
       if (!epi_all(got)) {
         ok = false;
@@ -162,35 +188,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       ptx::tc_fence_after();
       const int t = tick - in->t0;
-      const int n = in->n, R = in->R, xp = in->xp, kb = in->kbytes;
-      const int row = w.m0 + 32 * q + lane;
       const float hv = (in->h && row < n) ? in->h[row] : 0.0f;
       const float pump = kEOnly ? 0.0f : in->pumps[t];
       const float c0 = in->c0, dt = in->dt, dta0 = in->dta0;
-      float *xs = in->x, *ys = in->y;
       uint8_t *vn = in->v[(t + 1) & 1];
 #pragma unroll 1
-      for (int c = c_lo; c < c_lo + kHalf; c += 16) {
-        uint32_t va[16];
-        ptx::tmem_ld16(t_acc + lane_off + c, va);
-        // all of the chunk's state loads first: they are independent and may all be in flight
-        // (interleaving them with the stores below would serialise them on possible aliasing)
-        float xv[16], yv[16];
+      for (int gi = 0; gi < kGroups; ++gi) {
+        const int g0 = c_lo + gi * kGroup;
+        float xn[kGroup], yn[kGroup];
+        if (gi + 1 < kGroups) load_group(g0 + kGroup, xn, yn);
+        uint32_t va[kSub][16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = w.r0 + c + j;
-          const bool ins = row < n && r < R;
-          const size_t k = (size_t)r * xp + row;
-          xv[j] = ins ? xs[k] : 0.0f;
-          if constexpr (!kEOnly) yv[j] = ins ? ys[k] : 0.0f;
-        }
+        for (int s = 0; s < kSub; ++s) ptx::tmem_ld16(t_acc + lane_off + g0 + 16 * s, va[s]);
         ptx::tmem_ld_wait();
-        float e2[16];
+        float e2[kGroup];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int r = w.r0 + c + j;
+        for (int j = 0; j < kGroup; ++j) {
+          const int r = w.r0 + g0 + j;
           const bool ins = row < n && r < R;
-          const float f = __uint_as_float(va[j]);
+          const float f = __uint_as_float(va[j / 16][j % 16]);
           float x = xv[j];
           if constexpr (kEOnly) {
             const float sg = sgnf(x);
@@ -203,48 +219,60 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
         }
         if constexpr (!kEOnly) {
+          const int rlim = row < n ? R - (w.r0 + g0) : 0;
+          const uint32_t o0 = (uint32_t)(w.r0 + g0) * uxp, v0 = (uint32_t)(w.r0 + g0) * (uint32_t)kb;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int r = w.r0 + c + j;
-            if (row < n && r < R && SB_BOUNDS(row < xp && (FP4 || row < kb) && r < in->Rp, status)) {
-              const size_t k = (size_t)r * xp + row;
-              xs[k] = xv[j];
-              ys[k] = yv[j];
-              if constexpr (!FP4) vn[(size_t)r * kb + row] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+          for (int j = 0; j < kGroup; ++j) {
+            if (j < rlim && SB_BOUNDS(row < xp && (FP4 || row < kb) && w.r0 + g0 + j < in->Rp, status)) {
+              const uint32_t o = o0 + (uint32_t)j * uxp;
+              xs[o] = xv[j];
+              ys[o] = yv[j];
+              if constexpr (!FP4) vn[row + v0 + (uint32_t)j * (uint32_t)kb] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
             }
           }
           if constexpr (FP4) {
-            // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte: the
-            // even lane writes replicas c..c+7, the odd lane c+8..c+15
-            uint32_t nib_lo = 0, nib_hi = 0;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const bool ins = row < n && w.r0 + c + j < R;
-              const uint32_t nib = ins ? (xv[j] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
-              if (j < 8) nib_lo |= nib << (4 * j);
-              else nib_hi |= nib << (4 * (j - 8));
-            }
-            const bool odd = (lane & 1) != 0;
-            const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
-            const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
-            const uint32_t lo_n = odd ? o_hi : nib_lo, hi_n = odd ? nib_hi : o_lo;
-            const int row_e = row & ~1;
+            for (int s = 0; s < kSub; ++s) {
+              // spins 2s (even lane, low nibble) and 2s + 1 (odd lane, high nibble) share a byte: per
+              // 16 columns, the even lane writes replicas c..c+7, the odd lane c+8..c+15
+              const int c = g0 + 16 * s;
+              uint32_t nib_lo = 0, nib_hi = 0;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int r = w.r0 + c + (odd ? 8 : 0) + j;
-              if (row_e < n && r < R && SB_BOUNDS((row_e >> 1) < kb && r < in->Rp, status))
-                vn[(size_t)r * kb + (row_e >> 1)] =
-                    (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
+              for (int j = 0; j < 16; ++j) {
+                const bool ins = row < n && w.r0 + c + j < R;
+                const uint32_t nib = ins ? (xv[16 * s + j] > 0.0f ? kE2m1Plus : kE2m1Minus) : 0u;
+                if (j < 8) nib_lo |= nib << (4 * j);
+                else nib_hi |= nib << (4 * (j - 8));
+              }
+              const bool odd = (lane & 1) != 0;
+              const uint32_t o_lo = __shfl_xor_sync(0xffffffffu, nib_lo, 1);
+              const uint32_t o_hi = __shfl_xor_sync(0xffffffffu, nib_hi, 1);
+              const uint32_t lo_n = odd ? o_hi : nib_lo, hi_n = odd ? nib_hi : o_lo;
+              const int row_e = row & ~1;
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int r = w.r0 + c + (odd ? 8 : 0) + j;
+                if (row_e < n && r < R && SB_BOUNDS((row_e >> 1) < kb && r < in->Rp, status))
+                  vn[(size_t)r * kb + (row_e >> 1)] =
+                      (uint8_t)(((lo_n >> (4 * j)) & 0xFu) | (((hi_n >> (4 * j)) & 0xFu) << 4));
+              }
             }
           }
         }
         if constexpr (kEOnly) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < kGroup; ++j) {
             float v = e2[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) ered[q][c + j] = v;
+            if (lane == 0) ered[q][g0 + j] = v;
+          }
+        }
+        if (gi + 1 < kGroups) {
+#pragma unroll
+          for (int j = 0; j < kGroup; ++j) {
+            xv[j] = xn[j];
+            if constexpr (!kEOnly) yv[j] = yn[j];
           }
         }
       }
