@@ -328,9 +328,11 @@ const char *bind(TcEngine *e, cudaError_t *ce) {
   g.jinv = e->jinv;
   g.xscale = e->s.dtype == kTcFp16Split ? 16384.0f : 1.0f;  // |x| <= 1 -> [-2^14, 2^14]
   g.wait_cycles = ptx::kWaitCycles;
-  // split operands: 8 chunks (512 spins of K) per accumulation segment; SB_SPLIT_SEG_CHUNKS
-  // overrides it (shorter segments take fewer roundings each and cost more hand-offs)
-  g.seg_chunks = 8;
+  // split operands: K chunks per accumulation segment (shorter segments take fewer roundings each
+  // and cost more hand-offs). BF16 hi + lo: 8 (512 spins); its error is mostly the representation's
+  // (16 bits per operand). FP16 hi + lo keeps 22 bits, so the accumulation's rounding is its error
+  // and 2 chunks pay (~5 % more time per solve). SB_SPLIT_SEG_CHUNKS overrides both.
+  g.seg_chunks = e->s.dtype == kTcFp16Split ? 2 : 8;
   if (const char *sc = getenv("SB_SPLIT_SEG_CHUNKS")) {
     const int v = atoi(sc);
     if (v > 0) g.seg_chunks = v;

@@ -86,6 +86,8 @@ NCU_TRAFFIC = {
     # uneven batch: measured bytes per algorithmic byte on a 48-instance batch (441.2 MB of
     # 451.8 MB); the launch of the full batch is scaled by its algorithmic bytes
     "uneven-batch": (441.2 / 451.8, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
+    # the same with E2M1 couplings (255.2 MB of 284.0 MB)
+    "uneven-batch-e2m1": (255.2 / 284.0, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
 }
 
 
@@ -564,10 +566,10 @@ def run_batch(args, rank, world, local_rank):
     # J + per spin-replica: x, y read and written (16 B) and the next sign operand (1 B, or 1/2)
     bytes_per_launch = np_kp + sum(p.n for p in probs) * R * (16.5 if fp4 else 17.0)
     achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
+    tkey = "uneven-batch-e2m1" if fp4 else "uneven-batch"
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": NCU_TRAFFIC["uneven-batch"][0] * bytes_per_launch if not fp4 else None,
-            "traffic_source": NCU_TRAFFIC["uneven-batch"][1] + " (48-instance capture, scaled by algorithmic bytes)"
-            if not fp4 else None,
+            "traffic": NCU_TRAFFIC[tkey][0] * bytes_per_launch,
+            "traffic_source": NCU_TRAFFIC[tkey][1] + " (48-instance capture, scaled by algorithmic bytes)",
             "kernel": "grouped_kernel (one launch per SB step)",
             "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
             "peak_source": f"{src} HBM copy"}

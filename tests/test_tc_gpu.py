@@ -261,15 +261,18 @@ def test_fp16_split_integer_dsb_bit_exact(ctx):
 
 
 def test_fp16_split_real_couplings_vs_fp64():
-    """FP16 hi + lo operands (22 bits per operand) on the batched bSB workload's distribution: one
-    step at N=1024 has a field error of at most 2e-7 rms against FP64 (measured 1.15e-7; BF16 hi + lo
-    2.8e-7), and the full shape (N=8192, R=256) stays within 5e-6 of FP64 over 2 steps (measured 2.5e-6)."""
+    """FP16 hi + lo operands (22 bits per operand, K accumulated in segments of 128 spins) on the
+    batched bSB workload's distribution against FP64. One step at N=1024: field error at most 6e-8
+    rms (measured 3.9e-8; BF16 hi + lo 2.8e-7, the plain FP32 kernel 2.4e-8). The full shape
+    (N=8192, R=256): within 2e-6 of FP64 over 2 steps (measured 8.9e-7), and after 10 steps no more
+    replicas off by more than 1e-2 than the plain FP32 kernel has on the same run (measured 0 and 0),
+    with the 99th percentile of |x - x_fp64| below 2e-5 (measured 8.5e-6)."""
     import torch
 
     dev = torch.device("cuda", 0)
     ctx = sb.Context(0)
     try:
-        for n, K in ((1024, 1), (8192, 2)):
+        for n, K in ((1024, 1), (8192, 2), (8192, 10)):
             J, h = instances.gaussian(n, seed=1234)
             prob = sb.Problem.from_dense(J, h)
             c0 = float(prob.default_c0())
@@ -280,8 +283,20 @@ def test_fp16_split_real_couplings_vs_fp64():
             x64, y64 = _fp64_bsb(torch, J, h, x0, y0, c0, K, dev)
             if K == 1:
                 dF = (torch.from_numpy(res.final_y).double().to(dev) - y64) / (1.25 * c0)
-                assert float(dF.pow(2).mean().sqrt()) <= 2e-7
-            else:
-                assert float((torch.from_numpy(res.final_x).double().to(dev) - x64).abs().max()) <= 5e-6
+                assert float(dF.pow(2).mean().sqrt()) <= 6e-8
+                continue
+            d = (torch.from_numpy(res.final_x).double().to(dev) - x64).abs()
+            if K == 2:
+                assert float(d.max()) <= 2e-6
+                continue
+            f32 = ctx.solve(prob, sb.Params.default(sb.BSB, steps=K, replicas=256, seed=3, field_mode=sb.FIELD_FP32),
+                            want_state=True)
+            d32 = (torch.from_numpy(f32.final_x).double().to(dev) - x64).abs()
+            off = int((d.max(dim=1).values > 1e-2).sum())
+            off32 = int((d32.max(dim=1).values > 1e-2).sum())
+            p99 = float(d.flatten().kthvalue(int(0.99 * d.numel())).values)
+            print(f"fp16x2 after {K} steps: replicas off by > 1e-2: {off} (plain FP32 kernel: {off32}), p99 {p99:.3g}")
+            assert off <= off32
+            assert p99 <= 2e-5
     finally:
         ctx.close()
