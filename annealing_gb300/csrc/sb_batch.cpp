@@ -2,8 +2,9 @@
 //
 // The reference solves one instance per program run and its trials one after another
 // (SB/CUDA_GPU/m2_opt.cu:152); a batch here advances every instance and every replica of it in
-// one grouped launch per SB step, the step loop replayed from a CUDA graph. Per instance the
-// outputs are those of sb_solve (best spins, per-replica energies, host int64 re-check).
+// one grouped launch per SB step and operand bucket (packed E2M1 where the couplings allow it,
+// FP8 for the rest), the step loop replayed from a CUDA graph. Per instance the outputs are those
+// of sb_solve (best spins, per-replica energies, host int64 re-check).
 #include <math.h>
 #include <string.h>
 
@@ -22,11 +23,19 @@
 #include "sb_host.h"
 #include "sb_internal.h"
 
+// One operand bucket of a batch: the instances whose couplings share an operand type (packed E2M1
+// when every coupling is an integer |J| <= 4, else FP8), advanced by their own grouped launch per
+// step with their own autotuned replica tile and item order.
+struct sb_bucket {
+  sbk::Grouped *g = nullptr;
+  std::vector<int> members;  // batch index of each resident instance, in residence order
+};
+
 struct sb_batch {
   sb_ctx *ctx = nullptr;
   std::vector<const sb_problem *> probs;
   sb_params prm{};
-  sbk::Grouped *g = nullptr;
+  std::vector<sb_bucket> buckets;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // compact copies of the couplings for the host re-check, built in the background (the first
   // runs' device time hides them)
@@ -38,18 +47,19 @@ namespace {
 std::mutex g_tune_mu;
 std::map<std::string, std::pair<int, int>> g_tune_cache;
 
-sb_status init_all(sb_batch *b, uint64_t seed, std::string &err) {
-  for (size_t k = 0; k < b->g->insts.size(); ++k) {
-    sb_status s = b->g->init_state(b->g->insts[k], seed + k, err);
+// instance k of the batch starts from seed + k, whichever bucket holds it
+sb_status init_all(sb_bucket &bk, uint64_t seed, std::string &err) {
+  for (size_t j = 0; j < bk.g->insts.size(); ++j) {
+    sb_status s = bk.g->init_state(bk.g->insts[j], seed + (uint64_t)bk.members[j], err);
     if (s != SB_OK) return s;
   }
   return SB_OK;
 }
 
-// Times a few steps of each (replica tile, item order) candidate on the batch itself and keeps the
-// fastest; the choice is cached by (replica count, total work bucket, batch size bucket).
-sb_status autotune(sb_batch *b, std::string &err) {
-  sbk::Grouped &g = *b->g;
+// Times a few steps of each (replica tile, item order) candidate on the bucket itself and keeps the
+// fastest; the choice is cached by (replica count, total work bucket, batch size bucket, operands).
+sb_status autotune(sb_batch *b, sb_bucket &bk, std::string &err) {
+  sbk::Grouped &g = *bk.g;
   const std::string key = g.tune_key();
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -70,7 +80,7 @@ sb_status autotune(sb_batch *b, std::string &err) {
       if (s != SB_OK) return s;
       g.set_order(c.second);
       if ((s = g.sync_tables(err)) != SB_OK) return s;
-      if ((s = init_all(b, b->prm.seed, err)) != SB_OK) return s;
+      if ((s = init_all(bk, b->prm.seed, err)) != SB_OK) return s;
       if (g.run_steps(0, 1, false) != cudaSuccess) continue;
       cudaEventRecord(b->ev0, st);
       if (g.run_steps(1, 3, false) != cudaSuccess) continue;
@@ -93,7 +103,7 @@ sb_status autotune(sb_batch *b, std::string &err) {
 
 void destroy(sb_batch *b) {
   if (!b) return;
-  delete b->g;
+  for (auto &bk : b->buckets) delete bk.g;
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   delete b;
@@ -120,13 +130,18 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
       return SB_ERR_UNSUPPORTED;
     }
   }
-  // operands: packed E2M1 when every instance's couplings allow it (|J| <= 4), else FP8 E4M3
-  bool fp4 = true;
-  for (int k = 0; k < count; ++k) fp4 = fp4 && sbk::grouped_fp4_exact(&problems[k]);
+  // operands per instance: packed E2M1 where its couplings allow it (integers |J| <= 4; half the
+  // bytes of FP8), else FP8 E4M3; SB_OPERAND_FP8 / SB_OPERAND_FP4 force one type for the batch
+  std::vector<char> fp4(count, 0);
+  bool all_fp4 = true;
+  for (int k = 0; k < count; ++k) {
+    fp4[k] = sbk::grouped_fp4_exact(&problems[k]) ? 1 : 0;
+    all_fp4 = all_fp4 && fp4[k];
+  }
   if (prm->operand_dtype == SB_OPERAND_FP8) {
-    fp4 = false;
+    std::fill(fp4.begin(), fp4.end(), 0);
   } else if (prm->operand_dtype == SB_OPERAND_FP4) {
-    if (!fp4) {
+    if (!all_fp4) {
       err = "E2M1 operands need integer couplings |J| <= 4 in every problem of the batch";
       return SB_ERR_UNSUPPORTED;
     }
@@ -139,7 +154,15 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
   b->prm = *prm;
   b->probs.resize(count);
   const int R = prm->replicas;
-  b->g = new sbk::Grouped(ctx->stream, R <= 32 ? 32 : (R <= 64 ? 64 : 128), 0, fp4);
+  const int nr = R <= 32 ? 32 : (R <= 64 ? 64 : 128);  // the autotuner may retile each bucket
+  for (int f : {1, 0}) {
+    sb_bucket bk;
+    for (int k = 0; k < count; ++k)
+      if (fp4[k] == f) bk.members.push_back(k);
+    if (bk.members.empty()) continue;
+    bk.g = new sbk::Grouped(ctx->stream, nr, 0, f == 1);
+    b->buckets.push_back(std::move(bk));
+  }
   if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
     destroy(b);
     err = "cudaEventCreate";
@@ -153,7 +176,6 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
   std::vector<std::string> errs(nw);
   std::atomic<int> next{0};
   std::atomic<bool> failed{false};
-  const int nr = b->g->nr;
   auto worker = [&](int w) {
     if (cudaSetDevice(ctx->device) != cudaSuccess) {
       errs[w] = "cudaSetDevice";
@@ -169,7 +191,8 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     {
       sbk::Staging stg;
       for (int k; !failed.load() && (k = next.fetch_add(1)) < count;) {
-        const sb_status st = sbk::Grouped::prepare(hosts[k], &problems[k], prm, prm->seed + k, k, nr, ps, stg, errs[w], fp4);
+        const sb_status st =
+            sbk::Grouped::prepare(hosts[k], &problems[k], prm, prm->seed + k, k, nr, ps, stg, errs[w], fp4[k] != 0);
         if (st != SB_OK) {
           sts[k] = st;
           failed = true;
@@ -198,15 +221,16 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     destroy(b);
     return first;
   }
-  for (int k = 0; k < count; ++k) {
-    b->probs[k] = &problems[k];
-    b->g->attach(hosts[k], 0);
-  }
-  sb_status s = autotune(b, err);
-  if (s == SB_OK) s = b->g->sync_tables(err);
-  if (s != SB_OK) {
-    destroy(b);
-    return s;
+  for (int k = 0; k < count; ++k) b->probs[k] = &problems[k];
+  for (auto &bk : b->buckets)
+    for (int k : bk.members) bk.g->attach(hosts[k], 0);
+  for (auto &bk : b->buckets) {
+    sb_status s = autotune(b, bk, err);
+    if (s == SB_OK) s = bk.g->sync_tables(err);
+    if (s != SB_OK) {
+      destroy(b);
+      return s;
+    }
   }
   b->copies.reset(new sbh::CouplingCopies(
       b->probs, (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2))));
@@ -215,56 +239,76 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
 }
 
 sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
-  sbk::Grouped &g = *b->g;
   cudaStream_t st = b->ctx->stream;
   const int steps = b->prm.steps;
   const auto t_start = std::chrono::steady_clock::now();
-  sb_status s = g.sync_tables(err);
-  if (s != SB_OK) return s;
-  if (cudaMemsetAsync(g.d_status, 0, sizeof(uint32_t), st) != cudaSuccess) return SB_ERR_CUDA;
-  const int64_t l0 = g.launches;
-  cudaEventRecord(b->ev0, st);
-  if ((s = init_all(b, seed, err)) != SB_OK) return s;
-  cudaError_t e = cudaSuccess;
-  double kernel_ms = 0.0;
-  if (b->prm.profile && steps > 0) {
-    std::vector<cudaEvent_t> evs(2 * (size_t)steps);
-    for (auto &ev : evs) cudaEventCreate(&ev);
-    for (int t = 0; t < steps && e == cudaSuccess; ++t) {
-      cudaEventRecord(evs[2 * t], st);
-      e = g.run_steps(t, 1, false);
-      cudaEventRecord(evs[2 * t + 1], st);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    for (int t = 0; t < steps && e == cudaSuccess; ++t) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, evs[2 * t], evs[2 * t + 1]);
-      kernel_ms += ms;
-    }
-    for (auto &ev : evs) cudaEventDestroy(ev);
-    kernel_ms /= steps;
-  } else {
-    e = g.run_steps(0, steps, true);
+  int64_t l0 = 0;
+  for (auto &bk : b->buckets) {
+    sb_status s = bk.g->sync_tables(err);
+    if (s != SB_OK) return s;
+    if (cudaMemsetAsync(bk.g->d_status, 0, sizeof(uint32_t), st) != cudaSuccess) return SB_ERR_CUDA;
+    l0 += bk.g->launches;
   }
-  if (e == cudaSuccess) e = g.energy_pass(steps);
+  cudaEventRecord(b->ev0, st);
+  for (auto &bk : b->buckets) {
+    sb_status s = init_all(bk, seed, err);
+    if (s != SB_OK) return s;
+  }
+  cudaError_t e = cudaSuccess;
+  double kernel_ms = 0.0;  // profile: device time of one SB step, all buckets' launches
+  for (auto &bk : b->buckets) {
+    sbk::Grouped &g = *bk.g;
+    if (b->prm.profile && steps > 0) {
+      std::vector<cudaEvent_t> evs(2 * (size_t)steps);
+      for (auto &ev : evs) cudaEventCreate(&ev);
+      for (int t = 0; t < steps && e == cudaSuccess; ++t) {
+        cudaEventRecord(evs[2 * t], st);
+        e = g.run_steps(t, 1, false);
+        cudaEventRecord(evs[2 * t + 1], st);
+      }
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      double ms_sum = 0.0;
+      for (int t = 0; t < steps && e == cudaSuccess; ++t) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, evs[2 * t], evs[2 * t + 1]);
+        ms_sum += ms;
+      }
+      for (auto &ev : evs) cudaEventDestroy(ev);
+      kernel_ms += ms_sum / steps;
+    } else if (e == cudaSuccess) {
+      e = g.run_steps(0, steps, true);
+    }
+    if (e == cudaSuccess) e = g.energy_pass(steps);
+  }
   cudaEventRecord(b->ev1, st);
-  const size_t count = g.insts.size();
+  const size_t count = b->probs.size();
+  // (bucket, position) of every batch index
+  std::vector<const sbk::GHost *> inst(count, nullptr);
+  std::vector<bool> inst_fp4(count, false);
+  for (auto &bk : b->buckets)
+    for (size_t j = 0; j < bk.members.size(); ++j) {
+      inst[bk.members[j]] = &bk.g->insts[j];
+      inst_fp4[bk.members[j]] = bk.g->fp4;
+    }
   std::vector<std::vector<double>> energies(count);
-  uint32_t status = 0;
+  std::vector<uint32_t> status(b->buckets.size(), 0);
   for (size_t k = 0; k < count && e == cudaSuccess; ++k) {
-    energies[k].resize(g.insts[k].R);
-    e = cudaMemcpyAsync(energies[k].data(), g.insts[k].energy, (size_t)g.insts[k].R * sizeof(double),
+    energies[k].resize(inst[k]->R);
+    e = cudaMemcpyAsync(energies[k].data(), inst[k]->energy, (size_t)inst[k]->R * sizeof(double),
                         cudaMemcpyDeviceToHost, st);
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, g.d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  for (size_t i = 0; i < b->buckets.size() && e == cudaSuccess; ++i)
+    e = cudaMemcpyAsync(&status[i], b->buckets[i].g->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     err = std::string("batch run: ") + cudaGetErrorString(e);
     return SB_ERR_CUDA;
   }
-  if (status) {
-    err = sbh::device_status_text(status);
-    return (status & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
+  uint32_t any = 0;
+  for (uint32_t v : status) any |= v;
+  if (any) {
+    err = sbh::device_status_text(any);
+    return (any & sbk::kErrWaitTimeout) ? SB_ERR_TIMEOUT : SB_ERR_CUDA;
   }
   float dev_ms = 0;
   cudaEventElapsedTime(&dev_ms, b->ev0, b->ev1);
@@ -272,7 +316,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
   std::vector<int> best(count, 0);
   std::vector<std::vector<float>> xb(count);
   for (size_t k = 0; k < count; ++k) {
-    const auto &gi = g.insts[k];
+    const auto &gi = *inst[k];
     for (int r = 1; r < gi.R; ++r)
       if (energies[k][r] < energies[k][best[k]]) best[k] = r;
     xb[k].resize(gi.n);
@@ -300,7 +344,7 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
   for (unsigned w = 0; w < nth; ++w)
     th.emplace_back([&, w] {
       for (size_t k = w; k < count; k += nth) {
-        const auto &gi = g.insts[k];
+        const auto &gi = *inst[k];
         spins[k].resize(gi.n);
         for (int i = 0; i < gi.n; ++i) spins[k][i] = xb[k][i] > 0.0f ? 1 : -1;
         if (b->copies->energy(k, spins[k].data(), &e64[k], 1) == SB_OK)
@@ -311,7 +355,9 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
   const double total_ms =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   double updates = 0;
-  for (size_t k = 0; k < count; ++k) updates += (double)g.insts[k].n * g.insts[k].R * steps;
+  int64_t launches = -l0;
+  for (size_t k = 0; k < count; ++k) updates += (double)inst[k]->n * inst[k]->R * steps;
+  for (auto &bk : b->buckets) launches += bk.g->launches;
   for (size_t k = 0; k < count; ++k) {
     sb_result &r = res[k];
     if (r.best_spins) memcpy(r.best_spins, spins[k].data(), spins[k].size());
@@ -320,12 +366,12 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
     r.best_energy_i64 = e64[k];
     r.best_replica = best[k];
     r.field_mode_used = SB_FIELD_TC;
-    r.field_dtype_used = g.fp4 ? SB_OPERAND_FP4 : SB_OPERAND_FP8;
+    r.field_dtype_used = inst_fp4[k] ? SB_OPERAND_FP4 : SB_OPERAND_FP8;
     r.energy_check_ok = okv[k];
     r.device_ms = dev_ms;
     r.kernel_ms_avg = kernel_ms;
     r.steps_per_launch = 1;
-    r.kernel_launches = g.launches - l0 + 2 * (int64_t)count;  // + init and sign kernels per instance
+    r.kernel_launches = launches + 2 * (int64_t)count;  // + init and sign kernels per instance
     r.total_ms = total_ms;
     r.spin_updates_per_s = dev_ms > 0 ? updates / (dev_ms * 1e-3) : 0.0;
   }

@@ -287,10 +287,12 @@ int64_t sb_plan_footprint(const sb_problem *p, const sb_params *params);
 
 /* ---- batches: many instances of uneven size, solved together ----
  * The reference runs one instance per program run and its trials one after another
- * (SB/CUDA_GPU/m2_opt.cu:152). A batch advances every instance, with all of its replicas, in one
- * grouped tensor-core launch per SB step (dSB, integer |J| <= 16 on exact FP8 operands), the step
- * loop replayed from a CUDA graph; the replica tile and work order are chosen by timing the
- * candidates on the batch itself (cached per shape). params is shared; instance k uses seed
+ * (SB/CUDA_GPU/m2_opt.cu:152). A batch advances every instance, with all of its replicas, by
+ * grouped tensor-core launches, the step loop replayed from a CUDA graph (dSB, integer |J| <= 16).
+ * Instances whose couplings are integers |J| <= 4 run on packed E2M1 operands (half the bytes), the
+ * others on FP8 (params->operand_dtype SB_OPERAND_FP8 / SB_OPERAND_FP4 forces one type); each operand
+ * bucket has one grouped launch per SB step, with its replica tile and work order chosen by timing
+ * the candidates on the bucket itself (cached per shape). params is shared; instance k uses seed
  * seed + k; results[k] is filled as sb_solve would fill it (arrays sized for instance k). The
  * problems must stay alive until sb_batch_destroy. */
 typedef struct sb_batch sb_batch;

@@ -60,3 +60,31 @@ def test_batch_profile_reports_step_kernel_time(ctx):
     prm = sb.Params.default(sb.DSB, steps=12, replicas=64, field_mode=sb.FIELD_TC, profile=1)
     res = ctx.batch(probs, prm).run()
     assert res[0].kernel_ms_avg > 0 and res[0].steps_per_launch == 1
+
+
+def test_batch_mixed_operands_per_instance(ctx):
+    """A batch mixing couplings |J| <= 4 and |J| <= 9 runs two operand buckets: the first instances on
+    packed E2M1, the others on FP8, each bit-exact against the oracle, in one run."""
+    ns = [64, 129, 300, 513, 700, 1000]
+    insts = []
+    for k, n in enumerate(ns):
+        jmax = 4 if k % 2 == 0 else 9
+        J = instances.erdos_renyi(n, 0.5, seed=70 + k, jmax=jmax, allow_zero=True)
+        if jmax == 9:
+            J[0, 1] = J[1, 0] = 9.0  # at least one coupling E2M1 cannot hold
+        h = np.random.default_rng(k).integers(-3, 4, n).astype(np.float32) if k == 3 else None
+        insts.append((J, h))
+    probs = [sb.Problem.from_dense(J, h) for J, h in insts]
+    steps, seed, R = 25, 300, 64
+    prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
+    batch = ctx.batch(probs, prm, want_state=True)
+    res = batch.run()
+    assert [r.field_dtype for r in res] == ["fp4e2m1", "fp8e4m3"] * 3
+    for k, ((J, h), p, r) in enumerate(zip(insts, probs, res)):
+        x, y = orc.init_uniform(J.shape[0], R, seed + k)
+        orc.sb_run_f32(2, J, h, x, y, steps, 1.0, p.default_c0(), 1.25)
+        np.testing.assert_array_equal(r.final_x, x, err_msg=f"instance {k}")
+        np.testing.assert_array_equal(r.final_y, y, err_msg=f"instance {k}")
+        np.testing.assert_array_equal(r.replica_energies, orc.energies_of_x(J, h, x))
+        assert r.energy_check_ok
+    batch.close()
