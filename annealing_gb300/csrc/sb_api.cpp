@@ -121,9 +121,13 @@ sb_status resolve_mode(const sb_problem *p, const sb_params *prm, int &mode, int
     return SB_ERR_UNSUPPORTED;
   }
   const int want = prm->operand_dtype;
-  if (want < SB_OPERAND_AUTO || want > SB_OPERAND_FP16X2) {
+  if (want < SB_OPERAND_AUTO || want > SB_OPERAND_FP6) {
     err = "unknown operand_dtype";
     return SB_ERR_INVALID_ARG;
+  }
+  if (want == SB_OPERAND_FP6) {
+    err = "E2M3 operands run on the grouped path (sb_batch_*, serving)";
+    return SB_ERR_UNSUPPORTED;
   }
   if (prm->variant == SB_DSB) {
     const bool fp4 = p->integer_valued && p->max_abs_j <= 4 && sbk::tc_fp4_fits(p->n, prm->replicas);

@@ -3,7 +3,7 @@
 // The reference solves one instance per program run and its trials one after another
 // (SB/CUDA_GPU/m2_opt.cu:152); a batch here advances every instance and every replica of it in
 // one grouped launch per SB step and operand bucket (packed E2M1 where the couplings allow it,
-// FP8 for the rest), the step loop replayed from a CUDA graph. Per instance the outputs are those
+// packed E2M3 for the rest), the step loop replayed from a CUDA graph. Per instance the outputs are those
 // of sb_solve (best spins, per-replica energies, host int64 re-check).
 #include <math.h>
 #include <string.h>
@@ -24,8 +24,8 @@
 #include "sb_internal.h"
 
 // One operand bucket of a batch: the instances whose couplings share an operand type (packed E2M1
-// when every coupling is an integer |J| <= 4, else FP8), advanced by their own grouped launch per
-// step with their own autotuned replica tile and item order.
+// when every coupling is an integer |J| <= 4, else packed E2M3), advanced by their own grouped
+// launch per step with their own autotuned replica tile and item order.
 struct sb_bucket {
   sbk::Grouped *g = nullptr;
   std::vector<int> members;  // batch index of each resident instance, in residence order
@@ -131,22 +131,23 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     }
   }
   // operands per instance: packed E2M1 where its couplings allow it (integers |J| <= 4; half the
-  // bytes of FP8), else FP8 E4M3; SB_OPERAND_FP8 / SB_OPERAND_FP4 force one type for the batch
-  std::vector<char> fp4(count, 0);
+  // bytes of FP8), else packed E2M3 (six bits per coupling); SB_OPERAND_FP8 / SB_OPERAND_FP6 /
+  // SB_OPERAND_FP4 force one type for the batch
+  std::vector<int> op(count, sbk::kGopE2m3);
   bool all_fp4 = true;
   for (int k = 0; k < count; ++k) {
-    fp4[k] = sbk::grouped_fp4_exact(&problems[k]) ? 1 : 0;
-    all_fp4 = all_fp4 && fp4[k];
+    if (sbk::grouped_fp4_exact(&problems[k])) op[k] = sbk::kGopE2m1;
+    all_fp4 = all_fp4 && op[k] == sbk::kGopE2m1;
   }
-  if (prm->operand_dtype == SB_OPERAND_FP8) {
-    std::fill(fp4.begin(), fp4.end(), 0);
+  if (prm->operand_dtype == SB_OPERAND_FP8 || prm->operand_dtype == SB_OPERAND_FP6) {
+    std::fill(op.begin(), op.end(), prm->operand_dtype == SB_OPERAND_FP8 ? sbk::kGopFp8 : sbk::kGopE2m3);
   } else if (prm->operand_dtype == SB_OPERAND_FP4) {
     if (!all_fp4) {
       err = "E2M1 operands need integer couplings |J| <= 4 in every problem of the batch";
       return SB_ERR_UNSUPPORTED;
     }
   } else if (prm->operand_dtype != SB_OPERAND_AUTO) {
-    err = "the grouped path runs E2M1 or FP8 operands";
+    err = "the grouped path runs E2M1, E2M3 or FP8 operands";
     return SB_ERR_UNSUPPORTED;
   }
   sb_batch *b = new sb_batch();
@@ -155,12 +156,12 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
   b->probs.resize(count);
   const int R = prm->replicas;
   const int nr = R <= 32 ? 32 : (R <= 64 ? 64 : 128);  // the autotuner may retile each bucket
-  for (int f : {1, 0}) {
+  for (int o : {sbk::kGopE2m1, sbk::kGopE2m3, sbk::kGopFp8}) {
     sb_bucket bk;
     for (int k = 0; k < count; ++k)
-      if (fp4[k] == f) bk.members.push_back(k);
+      if (op[k] == o) bk.members.push_back(k);
     if (bk.members.empty()) continue;
-    bk.g = new sbk::Grouped(ctx->stream, nr, 0, f == 1);
+    bk.g = new sbk::Grouped(ctx->stream, nr, 0, o);
     b->buckets.push_back(std::move(bk));
   }
   if (cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
@@ -192,7 +193,7 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
       sbk::Staging stg;
       for (int k; !failed.load() && (k = next.fetch_add(1)) < count;) {
         const sb_status st =
-            sbk::Grouped::prepare(hosts[k], &problems[k], prm, prm->seed + k, k, nr, ps, stg, errs[w], fp4[k] != 0);
+            sbk::Grouped::prepare(hosts[k], &problems[k], prm, prm->seed + k, k, nr, ps, stg, errs[w], op[k]);
         if (st != SB_OK) {
           sts[k] = st;
           failed = true;
@@ -284,11 +285,11 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
   const size_t count = b->probs.size();
   // (bucket, position) of every batch index
   std::vector<const sbk::GHost *> inst(count, nullptr);
-  std::vector<bool> inst_fp4(count, false);
+  std::vector<int> inst_op(count, sbk::kGopFp8);
   for (auto &bk : b->buckets)
     for (size_t j = 0; j < bk.members.size(); ++j) {
       inst[bk.members[j]] = &bk.g->insts[j];
-      inst_fp4[bk.members[j]] = bk.g->fp4;
+      inst_op[bk.members[j]] = bk.g->op;
     }
   std::vector<std::vector<double>> energies(count);
   std::vector<uint32_t> status(b->buckets.size(), 0);
@@ -366,7 +367,8 @@ sb_status run(sb_batch *b, uint64_t seed, sb_result *res, std::string &err) {
     r.best_energy_i64 = e64[k];
     r.best_replica = best[k];
     r.field_mode_used = SB_FIELD_TC;
-    r.field_dtype_used = inst_fp4[k] ? SB_OPERAND_FP4 : SB_OPERAND_FP8;
+    r.field_dtype_used = inst_op[k] == sbk::kGopE2m1 ? SB_OPERAND_FP4
+                         : inst_op[k] == sbk::kGopE2m3 ? SB_OPERAND_FP6 : SB_OPERAND_FP8;
     r.energy_check_ok = okv[k];
     r.device_ms = dev_ms;
     r.kernel_ms_avg = kernel_ms;

@@ -52,6 +52,29 @@ __global__ void g_signs_fp4_kernel(const float *x, int n, int R, int xp, uint8_t
   }
 }
 
+// packed E2M3 signs (+4: 0x18, -4: 0x38, padding 0): one thread per 16 spins of a replica, 12 bytes
+// (value i of the group at bits 6 i .. 6 i + 5, little-endian)
+__global__ void g_signs_fp6_kernel(const float *x, int n, int R, int xp, uint8_t *v, int kb) {
+  const int ng = (n + 15) / 16;
+  const size_t total = (size_t)ng * R;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = k / ng, g = k % ng;
+    uint32_t w[3] = {0u, 0u, 0u};
+    for (int i = 0; i < 16; ++i) {
+      const size_t sp = 16 * g + i;
+      if (sp >= (size_t)n) break;
+      const uint32_t code = x[r * xp + sp] > 0.0f ? 0x18u : 0x38u;
+      const int bit = 6 * i;
+      w[bit >> 5] |= code << (bit & 31);
+      if ((bit & 31) > 26) w[(bit >> 5) + 1] |= code >> (32 - (bit & 31));
+    }
+    uint32_t *dst = reinterpret_cast<uint32_t *>(v + r * kb + 12 * g);
+    dst[0] = w[0];
+    dst[1] = w[1];
+    dst[2] = w[2];
+  }
+}
+
 int grid1(size_t total) {
   size_t g = (total + 255) / 256;
   return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
@@ -82,17 +105,43 @@ bool encode_fp8(CUtensorMap *m, void *base, uint64_t inner, uint64_t outer, uint
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NR, bool FP4>
-const void *gk(int emode) {
-  return emode == kEmodeEnergy ? reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeEnergy, FP4>)
-                               : reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeStep, FP4>);
+// Packed E2M3 operand [rows][kelems] (six bits per value, rows of 3 kelems / 4 bytes): the tensor
+// map spreads each 12 bytes (sixteen values) into a 16-byte shared-memory slot, 128 values per box
+// row (kelems a multiple of 128, rows of a multiple of 32 bytes, base 32-byte aligned).
+bool encode_fp6(CUtensorMap *m, void *base, uint64_t kelems, uint64_t rows, uint32_t box_rows) {
+  auto enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {kelems, rows};
+  const cuuint64_t strides[1] = {kelems * 3 / 4};
+  const cuuint32_t box[2] = {128u, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_16U6_ALIGN16B, 2, base, dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool grouped_kernel_for(int nr, int emode, bool fp4, const void **k, size_t *smem) {
+// the operand maps of an instance: J (box of 128 rows) or V (box of nr rows)
+bool encode_operand(int op, CUtensorMap *m, void *base, int Kp, int kbytes, uint64_t rows, uint32_t box_rows) {
+  return op == kGopE2m3 ? encode_fp6(m, base, (uint64_t)Kp, rows, box_rows)
+                        : encode_fp8(m, base, (uint64_t)kbytes, rows, box_rows);
+}
+
+template <int NR, int OP>
+const void *gk(int emode) {
+  return emode == kEmodeEnergy ? reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeEnergy, OP>)
+                               : reinterpret_cast<const void *>(&grouped_kernel<NR, grouped_stages<NR>(), kEmodeStep, OP>);
+}
+
+template <int NR>
+const void *gk_op(int op, int emode) {
+  return op == kGopE2m1 ? gk<NR, kGopE2m1>(emode) : (op == kGopE2m3 ? gk<NR, kGopE2m3>(emode) : gk<NR, kGopFp8>(emode));
+}
+
+bool grouped_kernel_for(int nr, int emode, int op, const void **k, size_t *smem) {
   switch (nr) {
-    case 32: *k = fp4 ? gk<32, true>(emode) : gk<32, false>(emode); *smem = grouped_smem<32>(); return true;
-    case 64: *k = fp4 ? gk<64, true>(emode) : gk<64, false>(emode); *smem = grouped_smem<64>(); return true;
-    case 128: *k = fp4 ? gk<128, true>(emode) : gk<128, false>(emode); *smem = grouped_smem<128>(); return true;
+    case 32: *k = gk_op<32>(op, emode); *smem = grouped_smem<32>(); return true;
+    case 64: *k = gk_op<64>(op, emode); *smem = grouped_smem<64>(); return true;
+    case 128: *k = gk_op<128>(op, emode); *smem = grouped_smem<128>(); return true;
   }
   return false;
 }
@@ -204,6 +253,54 @@ CouplingSums pack_fp4(const float *J, int n, uint8_t *dst, int Np, int kb) {
   });
 }
 
+// Couplings as packed E2M3 (integers |J| <= 16 held as J / 4), rows of 3 Kp / 4 bytes, sixteen
+// values per 12 bytes (value i at bits 6 i .. 6 i + 5, little-endian), zero padded. E2M3 is
+// (-1)^s 2^(e-1) (1 + m / 8) for e >= 1 and m / 8 for e = 0, so every quarter-integer up to 4 is exact:
+// |J| < 4: e 0, m 2|J|; 4 <= |J| < 8: e 1, m 2|J| - 8; 8 <= |J| < 16: e 2, m |J| - 8; 16: e 3, m 0.
+uint8_t fp6_code(int v) {
+  const int a = v < 0 ? -v : v;
+  int e, m;
+  if (a < 4) e = 0, m = 2 * a;
+  else if (a < 8) e = 1, m = 2 * a - 8;
+  else if (a < 16) e = 2, m = a - 8;
+  else e = 3, m = 0;
+  return (uint8_t)((a == 0 ? 0 : (v < 0 ? 0x20 : 0)) | (e << 3) | m);
+}
+
+CouplingSums pack_fp6(const float *J, int n, uint8_t *dst, int Np, int Kp) {
+  uint8_t lut[33];
+  for (int v = -16; v <= 16; ++v) lut[v + 16] = fp6_code(v);
+  const int kb = Kp / 4 * 3;
+  return pack_rows(n, dst, Np, kb, 2 << 20, [&](int i, uint8_t *d, int32_t &rs, int32_t &rs2) {
+    const float *Ji = J + (size_t)i * n;
+    int32_t s1 = 0, s2 = 0;
+    for (int g = 0; g < Kp / 16; ++g) {
+      uint64_t lo = 0;  // bits 0..63 of the group
+      uint32_t hi = 0;  // bits 64..95
+      for (int t = 0; t < 16; ++t) {
+        const int j = 16 * g + t;
+        const int v = j < n ? (int)Ji[j] : 0;
+        s1 += v;
+        s2 += v * v;
+        const uint64_t c = lut[v + 16];
+        const int bit = 6 * t;
+        if (bit < 64) {
+          lo |= c << bit;
+          if (bit > 58) hi |= (uint32_t)(c >> (64 - bit));
+        } else {
+          hi |= (uint32_t)(c << (bit - 64));
+        }
+      }
+      uint8_t *q = d + 12 * g;
+      for (int b = 0; b < 8; ++b) q[b] = (uint8_t)(lo >> (8 * b));
+      for (int b = 0; b < 4; ++b) q[8 + b] = (uint8_t)(hi >> (8 * b));
+    }
+    const int dg = (int)Ji[i];  // the diagonal does not count
+    rs = s1 - dg;
+    rs2 = s2 - dg * dg;
+  });
+}
+
 int device_sms() {
   int dev = 0, n = 0;
   cudaGetDevice(&dev);
@@ -222,9 +319,9 @@ bool grouped_supports(const sb_problem *p, const sb_params *prm) {
 
 bool grouped_fp4_exact(const sb_problem *p) { return p->integer_valued && p->max_abs_j <= 4; }
 
-int64_t grouped_instance_bytes(int n, int R, int steps, int nr, bool fp4) {
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr, int op) {
   const int64_t Np = (n + 127) / 128 * 128, Rp = (R + nr - 1) / nr * nr, xp = (n + 3) / 4 * 4;
-  const int64_t kb = fp4 ? (n + 255) / 256 * 128 : Np;
+  const int64_t kb = op == kGopE2m1 ? (n + 255) / 256 * 128 : (op == kGopE2m3 ? Np / 4 * 3 : Np);
   return Np * kb + 2 * Rp * kb + 2 * (int64_t)R * xp * 4 + (int64_t)n * 4 + (int64_t)R * 8 + (int64_t)steps * 4 + 4096;
 }
 
@@ -268,7 +365,7 @@ void Grouped::release(GHost &g, cudaStream_t s) {
 }
 
 sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
-                           cudaStream_t st, Staging &stg, std::string &err, bool fp4) {
+                           cudaStream_t st, Staging &stg, std::string &err, int op) {
   g.tag = tag;
   g.prob = p;
   g.n = p->n;
@@ -276,9 +373,10 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   g.steps = prm->steps;
   g.t0 = 0;
   g.Np = (g.n + 127) / 128 * 128;
-  g.fp4 = fp4;
-  g.Kp = fp4 ? (g.n + 255) / 256 * 256 : g.Np;  // K extent in spins: whole 128-byte chunks
-  g.kbytes = fp4 ? g.Kp / 2 : g.Kp;
+  g.op = op;
+  const bool fp4 = op == kGopE2m1;
+  g.Kp = fp4 ? (g.n + 255) / 256 * 256 : g.Np;  // K extent in spins: whole 128-byte shared-memory chunks
+  g.kbytes = fp4 ? g.Kp / 2 : (op == kGopE2m3 ? g.Kp / 4 * 3 : g.Kp);
   g.Rp = (g.R + nr - 1) / nr * nr;
   g.xp = (g.n + 3) / 4 * 4;
   g.c0 = prm->c0;  // or, when unset, the default from the coupling sums the packing gathers
@@ -304,9 +402,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     if ((e = cudaMemcpyAsync(g.h, p->h, (size_t)g.n * sizeof(float), cudaMemcpyHostToDevice, st)) != cudaSuccess)
       return fail("upload h");
   }
-  // couplings: packed to FP8 E4M3 (integers |J| <= 16 are exact, see fp8_code) or to E2M1 pairs
-  // (|J| <= 4) on the host threads into a pinned staging buffer, then one copy into the padded
-  // operand layout: a quarter (an eighth) of the bytes of an FP32 upload.
+  // couplings: packed to FP8 E4M3 (integers |J| <= 16 are exact, see fp8_code), to E2M3 (J / 4,
+  // six bits; fp6_code) or to E2M1 pairs (|J| <= 4) on the host threads into a pinned staging
+  // buffer, then one copy into the padded operand layout.
   const size_t ab = (size_t)g.Np * g.kbytes;
   if (ab > stg.bytes) {
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("synchronize");
@@ -316,8 +414,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
     if ((e = cudaMallocHost(&stg.pin, ab)) != cudaSuccess) return fail("cudaMallocHost(staging)");
     stg.bytes = ab;
   }
-  const CouplingSums sums =
-      fp4 ? pack_fp4(p->J, g.n, stg.pin, g.Np, g.kbytes) : pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp);
+  const CouplingSums sums = fp4 ? pack_fp4(p->J, g.n, stg.pin, g.Np, g.kbytes)
+                                : (op == kGopE2m3 ? pack_fp6(p->J, g.n, stg.pin, g.Np, g.Kp)
+                                                  : pack_fp8(p->J, g.n, stg.pin, g.Np, g.Kp));
   if (!(g.c0 > 0.0f)) g.c0 = sbh::c0_from_sums(g.n, sums.s, sums.s2);
   if ((e = cudaMemcpyAsync(g.a, stg.pin, ab, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail("upload J");
   std::vector<float> pumps((size_t)(g.steps > 0 ? g.steps : 1), 0.0f);
@@ -331,9 +430,9 @@ sb_status Grouped::prepare(GHost &g, const sb_problem *p, const sb_params *prm, 
   if ((e = cudaMemsetAsync(g.v[1], 0, vb, st)) != cudaSuccess) return fail("memset");
   if ((e = cudaMemsetAsync(g.x, 0, xs, st)) != cudaSuccess) return fail("memset");
   if ((e = cudaMemsetAsync(g.y, 0, xs, st)) != cudaSuccess) return fail("memset");
-  if (!encode_fp8(&g.desc.tmA, g.a, (uint64_t)g.kbytes, (uint64_t)g.Np, kBM) ||
-      !encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
-      !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
+  if (!encode_operand(op, &g.desc.tmA, g.a, g.Kp, g.kbytes, (uint64_t)g.Np, kBM) ||
+      !encode_operand(op, &g.desc.tmB[0], g.v[0], g.Kp, g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
+      !encode_operand(op, &g.desc.tmB[1], g.v[1], g.Kp, g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
     e = cudaErrorInvalidValue;
     return fail("cuTensorMapEncodeTiled");
   }
@@ -374,7 +473,7 @@ void Grouped::attach(GHost &g, int t0) {
 
 sb_status Grouped::add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err) {
   GHost g;
-  sb_status s = prepare(g, p, prm, seed, tag, nr, st, stg_, err, fp4);
+  sb_status s = prepare(g, p, prm, seed, tag, nr, st, stg_, err, op);
   if (s != SB_OK) return s;
   attach(g, t0);
   return SB_OK;
@@ -386,8 +485,10 @@ sb_status Grouped::init_state(GHost &g, uint64_t seed, std::string &err) { retur
 sb_status Grouped::init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err) {
   cudaError_t e = launch_init_uniform(g.x, g.y, g.n, g.R, g.xp, seed, st);
   if (e == cudaSuccess) {
-    if (g.fp4)
+    if (g.op == kGopE2m1)
       g_signs_fp4_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.kbytes);
+    else if (g.op == kGopE2m3)
+      g_signs_fp6_kernel<<<grid1((size_t)(g.n + 15) / 16 * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.kbytes);
     else
       g_signs_kernel<<<grid1((size_t)g.n * g.R), 256, 0, st>>>(g.x, g.n, g.R, g.xp, g.v[0], g.Kp);
     e = cudaGetLastError();
@@ -416,8 +517,8 @@ sb_status Grouped::retile(int new_nr, std::string &err) {
     }
     cudaMemsetAsync(g.v[0], 0, vb, st);
     cudaMemsetAsync(g.v[1], 0, vb, st);
-    if (!encode_fp8(&g.desc.tmB[0], g.v[0], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
-        !encode_fp8(&g.desc.tmB[1], g.v[1], (uint64_t)g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
+    if (!encode_operand(g.op, &g.desc.tmB[0], g.v[0], g.Kp, g.kbytes, (uint64_t)g.Rp, (uint32_t)nr) ||
+        !encode_operand(g.op, &g.desc.tmB[1], g.v[1], g.Kp, g.kbytes, (uint64_t)g.Rp, (uint32_t)nr)) {
       err = "cuTensorMapEncodeTiled";
       return SB_ERR_CUDA;
     }
@@ -453,7 +554,7 @@ sb_status Grouped::sync_tables(std::string &err) {
     descs[i] = insts[i].desc;
     const GHost &g = insts[i];
     for (int m0 = 0; m0 < g.Np; m0 += kBM)
-      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{(int)i, m0, r0, g.kbytes / kChunkBytes});
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{(int)i, m0, r0, grouped_kchunks(g.Kp, g.op)});
   }
   if (order == 0) {
     // longest first, dealt round-robin to the persistent CTAs
@@ -501,7 +602,7 @@ cudaError_t Grouped::launch(int tick, int emode) { return launch_items(d_items, 
 cudaError_t Grouped::launch_items(const GItem *items_ptr, int count, int tick, int emode) {
   const void *k = nullptr;
   size_t smem = 0;
-  if (!grouped_kernel_for(nr, emode, fp4, &k, &smem)) return cudaErrorInvalidValue;
+  if (!grouped_kernel_for(nr, emode, op, &k, &smem)) return cudaErrorInvalidValue;
   static std::mutex mu;
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -538,7 +639,7 @@ cudaError_t Grouped::run_steps(int tick0, int count, bool use_graph) {
     // kernel attributes are set before the capture starts
     const void *k = nullptr;
     size_t smem = 0;
-    grouped_kernel_for(nr, kEmodeStep, fp4, &k, &smem);
+    grouped_kernel_for(nr, kEmodeStep, op, &k, &smem);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -579,7 +680,7 @@ cudaError_t Grouped::energy_pass_for(const std::vector<int> &idx, int tick) {
     cudaError_t e = cudaMemsetAsync(g.energy, 0, (size_t)g.R * sizeof(double), st);
     if (e != cudaSuccess) return e;
     for (int m0 = 0; m0 < g.Np; m0 += kBM)
-      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{i, m0, r0, g.kbytes / kChunkBytes});
+      for (int r0 = 0; r0 < g.Rp; r0 += nr) items.push_back(GItem{i, m0, r0, grouped_kchunks(g.Kp, g.op)});
   }
   if (items.empty()) return cudaSuccess;
   if ((int)items.size() > cap_sub) {
@@ -604,14 +705,14 @@ std::string Grouped::tune_key() const {
   int64_t chunks = 0;
   int rmax = 0;
   for (const auto &g : insts) {
-    chunks += (int64_t)(g.Np / kBM) * (g.kbytes / kChunkBytes);
+    chunks += (int64_t)(g.Np / kBM) * grouped_kchunks(g.Kp, g.op);
     rmax = std::max(rmax, g.R);
   }
   // bucket by total work (log2) and replica count
   int b = 0;
   while ((int64_t(1) << b) < chunks) ++b;
   return std::to_string(rmax) + ":" + std::to_string(b) + ":" + std::to_string(insts.size() > 64 ? 2 : insts.size() > 8 ? 1 : 0) +
-         (fp4 ? ":e2m1" : ":e4m3");
+         (op == kGopE2m1 ? ":e2m1" : (op == kGopE2m3 ? ":e2m3" : ":e4m3"));
 }
 
 std::vector<std::pair<int, int>> Grouped::candidates(int R) {

@@ -24,9 +24,12 @@ namespace sbk {
 
 namespace tck {
 
+// OP (GOperand): FP8 E4M3; packed E2M3 (kind::f8f6f4 with both formats E2M3: J / 4 against signs of
+// +-4, sixteen 6-bit values per 12 bytes in global memory, spread by the tensor map to one 16-byte
+// slot per sixteen values in shared memory, the layout the MMA reads); or
 // FP4: packed E2M1 operands (kind::mxf4, every block scale 1.0 in TMEM columns [2NR, 2NR + 32)),
 // a 128-byte chunk holding 256 spins of K; V written as nibble pairs (spin 2s low, 2s + 1 high).
-template <int NR, int STAGES, int EMODE, bool FP4>
+template <int NR, int STAGES, int EMODE, int OP>
 __global__ void __launch_bounds__(kTcThreads, 1)
     grouped_kernel(const GInst *__restrict__ insts, const GItem *__restrict__ items, int n_items, int tick,
                    uint32_t *status) {
@@ -34,11 +37,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr int kATile = kBM * kChunkBytes;
   constexpr int kBTile = NR * kChunkBytes;
   constexpr int kStage = kATile + kBTile;
-  constexpr uint32_t kTx = (uint32_t)kStage;
   constexpr uint32_t kSf = 2 * NR;
+  constexpr bool FP4 = OP == kGopE2m1, FP6 = OP == kGopE2m3;
+  // bytes a stage's copies count on its barrier: the packed E2M3 boxes count their global bytes,
+  // 12 per 16-byte shared-memory slot
+  constexpr uint32_t kTx = FP6 ? (uint32_t)kStage / 4 * 3 : (uint32_t)kStage;
   constexpr uint32_t kNeed = FP4 ? 2 * NR + 32 : 2 * NR;
   constexpr uint32_t kCols = kNeed <= 32 ? 32 : (kNeed <= 64 ? 64 : (kNeed <= 128 ? 128 : (kNeed <= 256 ? 256 : 512)));
-  constexpr uint32_t kIdesc = FP4 ? make_idesc_mxf4(kBM, NR) : make_idesc(kTcFp8, kBM, NR);
+  // kind::f8f6f4 formats (A bits 7-9, B bits 10-12): E4M3 = 0, E2M3 = 3
+  constexpr uint32_t kIdesc = FP4 ? make_idesc_mxf4(kBM, NR)
+                                  : (make_idesc(kTcFp8, kBM, NR) | (FP6 ? ((3u << 7) | (3u << 10)) : 0u));
   constexpr int kHalf = NR / 2;
   constexpr bool kEOnly = EMODE == kEmodeEnergy;
   static_assert(NR == 32 || NR == 64 || NR == 128, "replica tile");
@@ -223,11 +231,44 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const uint32_t o0 = (uint32_t)(w.r0 + g0) * uxp, v0 = (uint32_t)(w.r0 + g0) * (uint32_t)kb;
 #pragma unroll
           for (int j = 0; j < kGroup; ++j) {
-            if (j < rlim && SB_BOUNDS(row < xp && (FP4 || row < kb) && w.r0 + g0 + j < in->Rp, status)) {
+            if (j < rlim && SB_BOUNDS(row < xp && (FP4 || FP6 || row < kb) && w.r0 + g0 + j < in->Rp, status)) {
               const uint32_t o = o0 + (uint32_t)j * uxp;
               xs[o] = xv[j];
               ys[o] = yv[j];
-              if constexpr (!FP4) vn[row + v0 + (uint32_t)j * (uint32_t)kb] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+              if constexpr (OP == kGopFp8) vn[row + v0 + (uint32_t)j * (uint32_t)kb] = xv[j] > 0.0f ? (uint8_t)0x38 : (uint8_t)0xB8;
+            }
+          }
+          if constexpr (FP6) {
+            // E2M3 signs (+4: 0x18, -4: 0x38, outside the instance 0), sixteen spins per 12 bytes (value i
+            // of a group at bits 6 i .. 6 i + 5, little-endian). The warp ballots each column's valid and
+            // negative spins, then lane l packs column l / 2, group l % 2: four spins at a time, bit b of a
+            // mask goes to bit 6 b (spread4), times 0x18 for the valid bits 3 and 4, shifted by 5 for the
+            // sign bit; the three 32-bit words of the group are cut from those 24-bit pieces.
+            uint32_t myv = 0, mys = 0;
+#pragma unroll
+            for (int j = 0; j < kGroup; ++j) {
+              const bool ins = row < n && w.r0 + g0 + j < R;
+              const uint32_t vm = __ballot_sync(0xffffffffu, ins);
+              const uint32_t sm = __ballot_sync(0xffffffffu, ins && !(xv[j] > 0.0f));
+              if ((lane >> 1) == j) {
+                myv = vm;
+                mys = sm;
+              }
+            }
+            const int grp = lane & 1;
+            const int r = w.r0 + g0 + (lane >> 1);
+            const uint32_t v16 = (myv >> (16 * grp)) & 0xFFFFu, s16 = (mys >> (16 * grp)) & 0xFFFFu;
+            auto spread4 = [](uint32_t b) { return (b & 1u) | ((b & 2u) << 5) | ((b & 4u) << 10) | ((b & 8u) << 15); };
+            uint32_t piece[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              piece[k] = spread4((v16 >> (4 * k)) & 0xFu) * 0x18u | (spread4((s16 >> (4 * k)) & 0xFu) << 5);
+            const uint32_t gbyte = (uint32_t)((w.m0 + 32 * q) / 16 + grp) * 12u;
+            if (r < R && SB_BOUNDS(r < in->Rp && gbyte + 12u <= (uint32_t)kb, status)) {
+              uint32_t *dst = reinterpret_cast<uint32_t *>(vn + (size_t)r * (uint32_t)kb + gbyte);
+              dst[0] = piece[0] | (piece[1] << 24);
+              dst[1] = (piece[1] >> 8) | (piece[2] << 16);
+              dst[2] = (piece[2] >> 16) | (piece[3] << 8);
             }
           }
           if constexpr (FP4) {

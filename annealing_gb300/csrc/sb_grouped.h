@@ -12,11 +12,15 @@
 
 namespace sbk {
 
+// Operand types of the grouped kernel: FP8 E4M3 (integer |J| <= 16), packed E2M1 (|J| <= 4), or
+// packed E2M3, six bits per value (|J| <= 16 held as J / 4 against signs of +-4, exact products).
+enum GOperand : int { kGopFp8 = 0, kGopE2m1 = 1, kGopE2m3 = 2 };
+
 // Per-instance descriptor read by the grouped kernel (device memory, 64-byte aligned for the
 // tensor maps).
 struct alignas(64) GInst {
-  CUtensorMap tmA;       // J operand FP8 [Np][Kp], 128 x 128-byte boxes, 128B swizzle
-  CUtensorMap tmB[2];    // V operand FP8 [Rp][Kp] buffers, 128-byte x NR boxes
+  CUtensorMap tmA;       // J operand [Np][Kp], 128 x 128-byte shared-memory boxes, 128B swizzle
+  CUtensorMap tmB[2];    // V operand [Rp][Kp] buffers, 128-byte x NR boxes
   uint8_t *v[2];         // the V buffers
   float *x, *y;          // state [R][xp]
   const float *h;        // fields or null
@@ -25,7 +29,7 @@ struct alignas(64) GInst {
   int n, Kp, R, Rp, xp;
   int t0;                // the instance's step t = tick - t0
   float c0, dt, dta0;
-  int kbytes;            // bytes of one operand row: Kp (FP8) or Kp / 2 (packed E2M1)
+  int kbytes;            // bytes of one operand row in global memory: Kp (FP8), Kp / 2 (E2M1), 3 Kp / 4 (E2M3)
 };
 
 // One work item: a 128-spin x NR-replica tile of one instance.
@@ -38,14 +42,16 @@ bool grouped_supports(const sb_problem *p, const sb_params *prm);
 // ... and integer |J| <= 4: exact as packed E2M1 operands (half the bytes of FP8)
 bool grouped_fp4_exact(const sb_problem *p);
 // device bytes one instance holds while resident
-int64_t grouped_instance_bytes(int n, int R, int steps, int nr, bool fp4 = false);
+int64_t grouped_instance_bytes(int n, int R, int steps, int nr, int op = kGopFp8);
+// K chunks (128 bytes of shared memory each) of an instance's operand rows
+inline int grouped_kchunks(int Kp, int op) { return op == kGopE2m1 ? Kp / 256 : Kp / 128; }
 
 struct GHost {
   int tag = 0;                  // caller's index / ticket
   const sb_problem *prob = nullptr;
   int n = 0, R = 0, steps = 0, t0 = 0, Np = 0, Kp = 0, Rp = 0, xp = 0;
-  int kbytes = 0;  // operand row bytes (Kp, or Kp / 2 for packed E2M1)
-  bool fp4 = false;
+  int kbytes = 0;  // operand row bytes in global memory (Kp, Kp / 2 for E2M1, 3 Kp / 4 for E2M3)
+  int op = kGopFp8;
   float c0 = 0, dt = 0, dta0 = 0;
   uint64_t seed = 0;
   uint8_t *a = nullptr, *v[2] = {nullptr, nullptr};
@@ -65,16 +71,17 @@ struct Staging {
 
 class Grouped {
  public:
-  // fp4: every instance's couplings are integers |J| <= 4, held as packed E2M1 (else FP8 E4M3)
-  explicit Grouped(cudaStream_t s, int replica_tile, int item_order, bool fp4_operands = false)
-      : st(s), nr(replica_tile), order(item_order), fp4(fp4_operands) {}
+  // operand: the type every instance's couplings are held in (GOperand)
+  explicit Grouped(cudaStream_t s, int replica_tile, int item_order, int operand = kGopFp8)
+      : st(s), nr(replica_tile), order(item_order), op(operand) {}
   ~Grouped();
-  // Uploads p (host), converts J to FP8, seeds the state. t0: the tick at which its step 0 runs.
+  // Uploads p (host) with J packed to the operand type, seeds the state. t0: the tick at which its
+  // step 0 runs.
   sb_status add(const sb_problem *p, const sb_params *prm, uint64_t seed, int t0, int tag, std::string &err);
   // The two halves of add: prepare builds a complete instance on stream `st` (any thread; memory
   // from the stream-ordered pool), attach makes it resident from tick t0 (the engine's thread).
   static sb_status prepare(GHost &g, const sb_problem *p, const sb_params *prm, uint64_t seed, int tag, int nr,
-                           cudaStream_t st, Staging &stg, std::string &err, bool fp4 = false);
+                           cudaStream_t st, Staging &stg, std::string &err, int op = kGopFp8);
   void attach(GHost &g, int t0);
   static void release(GHost &g, cudaStream_t s);
   static sb_status init_state_on(GHost &g, uint64_t seed, cudaStream_t st, std::string &err);
@@ -108,7 +115,7 @@ class Grouped {
 
   cudaStream_t st;
   int nr, order;
-  bool fp4;
+  int op;
   std::vector<GHost> insts;
   int64_t launches = 0;
   int n_items = 0;

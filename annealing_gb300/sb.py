@@ -23,8 +23,8 @@ SB_OK, SB_ERR_PENDING = 0, 12
 ASB, BSB, DSB = 0, 1, 2
 FIELD_AUTO, FIELD_FP32, FIELD_TC = 0, 1, 2
 INIT_UNIFORM, INIT_REFERENCE = 0, 1
-DTYPE_NAMES = {0: "f32", 1: "fp8e4m3", 2: "bf16", 3: "bf16x2", 4: "fp4e2m1", 5: "fp16x2"}
-OPERAND_AUTO, OPERAND_FP8, OPERAND_BF16, OPERAND_BF16X2, OPERAND_FP4, OPERAND_FP16X2 = 0, 1, 2, 3, 4, 5
+DTYPE_NAMES = {0: "f32", 1: "fp8e4m3", 2: "bf16", 3: "bf16x2", 4: "fp4e2m1", 5: "fp16x2", 6: "fp6e2m3"}
+OPERAND_AUTO, OPERAND_FP8, OPERAND_BF16, OPERAND_BF16X2, OPERAND_FP4, OPERAND_FP16X2, OPERAND_FP6 = 0, 1, 2, 3, 4, 5, 6
 VARIANTS = {"asb": ASB, "bsb": BSB, "dsb": DSB}
 
 

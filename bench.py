@@ -174,6 +174,19 @@ def weak_scaling_value(units_per_rank: float, world: int, steps: int, max_total_
     return world * units_per_rank * steps / (max_total_ms * 1e-3)
 
 
+# bytes of one grouped operand row (couplings as stored on the device) and of one sign per spin and
+# replica, by operand type: FP8 E4M3 [Np][Np]; packed E2M3, 3/4 byte per value [Np][3 Np / 4];
+# packed E2M1 pairs [Np][Kp / 2] with Kp = N rounded up to 256
+SIGN_BYTES = {"fp8e4m3": 1.0, "fp6e2m3": 0.75, "fp4e2m1": 0.5}
+
+
+def operand_row_bytes(n, dtype):
+    np_ = (n + 127) // 128 * 128
+    if dtype == "fp4e2m1":
+        return (n + 255) // 256 * 128
+    return np_ * 3 // 4 if dtype == "fp6e2m3" else np_
+
+
 def make_problem(name):
     from annealing_gb300 import instances
 
@@ -321,8 +334,8 @@ def run_ours(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     ctx = sb.Context(local_rank, stream=stream.cuda_stream)
     prob = sb.Problem.from_dense(J, h)
-    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16,
-           "bf16x2": sb.OPERAND_BF16X2, "fp16x2": sb.OPERAND_FP16X2}[args.operand]
+    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp6": sb.OPERAND_FP6, "fp8": sb.OPERAND_FP8,
+           "bf16": sb.OPERAND_BF16, "bf16x2": sb.OPERAND_BF16X2, "fp16x2": sb.OPERAND_FP16X2}[args.operand]
     prm = sb.Params.default(vcode, steps=sb_steps, replicas=R, field_mode=fmode, seed=1234 + rank, operand_dtype=odt)
     plan = ctx.plan(prob, prm)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -518,7 +531,8 @@ def run_batch(args, rank, world, local_rank):
     n_sum = sum(p.n for p in probs)
     stream = torch.cuda.current_stream(dev)
     ctx = sb.Context(local_rank, stream=stream.cuda_stream)
-    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "bf16": sb.OPERAND_BF16}[args.operand]
+    odt = {"auto": sb.OPERAND_AUTO, "fp4": sb.OPERAND_FP4, "fp8": sb.OPERAND_FP8, "fp6": sb.OPERAND_FP6,
+           "bf16": sb.OPERAND_BF16}[args.operand]
     prm = sb.Params.default(sb.DSB, steps=sb_steps, replicas=R, seed=1234 + 1000 * rank, field_mode=sb.FIELD_TC,
                             operand_dtype=odt)
     t0 = time.perf_counter()
@@ -559,13 +573,11 @@ def run_batch(args, rank, world, local_rank):
     rp = bp.run(seed=8)
     bp.close()
     hbm, bf16, src = peaks()
-    fp4s = [r.field_dtype == "fp4e2m1" for r in rp]  # each instance's operand bucket
-    fp4 = all(fp4s)
-    # couplings as stored on the device: FP8 [Np][Np], or E2M1 pairs [Np][Kp / 2] with Kp = N rounded to 256
-    np_kp = sum(((p.n + 127) // 128 * 128) * (((p.n + 255) // 256 * 128) if f4 else ((p.n + 127) // 128 * 128))
-                for p, f4 in zip(probs, fp4s))
-    # J + per spin-replica: x, y read and written (16 B) and the next sign operand (1 B, or 1/2)
-    bytes_per_launch = np_kp + sum(p.n * R * (16.5 if f4 else 17.0) for p, f4 in zip(probs, fp4s))
+    dts = [r.field_dtype for r in rp]  # each instance's operand bucket
+    fp4 = all(d == "fp4e2m1" for d in dts)
+    np_kp = sum(operand_row_bytes(p.n, d) * ((p.n + 127) // 128 * 128) for p, d in zip(probs, dts))
+    # J + per spin-replica: x, y read and written (16 B) and the next sign operand (1 B, 3/4 or 1/2)
+    bytes_per_launch = np_kp + sum(p.n * R * (16.0 + SIGN_BYTES[d]) for p, d in zip(probs, dts))
     achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
     tkey = "uneven-batch-e2m1" if fp4 else "uneven-batch"
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -606,10 +618,11 @@ def run_batch(args, rank, world, local_rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": ("e2m1 x e2m1 field (f32 accumulate, exact for |J| <= 4), f32 state" if fp4
-                  else "fp8e4m3 field (f32 accumulate), f32 state"), "data": "synthetic (seeded)",
+                  else "/".join(sorted(set(dts))) + " field (f32 accumulate, exact), f32 state"),
+        "data": "synthetic (seeded)",
         "config": {"workload": desc, "instances": len(probs), "sum_n": n_sum, "replicas": R,
                    "sb_steps": sb_steps, "parallelism": f"replicas-only x{world}",
-                   "l2": f"inputs ({np_kp / 1e9:.2f} GB of {'E2M1' if fp4 else 'FP8'} J) "
+                   "l2": f"inputs ({np_kp / 1e9:.2f} GB of {'/'.join(sorted(set(dts)))} J) "
                    + ("larger than L2" if np_kp > 129e6 else "smaller than L2") + "; 256 MB flush between runs"},
         "e2e": {"value": world * updates * args.steps / (e2e_total * 1e-3), "unit": "spin-updates/s",
                 "h2d_bytes_per_step": int(np_kp),  # couplings packed on the host, then copied
@@ -679,7 +692,12 @@ def serve_stream(sb, ctx, count, rate, pool_size, R, seed, device, warmup=2):
     updates = float(sum(p.n * R * prm.steps for _, p, prm in reqs))
     stats = ctx.serving_stats()
     busy_ms = stats["busy_ms"] - stats0["busy_ms"]
-    algo_bytes = float(sum((((p.n + 127) // 128 * 128) ** 2 + 17.0 * p.n * R) * prm.steps for _, p, prm in reqs))
+    # per request and step: its couplings as stored (the grouped path's operand type), x and y read
+    # and written, the next sign operand
+    algo_bytes = 0.0
+    for (_, p, prm), r in zip(reqs, results):
+        d = r.field_dtype if r.field_dtype in SIGN_BYTES else "fp8e4m3"
+        algo_bytes += (operand_row_bytes(p.n, d) * ((p.n + 127) // 128 * 128) + (16.0 + SIGN_BYTES[d]) * p.n * R) * prm.steps
     hbm, _, src = peaks()
     span = reqs[-1][0]
     # a queue that keeps up finishes the last request about one latency after its arrival; a
@@ -721,7 +739,7 @@ def run_serving(args, rank, world, local_rank):
         "metric": "SB spin-updates/s (serving stream)", "value": updates / makespan,
         "unit": "spin-updates/s", "n_gpus": world, "steps": len(reqs), "warmup": args.warmup,
         "ms_per_step": 1e3 * makespan / len(reqs), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp8e4m3 field (f32 accumulate), f32 state",
+        "vs_baseline": None, "dtype": "fp6e2m3 field (J / 4 in six bits, f32 accumulate, exact), f32 state",
         "data": "synthetic (seeded Poisson stream; sizes from a pool of distinct instances)",
         "config": {"workload": desc, "requests": len(reqs), "rate_per_s": args.rate,
                    "pool_instances": out["pool_instances"], "replicas": R},
@@ -1040,7 +1058,7 @@ def main():
     ap.add_argument("--pool", type=int, default=64, help="serving workload: distinct instances")
     ap.add_argument("--sb-steps", type=int, default=0,
                     help="smaller case for profiling: SB steps per solve (default: the workload's)")
-    ap.add_argument("--operand", choices=["auto", "fp4", "fp8", "bf16", "bf16x2", "fp16x2"], default="auto",
+    ap.add_argument("--operand", choices=["auto", "fp4", "fp6", "fp8", "bf16", "bf16x2", "fp16x2"], default="auto",
                     help="tensor-core operand type of the single-instance workloads (default: narrowest exact)")
     ap.add_argument("--instances", type=int, default=512,
                     help="uneven-batch workload: instance count (smaller cases for profiling)")

@@ -96,7 +96,9 @@ typedef enum sb_operand_dtype {
   SB_OPERAND_BF16 = 2,   /* integer |J| <= 256 */
   SB_OPERAND_BF16X2 = 3, /* BF16 hi + lo, real J */
   SB_OPERAND_FP4 = 4,    /* packed E2M1, integer |J| <= 4, single-instance dSB */
-  SB_OPERAND_FP16X2 = 5  /* FP16 hi + lo, real J scaled by powers of two: 22 bits per operand (opt-in) */
+  SB_OPERAND_FP16X2 = 5, /* FP16 hi + lo, real J scaled by powers of two: 22 bits per operand (opt-in) */
+  SB_OPERAND_FP6 = 6     /* packed E2M3 (6 bits), integer |J| <= 16 held as J/4 against signs of +-4:
+                            the grouped path (batches, serving); the same products as FP8 */
 } sb_operand_dtype;
 
 /* Initial x, y.

@@ -1,6 +1,7 @@
 """Grouped tensor-core batches (sb_batch_*): every instance bit-exact against the CPU oracle.
 
-Batches whose couplings are all integers |J| <= 4 run packed E2M1 operands; others FP8 E4M3.
+Instances whose couplings are integers |J| <= 4 run packed E2M1 operands, others packed E2M3 (J / 4
+in six bits against signs of +-4); FP8 E4M3 on request. All three give the same integer fields.
 """
 import numpy as np
 import pytest
@@ -21,15 +22,19 @@ def make_instances(ns, jmax=4, with_h=(2,)):
     return out
 
 
-@pytest.mark.parametrize("R,jmax,dtype", [(64, 4, "fp4e2m1"), (32, 4, "fp4e2m1"), (100, 4, "fp4e2m1"),
-                                          (64, 4, "fp8e4m3"), (100, 16, "fp8e4m3"), (32, 1, "fp4e2m1")])
-def test_batch_matches_oracle(ctx, R, jmax, dtype):
-    # odd sizes: a last E2M1 byte with one spin, padded K chunks, partial spin and replica tiles
+@pytest.mark.parametrize("R,jmax,odt,dtype", [
+    (64, 4, sb.OPERAND_AUTO, "fp4e2m1"), (32, 4, sb.OPERAND_AUTO, "fp4e2m1"), (100, 4, sb.OPERAND_AUTO, "fp4e2m1"),
+    (32, 1, sb.OPERAND_AUTO, "fp4e2m1"),
+    (64, 16, sb.OPERAND_AUTO, "fp6e2m3"), (100, 16, sb.OPERAND_AUTO, "fp6e2m3"), (32, 9, sb.OPERAND_AUTO, "fp6e2m3"),
+    (128, 16, sb.OPERAND_AUTO, "fp6e2m3"), (64, 4, sb.OPERAND_FP6, "fp6e2m3"),
+    (64, 4, sb.OPERAND_FP8, "fp8e4m3"), (100, 16, sb.OPERAND_FP8, "fp8e4m3")])
+def test_batch_matches_oracle(ctx, R, jmax, odt, dtype):
+    # odd sizes: a last E2M1 byte with one spin, a last E2M3 group of sixteen with a few spins,
+    # padded K chunks, partial spin and replica tiles
     ns = [64, 100, 129, 301, 513, 1000]
     insts = make_instances(ns, jmax=jmax)
     probs = [sb.Problem.from_dense(J, h) for J, h in insts]
     steps, seed = 30, 100
-    odt = sb.OPERAND_FP8 if (dtype == "fp8e4m3" and jmax <= 4) else sb.OPERAND_AUTO
     prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC, operand_dtype=odt)
     batch = ctx.batch(probs, prm, want_state=True)
     res = batch.run()
@@ -64,7 +69,7 @@ def test_batch_profile_reports_step_kernel_time(ctx):
 
 def test_batch_mixed_operands_per_instance(ctx):
     """A batch mixing couplings |J| <= 4 and |J| <= 9 runs two operand buckets: the first instances on
-    packed E2M1, the others on FP8, each bit-exact against the oracle, in one run."""
+    packed E2M1, the others on packed E2M3, each bit-exact against the oracle, in one run."""
     ns = [64, 129, 300, 513, 700, 1000]
     insts = []
     for k, n in enumerate(ns):
@@ -79,7 +84,7 @@ def test_batch_mixed_operands_per_instance(ctx):
     prm = sb.Params.default(sb.DSB, steps=steps, replicas=R, seed=seed, field_mode=sb.FIELD_TC)
     batch = ctx.batch(probs, prm, want_state=True)
     res = batch.run()
-    assert [r.field_dtype for r in res] == ["fp4e2m1", "fp8e4m3"] * 3
+    assert [r.field_dtype for r in res] == ["fp4e2m1", "fp6e2m3"] * 3
     for k, ((J, h), p, r) in enumerate(zip(insts, probs, res)):
         x, y = orc.init_uniform(J.shape[0], R, seed + k)
         orc.sb_run_f32(2, J, h, x, y, steps, 1.0, p.default_c0(), 1.25)
