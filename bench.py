@@ -88,6 +88,8 @@ NCU_TRAFFIC = {
     "uneven-batch": (441.2 / 451.8, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
     # the same with E2M1 couplings (255.2 MB of 284.0 MB)
     "uneven-batch-e2m1": (255.2 / 284.0, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
+    # the same with packed E2M3 couplings (349.6 MB of 366.7 MB)
+    "uneven-batch-e2m3": (349.6 / 366.75, "profiles/grouped_kernel_uneven_batch_48_instances.md"),
 }
 
 
@@ -579,10 +581,12 @@ def run_batch(args, rank, world, local_rank):
     # J + per spin-replica: x, y read and written (16 B) and the next sign operand (1 B, 3/4 or 1/2)
     bytes_per_launch = np_kp + sum(p.n * R * (16.0 + SIGN_BYTES[d]) for p, d in zip(probs, dts))
     achieved = bytes_per_launch / (rp[0].kernel_ms_avg * 1e-3) / 1e9
-    tkey = "uneven-batch-e2m1" if fp4 else "uneven-batch"
+    tkey = {"fp4e2m1": "uneven-batch-e2m1", "fp6e2m3": "uneven-batch-e2m3"}.get(dts[0], "uneven-batch") \
+        if len(set(dts)) == 1 else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": NCU_TRAFFIC[tkey][0] * bytes_per_launch,
-            "traffic_source": NCU_TRAFFIC[tkey][1] + " (48-instance capture, scaled by algorithmic bytes)",
+            "traffic": NCU_TRAFFIC[tkey][0] * bytes_per_launch if tkey else None,
+            "traffic_source": (NCU_TRAFFIC[tkey][1] + " (48-instance capture, scaled by algorithmic bytes)")
+            if tkey else None,
             "kernel": "grouped_kernel (one launch per SB step)",
             "launch_ms": rp[0].kernel_ms_avg, "bytes_per_launch": bytes_per_launch,
             "peak_source": f"{src} HBM copy",
