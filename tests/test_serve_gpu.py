@@ -10,14 +10,14 @@ pytestmark = pytest.mark.gpu
 
 
 def test_requests_match_solo_solves():
-    """Requests of uneven size (one of them, N = 12000, has FP8 couplings of 144 MB, more than the
-    L2 cache holds) and a bSB request outside the grouped engine, submitted together: each result
-    equals the same request solved alone."""
+    """Requests of uneven size (one of them, N = 13500, has packed E2M3 couplings of 138 MB, more
+    than the L2 cache holds) and a bSB request outside the grouped engine, submitted together: each
+    result equals the same request solved alone (there on the single-instance FP8 path)."""
     ctx = sb.Context(0)
     rng = np.random.default_rng(0)
     reqs = []
     for k, (n, steps) in enumerate([(100, 200), (700, 60), (1300, 150), (257, 120), (2000, 90), (64, 30),
-                                    (12000, 60)]):
+                                    (13500, 60)]):
         p = sb.Problem.random(n, float(rng.uniform(0.05, 1.0)), 8, 2 if k == 3 else 0, seed=300 + k)
         prm = sb.Params.default(sb.DSB, steps=steps, replicas=32, seed=900 + k, field_mode=sb.FIELD_TC)
         reqs.append((p, prm))
