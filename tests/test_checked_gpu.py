@@ -59,6 +59,12 @@ b = ctx.batch(probs, sb.Params.default(sb.DSB, steps=8, replicas=32, seed=1))
 for r in b.run(seed=1):
     assert r.energy_check_ok
 b.close()
+# the same with couplings up to 9: packed E2M3 operands
+probs = [sb.Problem.from_dense(instances.erdos_renyi(n, 0.4, seed=n, jmax=9, allow_zero=True)) for n in (64, 129, 300)]
+b = ctx.batch(probs, sb.Params.default(sb.DSB, steps=8, replicas=64, seed=1))
+for r in b.run(seed=1):
+    assert r.energy_check_ok and r.field_dtype == "fp6e2m3"
+b.close()
 # SQA (hash mode)
 J = instances.erdos_renyi(96, 0.5, seed=6, jmax=3)
 s, _ = orc.sqa_init(96, 8, 2, 1, 3)

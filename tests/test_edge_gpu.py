@@ -13,7 +13,7 @@ from oracle import binding as orc
 
 pytestmark = pytest.mark.gpu
 
-OPERAND = {"fp4e2m1": sb.OPERAND_FP4, "fp8e4m3": sb.OPERAND_FP8}
+OPERAND = {"fp4e2m1": sb.OPERAND_FP4, "fp8e4m3": sb.OPERAND_FP8, "fp6e2m3": sb.OPERAND_FP6}
 
 
 def oracle(J, h, R, steps, seed, c0):
@@ -95,7 +95,7 @@ def test_past_the_resident_shape_falls_back_to_fp8(ctx):
     assert e.value.status == 6
 
 
-@pytest.mark.parametrize("dtype", ["fp4e2m1", "fp8e4m3"])
+@pytest.mark.parametrize("dtype", ["fp4e2m1", "fp8e4m3", "fp6e2m3"])
 def test_batch_with_tiny_and_empty_instances(ctx, dtype):
     ns, kinds = [1, 2, 5, 300, 255, 64], ["er", "er", "zero", "er", "zero", "er"]
     Js = [couplings(n, k, seed=i) for i, (n, k) in enumerate(zip(ns, kinds))]
