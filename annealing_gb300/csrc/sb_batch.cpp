@@ -126,7 +126,7 @@ sb_status create(sb_ctx *ctx, const sb_problem *problems, int32_t count, const s
     }
     if (!sbk::grouped_supports(&problems[k], prm)) {
       err = "problem " + std::to_string(k) +
-            ": the grouped path runs dSB with integer couplings |J| <= 16 (exact FP8 operands)";
+            ": the grouped path runs dSB with integer couplings |J| <= 16 (exact E2M1 / E2M3 / FP8 operands)";
       return SB_ERR_UNSUPPORTED;
     }
   }

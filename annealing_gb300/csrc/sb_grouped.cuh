@@ -1,4 +1,5 @@
-// Grouped tcgen05 SB step over many instances of uneven size (dSB, FP8 E4M3 operands).
+// Grouped tcgen05 SB step over many instances of uneven size (dSB; packed E2M1, packed E2M3 or
+// FP8 E4M3 operands).
 //
 // The batched workloads of the benchmark spec (hundreds of instances with N from 64 to 16384, each
 // with its own replicas, and the serving stream) do not fit the one-unit-per-SM residency of
@@ -8,7 +9,8 @@
 //     per SM) walk a cost-sorted item list round-robin;
 //   * warp 0 (lane 0) streams each item's J tile and V tile with 2-D TMA through the shared-memory
 //     ring, using the instance's tensor maps, which live in device memory next to its descriptor;
-//   * warp 1 (lane 0) issues tcgen05.mma (kind::f8f6f4) into one of two TMEM accumulators, so the
+//   * warp 1 (lane 0) issues tcgen05.mma (kind::f8f6f4, or kind::mxf4 for E2M1) into one of two
+//     TMEM accumulators, so the
 //     epilogue of item k overlaps the contraction of item k + 1;
 //   * 8 epilogue warps read the accumulator, load x and y from global memory (coalesced), apply
 //     the dSB update in the oracle's operation order, store x and y and the next operand.

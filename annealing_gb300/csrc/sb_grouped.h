@@ -37,7 +37,7 @@ struct GItem {
   int inst, m0, r0, kchunks;
 };
 
-// dSB with integer |J| <= 16 (exact FP8 operands) and n * 16 < 2^24 (exact FP32 accumulation).
+// dSB with integer |J| <= 16 (exact E2M3 and FP8 operands) and n * 16 < 2^24 (exact FP32 accumulation).
 bool grouped_supports(const sb_problem *p, const sb_params *prm);
 // ... and integer |J| <= 4: exact as packed E2M1 operands (half the bytes of FP8)
 bool grouped_fp4_exact(const sb_problem *p);

@@ -81,8 +81,9 @@ typedef enum sb_variant { SB_ASB = 0, SB_BSB = 1, SB_DSB = 2 } sb_variant;
  *  SB_FIELD_FP32: the plain fused FP32 kernel, one launch per step (the drop-in form).
  *  SB_FIELD_TC:   tcgen05 tensor cores. dSB with integer |J| <= 4 and n <= ~2300: packed E2M1
  *                 operands with J resident in shared memory, FP32 accumulation (bit-exact).
- *                 dSB with integer |J| <= 16: FP8 E4M3 operands, FP32
- *                 accumulation (bit-exact). dSB with integer |J| <= 256: BF16 operands (bit-exact).
+ *                 dSB with integer |J| <= 16: FP8 E4M3 operands (grouped batches and serving:
+ *                 packed E2M3, J / 4 in six bits), FP32 accumulation (bit-exact).
+ *                 dSB with integer |J| <= 256: BF16 operands (bit-exact).
  *                 dSB with real J: BF16 hi+lo split of J. bSB: BF16 hi+lo split of J and of x
  *                 (three products), FP32 accumulation. aSB is not offered on tensor cores. */
 typedef enum sb_field_mode { SB_FIELD_AUTO = 0, SB_FIELD_FP32 = 1, SB_FIELD_TC = 2 } sb_field_mode;
