@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <functional>
 #include <memory>
 #include <string>
 #include <thread>
@@ -12,6 +13,13 @@
 #include "sb.h"
 
 namespace sbh {
+// Runs fn(0) .. fn(nt - 1) on the calling thread and on a process-wide pool of host worker threads
+// (created on first use, kept until exit, so a short parallel loop pays no thread start-up), and
+// returns when all have finished. Safe to call from several threads at once; a caller waiting for
+// its own tasks runs queued ones meanwhile.
+void parallel_run(int nt, const std::function<void(int)> &fn);
+// Host threads worth using for an n x n pass (1 below n = 1024), at most the pool's size.
+int host_threads(int n);
 void problem_scan(sb_problem *p);
 sb_status load_graph(const char *path, const sb_graph_opts *opts, sb_problem *out,
                      std::string &err);

@@ -6,6 +6,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -76,10 +80,7 @@ float sb_default_c0(const sb_problem *p) { return sbh::default_c0(p, 0); }
 }  // extern "C"
 
 namespace {
-int auto_threads(int n, int threads) {
-  if (threads > 0) return threads;
-  return n >= 1024 ? (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency())) : 1;
-}
+int auto_threads(int n, int threads) { return threads > 0 ? threads : sbh::host_threads(n); }
 }  // namespace
 
 float sbh::default_c0(const sb_problem *p, int threads) {
@@ -130,14 +131,7 @@ double sbh::coupling_std(const sb_problem *p, int threads) {
       ps[t] = a;
       ps2[t] = a2;
     };
-    if (nt == 1) {
-      rows(0);
-    } else {
-      std::vector<std::thread> th;
-      for (int t = 1; t < nt; ++t) th.emplace_back(rows, t);
-      rows(0);
-      for (auto &x : th) x.join();
-    }
+    sbh::parallel_run(nt, rows);
     int64_t a = 0, a2 = 0;
     for (int t = 0; t < nt; ++t) {
       a += ps[t];
@@ -211,14 +205,7 @@ sb_status sbh::energy_i64(const sb_problem *p, const int8_t *spins, int64_t *out
   const int nt = auto_threads(n, threads);
   std::vector<int64_t> part((size_t)nt, 0);
   std::vector<char> ok((size_t)nt, 1);
-  if (nt == 1) {
-    ok[0] = rows(0, 1, part[0]);
-  } else {
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; ++t) th.emplace_back([&, t] { ok[t] = rows(t, nt, part[t]); });
-    ok[0] = rows(0, nt, part[0]);
-    for (auto &x : th) x.join();
-  }
+  sbh::parallel_run(nt, [&](int t) { ok[t] = rows(t, nt, part[t]); });
   int64_t e = 0;
   for (int t = 0; t < nt; ++t) {
     if (!ok[t]) return SB_ERR_UNSUPPORTED;
@@ -346,10 +333,7 @@ int64_t sbh::CouplingCopy::energy(const int8_t *spins, int threads) const {
   const int nt = threads > 0 ? threads : (mode == kInt8 && n >= 4096 ? auto_threads(n, 0) : 1);
   if (nt <= 1) return rows(0, 1);
   std::vector<int64_t> part((size_t)nt, 0);
-  std::vector<std::thread> th;
-  for (int t = 1; t < nt; ++t) th.emplace_back([&, t] { part[(size_t)t] = rows(t, nt); });
-  part[0] = rows(0, nt);
-  for (auto &x : th) x.join();
+  sbh::parallel_run(nt, [&](int t) { part[(size_t)t] = rows(t, nt); });
   int64_t e = 0;
   for (int64_t v : part) e += v;
   return e;
@@ -436,9 +420,90 @@ std::string sbh::device_status_text(uint32_t status) {
 
 // Integrality, max |J| and the edge count of the couplings: branch-free row loops (vectorised), rows
 // dealt round-robin to host threads for large n; none of the three depends on the order.
+namespace {
+// The process-wide worker pool behind sbh::parallel_run: a queue of (loop, index) tasks.
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool *pool = new HostPool();  // never destroyed: its threads outlive static teardown
+    return *pool;
+  }
+  int size() const { return (int)workers_.size() + 1; }
+  void run(int nt, const std::function<void(int)> &fn) {
+    if (nt <= 1 || workers_.empty()) {
+      for (int t = 0; t < nt; ++t) fn(t);
+      return;
+    }
+    Loop loop{&fn, nt - 1};
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      for (int t = 1; t < nt; ++t) queue_.push_back(Task{&loop, t});
+    }
+    cv_.notify_all();
+    fn(0);
+    // help with queued tasks (this loop's or another caller's) until this loop's are all done
+    for (;;) {
+      Task task{nullptr, 0};
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        if (loop.left == 0) return;
+        if (queue_.empty()) {
+          done_cv_.wait(lk, [&] { return loop.left == 0 || !queue_.empty(); });
+          if (loop.left == 0) return;
+          continue;
+        }
+        task = queue_.front();
+        queue_.pop_front();
+      }
+      execute(task);
+    }
+  }
+
+ private:
+  struct Loop {
+    const std::function<void(int)> *fn;
+    int left;  // tasks not yet finished (guarded by mu_)
+  };
+  struct Task {
+    Loop *loop;
+    int t;
+  };
+  HostPool() {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned n = std::min(hw, 16u) - 1;
+    for (unsigned i = 0; i < n; ++i) workers_.emplace_back([this] { work(); });
+  }
+  void execute(const Task &task) {
+    (*task.loop->fn)(task.t);
+    std::lock_guard<std::mutex> lk(mu_);
+    if (--task.loop->left == 0) done_cv_.notify_all();
+  }
+  void work() {
+    for (;;) {
+      Task task{nullptr, 0};
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !queue_.empty(); });
+        task = queue_.front();
+        queue_.pop_front();
+      }
+      execute(task);
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  std::deque<Task> queue_;
+  std::vector<std::thread> workers_;
+};
+}  // namespace
+
+void sbh::parallel_run(int nt, const std::function<void(int)> &fn) { HostPool::get().run(nt, fn); }
+
+int sbh::host_threads(int n) { return n >= 1024 ? HostPool::get().size() : 1; }
+
 void sbh::problem_scan(sb_problem *p) {
   const int n = p->n;
-  const int nt = auto_threads(n, 0);
+  const int nt = host_threads(n);
   std::vector<int> nonint((size_t)nt, 0);
   std::vector<float> mx((size_t)nt, 0.0f);
   std::vector<int64_t> ed((size_t)nt, 0);
@@ -450,25 +515,39 @@ void sbh::problem_scan(sb_problem *p) {
     int64_t a1 = 0, a2 = 0;
     for (int i = t; i < n; i += nt) {
       const float *Ji = p->J + (size_t)i * n;
-      // integrality and the largest |J| of the row, in a form the compiler vectorises: |w| < 2^23
-      // is an integer exactly when adding and subtracting 2^23 gives it back, larger floats all
-      // are, NaN is not; the maximum runs on the bit patterns of |w| (monotonic for non-negative
-      // floats; NaN counts as 0)
+      // one pass over the row for integrality, the largest |J| and the nonzero couplings right of
+      // the diagonal, in a form the compiler vectorises: |w| < 2^23 is an integer exactly when
+      // adding and subtracting 2^23 gives it back, larger floats all are, NaN is not; the maximum
+      // runs on the bit patterns of |w| (monotonic for non-negative floats; NaN counts as 0)
       uint32_t rb = 0, rm = 0;
+      int32_t re = 0;
       for (int j = 0; j < n; ++j) {
-        const float a = fabsf(Ji[j]);
+        const float w = Ji[j];
+        const float a = fabsf(w);
         const float r = (a + 8388608.0f) - 8388608.0f;
         rb |= (uint32_t)((r != a) & (a < 8388608.0f)) | (uint32_t)(a != a);
         uint32_t u;
         memcpy(&u, &a, sizeof(u));
         u &= (a == a) ? 0xFFFFFFFFu : 0u;
         rm = u > rm ? u : rm;
+        re += (int32_t)((j > i) & (w != 0.0f));
       }
       float rmax;
       memcpy(&rmax, &rm, sizeof(rmax));
       // the off-diagonal sums of J and J^2, kept only for integer couplings: exact integer sums
-      // (a row sum of |J| < 2^15 stays below 2^31 for n <= 65536)
-      if (rb == 0 && rmax < 32768.0f) {
+      // (a row sum of |J| < 2^15 stays below 2^31 for n <= 65536); the row is still in L1
+      if (rb == 0 && (double)rmax * (double)rmax * (double)n < 2147483648.0) {
+        // every partial sum of J^2 fits int32 too (the common case: small integer couplings)
+        int32_t s1 = 0, s2 = 0;
+        for (int j = 0; j < n; ++j) {
+          const int32_t v = (int32_t)Ji[j];
+          s1 += v;
+          s2 += v * v;
+        }
+        const int64_t dg = (int64_t)Ji[i];  // the diagonal does not count
+        a1 += (int64_t)s1 - dg;
+        a2 += (int64_t)s2 - dg * dg;
+      } else if (rb == 0 && rmax < 32768.0f) {
         int32_t s1 = 0;
         int64_t s2 = 0;
         for (int j = 0; j < n; ++j) {
@@ -487,8 +566,6 @@ void sbh::problem_scan(sb_problem *p) {
           a2 += v * v;
         }
       }
-      int64_t re = 0;
-      for (int j = i + 1; j < n; ++j) re += Ji[j] != 0.0f ? 1 : 0;
       bad |= rb != 0 ? 1 : 0;
       m = rmax > m ? rmax : m;
       e += re;
@@ -499,14 +576,7 @@ void sbh::problem_scan(sb_problem *p) {
     sj[t] = (double)a1;
     sj2[t] = (double)a2;
   };
-  if (nt == 1) {
-    rows(0);
-  } else {
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; ++t) th.emplace_back(rows, t);
-    rows(0);
-    for (auto &x : th) x.join();
-  }
+  parallel_run(nt, rows);
   bool integral = true;
   double maxabs = 0.0, s1 = 0.0, s2 = 0.0;
   int64_t edges = 0;
