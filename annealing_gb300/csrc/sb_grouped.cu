@@ -188,10 +188,7 @@ CouplingSums pack_rows(int n, uint8_t *dst, int Np, int row_bytes, int64_t elems
     part[w].s = a;
     part[w].s2 = a2;
   };
-  std::vector<std::thread> th;
-  for (unsigned w = 1; w < nt; ++w) th.emplace_back(work, w);
-  work(0);
-  for (auto &t : th) t.join();
+  sbh::parallel_run((int)nt, [&](int w) { work((unsigned)w); });
   CouplingSums out;
   for (const auto &c : part) {
     out.s += c.s;
