@@ -6,8 +6,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <pthread.h>
+
 #include <condition_variable>
 #include <deque>
+#include <new>
 #include <functional>
 #include <mutex>
 #include <string>
@@ -422,11 +425,27 @@ std::string sbh::device_status_text(uint32_t status) {
 // dealt round-robin to host threads for large n; none of the three depends on the order.
 namespace {
 // The process-wide worker pool behind sbh::parallel_run: a queue of (loop, index) tasks.
+class HostPool;
+HostPool *g_pool = nullptr;  // never destroyed: its threads outlive static teardown
+std::mutex g_pool_mu;
+
+// A child process made by fork() has none of the parent's worker threads (and may have inherited a
+// lock held at the fork): it starts a pool of its own on first use.
+void pool_after_fork_child() {
+  new (&g_pool_mu) std::mutex();
+  g_pool = nullptr;
+}
+
 class HostPool {
  public:
   static HostPool &get() {
-    static HostPool *pool = new HostPool();  // never destroyed: its threads outlive static teardown
-    return *pool;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool) {
+      static const int registered = pthread_atfork(nullptr, nullptr, pool_after_fork_child);
+      (void)registered;
+      g_pool = new HostPool();
+    }
+    return *g_pool;
   }
   int size() const { return (int)workers_.size() + 1; }
   void run(int nt, const std::function<void(int)> &fn) {
