@@ -294,11 +294,16 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->denergy, energy_slots(*prm) * (size_t)pl->R * sizeof(double));
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
   PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
-  // plain FP32 SB whose rows fit one co-resident grid runs every step in one launch, unless
-  // SB_PLAIN_PERSIST=0 keeps the one-launch-per-step kernel
+  // plain FP32 dSB whose rows fit one co-resident grid runs every step in one launch (its signs
+  // travel as one tagged word per CTA: N=2000, 1000 steps 5.7 -> 2.2 ms). aSB and bSB exchange x
+  // itself, sixteen tagged words per CTA, and measured slower that way than with one launch per step
+  // (aSB 100 steps 0.78 -> 1.90 ms, bSB 1000 steps 6.27 -> 6.95 ms): they take one launch per step
+  // unless SB_PLAIN_PERSIST=1 asks for the one-launch form; SB_PLAIN_PERSIST=0 keeps one launch per
+  // step for dSB too
   if (mode == SB_FIELD_FP32 && !needs_trace(*prm) && prm->steps > 0) {
     const char *env = getenv("SB_PLAIN_PERSIST");
-    const int ctas = (env && env[0] == '0') ? 0 : sbk::plain_persist_ctas(pl->n, pl->R, pl->jp);
+    const bool want = env ? env[0] == '1' || (env[0] != '0' && prm->variant == SB_DSB) : prm->variant == SB_DSB;
+    const int ctas = want ? sbk::plain_persist_ctas(pl->n, pl->R, pl->jp) : 0;
     if (ctas > 0) {
       pl->words_bytes = (size_t)2 * ctas * 128;  // one 128-byte line per CTA's word
       PLAN_ALLOC(pl->dwords, pl->words_bytes);

@@ -667,10 +667,24 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
       if (!poll(src, t, v)) return false;
       sbits[tid] = (uint32_t)v & 0xFFFFu;
     } else {
-      for (int w = 0; w < kPersistRows; ++w) {
-        if (!poll(src + w, t, v)) return false;
-        xs[tid * kPersistRows + w] = __uint_as_float((uint32_t)v);
+      // the line's sixteen words are read together, one L2 round trip per poll, until every one
+      // carries this step's tag (one word at a time took sixteen round trips per step)
+      unsigned long long wv[kPersistRows];
+      const uint32_t want = (uint32_t)(t + 1);
+      const long long t0 = clock64();
+      int spins = 0;
+      for (;;) {
+#pragma unroll
+        for (int w = 0; w < kPersistRows; ++w) wv[w] = ld_relaxed_u64(src + w);
+        bool all = true;
+#pragma unroll
+        for (int w = 0; w < kPersistRows; ++w) all = all && (uint32_t)(wv[w] >> 32) == want;
+        if (all) break;
+        if (clock64() - t0 > ptx::kWaitCycles) return false;
+        if (++spins > 8) __nanosleep(32);
       }
+#pragma unroll
+      for (int w = 0; w < kPersistRows; ++w) xs[tid * kPersistRows + w] = __uint_as_float((uint32_t)wv[w]);
     }
     return true;
   };
