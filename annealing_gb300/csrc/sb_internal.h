@@ -54,7 +54,7 @@ struct PlainStep {
 // 16 sign bits), bSB / aSB sixteen (step tag << 32 | bits of x). Eligible when jp <= kPersistMaxJp
 // and G R CTAs (G = ceil(n / 16)) are co-resident.
 struct PlainPersist {
-  int variant;                // 0 aSB, 1 bSB (x exchanged), 2 dSB (signs exchanged)
+  int variant;                // 0 aSB, 1 bSB (x exchanged), 2 dSB (signs exchanged), 3 NMFA (states exchanged)
   int n, R, jp, xp;
   const float *J, *h;         // J [n][jp], h [n] or null
   const float *x_in;          // x(0) [R][xp]
@@ -66,6 +66,13 @@ struct PlainPersist {
   int steps;
   unsigned long long *words;  // [2][R][G] words, one per 128-byte line (16 x 8 bytes), zero on entry
   uint32_t *status;
+  // NMFA (variant 3): x holds the states s, pumps[t] the beta of sweep t (two sweeps per stage),
+  // norm [n] the row norms, rng [5][R][xp] the XORWOW words (read at the start, written at the end),
+  // samples [R][n] receives sign(s) after the last sweep (or null)
+  const float *norm;
+  uint32_t *rng;
+  int32_t *samples;
+  float noise, keep, mix;
 };
 constexpr int kPersistRows = 16;
 constexpr int kPersistMaxJp = 2048;

@@ -4,16 +4,20 @@
 // gpu_nmfa_kernel with one CTA per sample, copy the samples back, return the kernel's event time).
 // Here the samples are replicas. J is padded to [n][jp] once and every (sample, spin) gets its
 // XORWOW words from one seeding launch; then either
-//   * FP32 (the plain fused kernel's layout, sb_plain.cu): each of a stage's two sweeps is one fused
-//     launch (field + noise + tanh update), issued back to back so that consecutive launches overlap
-//     (programmatic dependent launch); the last sweep writes the +-1 samples and one energy pass
-//     gives every sample's energy; or
+//   * FP32 (the plain fused kernel's layout, sb_plain.cu): when the rows fit one co-resident grid
+//     (few samples: the reference program's single sample), every sweep runs in one cooperative
+//     launch of the plain solve's persistent kernel (J rows in registers, the states exchanged as
+//     tagged words through L2, the same summation order and bits); otherwise each of a stage's two
+//     sweeps is one fused launch (field + noise + tanh update), issued back to back so that
+//     consecutive launches overlap (programmatic dependent launch); the last sweep writes the +-1
+//     samples and one energy pass gives every sample's energy; or
 //   * tensor cores (sb_tc_kernel.cuh, variant 3): all sweeps in one persistent tcgen05 launch, the
 //     states as BF16 hi + lo against exact BF16 couplings, then one launch writes the samples and
 //     the dSB energy contraction on the same couplings gives the energies.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
@@ -45,6 +49,8 @@ struct NmfaCache {
   uint32_t *drng = nullptr, *dstatus = nullptr;
   int32_t *dsamp = nullptr;
   double *den = nullptr;
+  unsigned long long *dwords = nullptr;  // the one-launch FP32 solve's exchange lines
+  size_t words_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -61,6 +67,7 @@ void nmfa_cache_free(NmfaCache *c) {
   cudaFree(c->dstatus);
   cudaFree(c->dsamp);
   cudaFree(c->den);
+  cudaFree(c->dwords);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   delete c;
@@ -95,6 +102,7 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     return fail(ctx, SB_ERR_UNSUPPORTED, std::string(who) + ": the tensor-core field needs integer couplings "
                                                             "with |J| <= 256");
   bool use_tc = prm->field_mode == SB_FIELD_TC || (prm->field_mode == SB_FIELD_AUTO && tc_ok && R >= 32);
+  int persist_ctas = 0;  // FP32 field: CTAs of the one-launch solve, 0 when it does not fit
   std::vector<float> sweep_betas((size_t)2 * stages);
   for (int t = 0; t < 2 * stages; ++t) sweep_betas[t] = betas[t / 2];
   cudaSetDevice(ctx->device);
@@ -182,6 +190,19 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
       }
     }
   }
+  if (!use_tc) {
+    // SB_PLAIN_PERSIST=0 keeps one launch per sweep
+    const char *env = getenv("SB_PLAIN_PERSIST");
+    persist_ctas = (env && env[0] == '0') ? 0 : sbk::plain_persist_ctas(n, R, jp);
+    const size_t need = (size_t)2 * persist_ctas * 128;  // one 128-byte line per CTA and parity
+    if (persist_ctas > 0 && c->words_bytes < need) {
+      cudaFree(c->dwords);
+      c->dwords = nullptr;
+      c->words_bytes = 0;
+      NM_CUDA(cudaMalloc((void **)&c->dwords, need));
+      c->words_bytes = need;
+    }
+  }
   NM_CUDA(cudaEventRecord(c->ev0, st));
   NM_CUDA(sbk::launch_nmfa_seed(c->drng, n, R, xp, prm->seed, st));
   ++launches;
@@ -192,6 +213,47 @@ sb_status nmfa_run(sb_ctx *ctx, const sb_problem *prob, const sb_nmfa_params *pr
     NM_CUDA(sbk::launch_nmfa_signs(c->ds, n, R, xp, c->dsamp, st));
     NM_CUDA(sbk::tc_energy_signs(c->te, c->ds, nullptr, c->den, c->dstatus, st));
     launches += 5;
+  } else if (persist_ctas > 0) {
+    // every sweep in one cooperative launch: J rows in registers, states exchanged as tagged words
+    // (the plain solve's one-launch kernel with the NMFA update; the same bits as one launch per
+    // sweep)
+    NM_CUDA(cudaMemsetAsync(c->dwords, 0, c->words_bytes, st));
+    sbk::PlainPersist a;
+    memset(&a, 0, sizeof(a));
+    a.variant = 3;
+    a.n = n;
+    a.R = R;
+    a.jp = jp;
+    a.xp = xp;
+    a.J = c->dJ;
+    a.x_in = c->ds;
+    a.x_out = c->ds;
+    a.pumps = c->dbetas;
+    a.steps = 2 * stages;
+    a.words = c->dwords;
+    a.status = c->dstatus;
+    a.norm = c->dnorm;
+    a.rng = c->drng;
+    a.samples = c->dsamp;
+    a.noise = prm->noise;
+    a.keep = (float)(1.0 - (double)prm->recombination);  // nmfa.cu:95, 1.0 - recombination
+    a.mix = prm->recombination;
+    NM_CUDA(sbk::launch_plain_persist(a, st));
+    ++launches;
+    sbk::PlainEnergy pe;
+    memset(&pe, 0, sizeof(pe));
+    pe.n = n;
+    pe.R = R;
+    pe.jp = jp;
+    pe.xp = xp;
+    pe.rb = rb;
+    pe.J = c->dJ;
+    pe.h = nullptr;
+    pe.x = c->ds;
+    pe.energy = c->den;
+    pe.status = c->dstatus;
+    NM_CUDA(sbk::launch_plain_energy(pe, !exact, st));
+    ++launches;
   } else {
     sbk::NmfaSweep a;
     memset(&a, 0, sizeof(a));

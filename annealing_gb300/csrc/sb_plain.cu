@@ -620,9 +620,21 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   float x = 0.0f, y = 0.0f;
   if (have && SB_BOUNDS(k_xy < (size_t)a.R * a.xp, a.status)) {
     x = a.x_in[k_xy];
-    y = a.y[k_xy];
+    if constexpr (VARIANT != 3) y = a.y[k_xy];
   }
   const float hv = (have && a.h) ? a.h[row] : 0.0f;
+  // NMFA: the row norm, the spin's XORWOW words and the stage's second Gaussian sample (drawn with
+  // the first on the stage's first sweep, used on its second)
+  const size_t plane = (size_t)a.R * a.xp;
+  float nv = 0.0f, z1 = 0.0f;
+  uint32_t wd[5] = {0u, 0u, 0u, 0u, 0u};
+  if constexpr (VARIANT == 3) {
+    if (have && SB_BOUNDS(k_xy < plane, a.status)) {
+      nv = a.norm[row];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) wd[q] = a.rng[q * plane + k_xy];
+    }
+  }
   // one 128-byte line per CTA: its store(s) and the other CTAs' polls share no line with any other
   // CTA's words
   constexpr int kLine = 16;                                       // words per line
@@ -660,33 +672,46 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   };
   // thread q < G: CTA q's word(s) of step t into shared memory; false when a wait gave up
   auto gather = [&](int t) -> bool {
-    if (tid >= G) return true;
-    const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
-    unsigned long long v;
     if constexpr (kSigns) {
+      if (tid >= G) return true;
+      const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
+      unsigned long long v;
       if (!poll(src, t, v)) return false;
       sbits[tid] = (uint32_t)v & 0xFFFFu;
+      return true;
     } else {
-      // the line's sixteen words are read together, one L2 round trip per poll, until every one
-      // carries this step's tag (one word at a time took sixteen round trips per step)
-      unsigned long long wv[kPersistRows];
+      // sixteen threads read a CTA's line together (one 128-byte request per line and poll, where
+      // one thread per line took sixteen): thread tid takes word tid % 16 of lines tid / 16 + 32 k,
+      // and each warp polls its lines until all of their words carry this step's tag
+      constexpr int kLinesPerPass = kPersistThreads / kLine;                   // 32
+      constexpr int kPasses = kPersistMaxJp / kPersistRows / kLinesPerPass;    // G <= 128: 4
+      const int w = tid & (kLine - 1), q0 = tid / kLine;
+      const unsigned long long *base = wr + (size_t)(t & 1) * par;
       const uint32_t want = (uint32_t)(t + 1);
+      unsigned long long wv[kPasses];
       const long long t0 = clock64();
       int spins = 0;
       for (;;) {
 #pragma unroll
-        for (int w = 0; w < kPersistRows; ++w) wv[w] = ld_relaxed_u64(src + w);
-        bool all = true;
+        for (int k = 0; k < kPasses; ++k) {
+          const int q = q0 + kLinesPerPass * k;
+          if (q < G) wv[k] = ld_relaxed_u64(base + (size_t)q * kLine + w);
+        }
+        bool mine = true;
 #pragma unroll
-        for (int w = 0; w < kPersistRows; ++w) all = all && (uint32_t)(wv[w] >> 32) == want;
-        if (all) break;
-        if (clock64() - t0 > ptx::kWaitCycles) return false;
+        for (int k = 0; k < kPasses; ++k)
+          if (q0 + kLinesPerPass * k < G) mine = mine && (uint32_t)(wv[k] >> 32) == want;
+        if (__all_sync(0xffffffffu, mine)) break;
+        if (__shfl_sync(0xffffffffu, (clock64() - t0 > ptx::kWaitCycles) ? 1 : 0, 0)) return false;
         if (++spins > 8) __nanosleep(32);
       }
 #pragma unroll
-      for (int w = 0; w < kPersistRows; ++w) xs[tid * kPersistRows + w] = __uint_as_float((uint32_t)wv[w]);
+      for (int k = 0; k < kPasses; ++k) {
+        const int q = q0 + kLinesPerPass * k;
+        if (q < G) xs[q * kLine + w] = __uint_as_float((uint32_t)wv[k]);
+      }
+      return true;
     }
-    return true;
   };
   publish(0);
   bool ok = true;
@@ -725,8 +750,20 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
       if constexpr (VARIANT == 0) {
         // aSB: the coupling kick, then the next step's local sub-steps (none after the last)
         y = __fmaf_rn(a.coeff, acc, y);
-        if (t + 1 < a.steps)
-          asb_local(x, y, __fdiv_rn((float)(t + 1), (float)a.steps), a.m, a.mts_dt, a.detune, a.kerr);
+        if (t + 1 < a.steps) {
+          // the FP64 sub-steps once per row (lane 0), not in every lane: FP64 is scarce on this part
+          if (lane == 0) asb_local(x, y, __fdiv_rn((float)(t + 1), (float)a.steps), a.m, a.mts_dt, a.detune, a.kerr);
+          x = __shfl_sync(0xffffffffu, x, 0);
+          y = __shfl_sync(0xffffffffu, y, 0);
+        }
+      } else if constexpr (VARIANT == 3) {
+        // NMFA sweep t (stage t / 2): the stage's first sweep draws its Gaussian pair
+        float z;
+        if ((t & 1) == 0)
+          sbm::nmfa_gauss(wd, a.noise, z, z1);
+        else
+          z = z1;
+        x = sbm::nmfa_update(acc, nv, z, pump, a.keep, a.mix, x);
       } else {
         sb_update(acc, hv, pump, a.c0, a.dt, a.dta0, x, y);
       }
@@ -739,7 +776,13 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   }
   if (have && lane == 0 && SB_BOUNDS(k_xy < (size_t)a.R * a.xp, a.status)) {
     a.x_out[k_xy] = x;
-    a.y[k_xy] = y;
+    if constexpr (VARIANT == 3) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) a.rng[q * plane + k_xy] = wd[q];
+      if (a.samples) a.samples[(size_t)r * a.n + row] = x > 0.0f ? 1 : -1;
+    } else {
+      a.y[k_xy] = y;
+    }
   }
 }
 
@@ -830,8 +873,8 @@ int plain_persist_ctas(int n, int R, int jp) {
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 0;
   // the variants differ in registers: the least co-resident one decides
-  const void *ks[3] = {(const void *)plain_persist_kernel<0>, (const void *)plain_persist_kernel<1>,
-                       (const void *)plain_persist_kernel<2>};
+  const void *ks[4] = {(const void *)plain_persist_kernel<0>, (const void *)plain_persist_kernel<1>,
+                       (const void *)plain_persist_kernel<2>, (const void *)plain_persist_kernel<3>};
   for (const void *k : ks) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kPersistThreads, 0) != cudaSuccess) return 0;
@@ -857,6 +900,7 @@ cudaError_t launch_plain_persist(const PlainPersist &a, cudaStream_t st) {
     case 0: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<0>, a);
     case 1: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<1>, a);
     case 2: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<2>, a);
+    case 3: return cudaLaunchKernelEx(&cfg, plain_persist_kernel<3>, a);
   }
   return cudaErrorInvalidValue;
 }

@@ -45,7 +45,13 @@ def _energies(J, samples):
     (600, 9, 3, "fully"),      # two chunks of K, staged layout
     (2050, 2, 2, "pm1"),       # five chunks of K through a four-stage ring (refills)
 ])
-def test_bit_exact_vs_oracle(ctx, n, R, stages, kind):
+@pytest.mark.parametrize("one_launch", [True, False], ids=["one-launch", "per-sweep"])
+def test_bit_exact_vs_oracle(ctx, monkeypatch, n, R, stages, kind, one_launch):
+    """Both FP32 forms: every sweep in one cooperative launch (shapes whose rows fit one co-resident
+    grid: ceil(n / 16) x samples CTAs, padded rows <= 2048) and one launch per sweep."""
+    if not one_launch:
+        monkeypatch.setenv("SB_PLAIN_PERSIST", "0")
+    fits = ((n + 15) // 16) * R <= 152 and (n + 3) // 4 * 4 <= 2048
     J = instances.nmfa_fully(n, seed=n + 7) if kind == "fully" else instances.complete_pm1(n, seed=n + 7)
     betas = sb.nmfa_schedule(100)[:stages]
     p = sb.NmfaParams.default(samples=R, seed=99 + n, field_mode=sb.FIELD_FP32)
@@ -57,7 +63,8 @@ def test_bit_exact_vs_oracle(ctx, n, R, stages, kind):
     e = _energies(J, sp)
     assert np.array_equal(res.energies, e.astype(np.float64))
     assert res.best_energy == e.min() and res.energy_check_ok
-    assert res.kernel_launches == 1 + 2 * stages + 1 and res.field_mode_used == sb.FIELD_FP32
+    sweeps = 1 if (one_launch and fits) else 2 * stages
+    assert res.kernel_launches == 1 + sweeps + 1 and res.field_mode_used == sb.FIELD_FP32
 
 
 def test_real_couplings_bit_exact(ctx):
