@@ -12,14 +12,14 @@
 // kNoAllocScratchBytes until the process exits. Host code cannot use the array's name as a device
 // address (on the host it names a stand-in object; a kernel given it would fault or silently use
 // the wrong memory), so the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current, and later calls reuse it. Make that first
-// call before any stream capture. Every call shares the one array and the array keeps the last
+// cudaGetSymbolAddress while that device is current, and later calls reuse it. Every call shares
+// the one array and the array keeps the last
 // call's contents: the parts that must start at zero are cleared by each call, and calls that
 // overlap on the GPU (different streams or threads at the same time) race on it.
 //
 // The call is synchronous: it reads the coupling scan back before the solve (couplings that no
 // operand type holds exactly are rejected without running a step) and the device status after it,
-// waiting for `stream` each time. Integer couplings with |J| <= 4 run on packed E2M1 operands when
+// waiting for `stream` each time, so no call can run under stream capture. Integer couplings with |J| <= 4 run on packed E2M1 operands when
 // the kernel that keeps J in shared memory fits the shape, others (|J| <= 16) on FP8; both give the
 // same bits as sb_solve's tensor-core dSB.
 #include <cuda_runtime.h>

@@ -396,8 +396,9 @@ sb_status sb_sqa_solve(sb_ctx *ctx, const sb_problem *p, const sb_sqa_params *pa
  * Scratch is one fixed array of 8,458,240 bytes in the library's device memory, held by every GPU
  * that loads the library until the process exits; hence the limits n <= 2048, replicas <= 1024,
  * steps <= 16384 (larger sizes return SB_ERR_INVALID_ARG). The first call on a device looks up
- * the array's device address; make that first call before any stream capture. All calls share the
- * array: calls that overlap on the GPU (other streams or threads at the same time) race. */
+ * the array's device address. No call can run under stream capture (each one waits for `stream`
+ * and reads its status back into host memory). All calls share the array: calls that overlap on
+ * the GPU (other streams or threads at the same time) race. */
 sb_status sb_dsb_solve_noalloc(const float *d_J, const float *d_h, int32_t n, int32_t replicas,
                                int32_t steps, uint64_t seed, float dt, float a0, float c0,
                                float *d_x, float *d_y, double *d_energies, void *stream);
