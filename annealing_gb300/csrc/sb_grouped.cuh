@@ -1,8 +1,8 @@
 // Grouped tcgen05 SB step over many instances of uneven size (dSB; packed E2M1, packed E2M3 or
 // FP8 E4M3 operands).
 //
-// The batched workloads of the benchmark spec (hundreds of instances with N from 64 to 16384, each
-// with its own replicas, and the serving stream) do not fit the one-unit-per-SM residency of
+// Uneven batches (hundreds of instances with N from 64 to 16384, each with its own replicas) and
+// the serving stream do not fit the one-unit-per-SM residency of
 // the single-instance kernel (sb_tc_kernel.cuh): their state is far larger than TMEM. Here one
 // launch advances every instance by one SB step:
 //   * work item = (instance, 128-spin tile, NR-replica tile); the CTAs of a persistent grid (one

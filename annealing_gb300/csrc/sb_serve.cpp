@@ -94,7 +94,7 @@ struct Server {
   sb_ctx *solo = nullptr;  // requests outside the grouped engine
   Clock::time_point t_start = Clock::now();
   // exact host re-checks run on their own threads so the device loop never waits for them
-  std::vector<std::thread> checkers;
+  std::vector<std::thread> energy_threads;
   std::deque<std::pair<Req *, sb_status>> check_q;
   std::condition_variable check_cv;
   bool check_stop = false;
@@ -386,7 +386,7 @@ sb_status server_create(Server **out, int device, int64_t hbm_budget, int max_in
   s->worker = std::thread([s] { s->run(); });
   for (int w = 0; w < Server::kPreparers; ++w) s->preparer[w] = std::thread([s, w] { s->prepare_loop(w); });
   const unsigned nc = std::max(2u, std::min(8u, std::thread::hardware_concurrency() / 2));
-  for (unsigned k = 0; k < nc; ++k) s->checkers.emplace_back([s] { s->check_loop(); });
+  for (unsigned k = 0; k < nc; ++k) s->energy_threads.emplace_back([s] { s->check_loop(); });
   *out = s;
   return SB_OK;
 }
@@ -407,7 +407,7 @@ void server_destroy(Server *s) {
     s->check_stop = true;
   }
   s->check_cv.notify_all();
-  for (auto &t : s->checkers) t.join();
+  for (auto &t : s->energy_threads) t.join();
   cudaSetDevice(s->device);
   for (auto &kv : s->groups) delete kv.second;
   for (auto &kv : s->reqs) delete kv.second;

@@ -718,7 +718,7 @@ constexpr size_t tc_smem() {
   return (size_t)tc_stages<DT, VARIANT, NR>() * kStage + tc_vtile_bytes<DT, VARIANT, NR>() + 1024;
 }
 
-// Kernel for one epilogue mode; MODES is the bit set of modes this build instantiates.
+// Kernel for one epilogue mode; MODES is the bit set of modes compiled in.
 template <int DT, int VARIANT, int NR, int MODES>
 inline bool tc_lookup(int emode, const void **k, size_t *smem) {
   constexpr int S = tc_stages<DT, VARIANT, NR>();

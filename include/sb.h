@@ -34,7 +34,7 @@
  * Threading: one CUDA stream per context; every call on a context is serialised by the context's
  * own mutex, so a context may be shared by threads. Different contexts run concurrently.
  *
- * Energy convention (README.md:9-13): H(s) = -sum_{i<j} J_ij s_i s_j - sum_i h_i s_i, with
+ * Energy convention (the reference project's README.md:9-13): H(s) = -sum_{i<j} J_ij s_i s_j - sum_i h_i s_i, with
  * s_i = (x_i > 0) ? +1 : -1 (SB/CUDA_GPU/m2_opt.cu:197-198). With h = 0 this is exactly the value
  * the reference writes to output.txt (it stores -E, m2_opt.cu:202).
  */

@@ -150,7 +150,8 @@ def nmfa_schedule(stages):
 
 class NmfaKernel:
     """gpu_nmfa_kernel for N spins: one CTA of N threads per sample, N floats of dynamic shared
-    memory; this build's last store writes the final mean-field state instead of its sign."""
+    memory; as oracle/build_ref.py expands it, its last store writes the final mean-field state
+    instead of its sign."""
 
     def __init__(self, n):
         self.cu = _driver()

@@ -15,7 +15,7 @@
  * (2) the field F = V * J^T as a blocked FP32 product over 64x64 (replica, spin) tiles with 4x4
  *     register micro-tiles (GCC vector extensions, portable to x86-64 and aarch64);
  * (3) per replica: the state update.
- * Build: -O3 -ffp-contract=fast (this file is a timed baseline, not a bit-exact checker).
+ * Build: -O3 -ffp-contract=fast (this file is a timed baseline, not a bit-exact restatement).
  */
 #include <math.h>
 #include <pthread.h>

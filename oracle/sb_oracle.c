@@ -2,7 +2,7 @@
  * CPU oracle for the SB step loop — TEST INFRASTRUCTURE ONLY.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this library, and
- * only as the checker or the timed CPU baseline. The solver never calls it.
+ * only to verify results or as the timed CPU baseline. The solver never calls it.
  *
  * What it restates (reference file:line, paths inside strongshih/Annealing):
  *   oracle_xorshift32 / oracle_init_reference   SB/CUDA_GPU/m2_opt.cu:38-56 (xorshift32,
@@ -19,7 +19,7 @@
  *       here is summed in index order (the order of the cuBLAS-free twin
  *       SB/CUDA_GPU/Bifurcation_m2.cu.c:93-95) and the kick is fmaf(coeff1, f, y).
  *   oracle_energy_i64 / oracle_energy_f64       SB/CUDA_GPU/m2_opt.cu:192-202 with
- *       s = x > 0 ? 1 : -1 and the reported value -E; h_i s_i terms follow README.md:9-13.
+ *       s = x > 0 ? 1 : -1 and the reported value -E; h_i s_i terms follow the reference project's README.md:9-13.
  *   oracle_sb_update_f32 / oracle_sb_run        bSB / dSB of Goto et al., Sci. Adv. 7, eabe7953
  *       (2021) (no reference code exists for these): y += dt*(-(a0-a(t)) x + c0 (f + h)),
  *       x += dt*a0*y, |x| > 1 -> x = sign(x), y = 0, with f = J x (bSB) or J sign(x) (dSB). The

@@ -235,7 +235,7 @@ def test_config3_split_bf16_error_vs_fp64():
             d = (torch.from_numpy(res.final_x).to(dev).double() - x).abs()
             off = int((d.max(dim=1).values > 1e-2).sum())
             p99 = float(d.flatten().kthvalue(int(0.99 * d.numel())).values)
-            print(f"config-3 split-bf16 after {K} steps: max |x - x_fp64| = {float(d.max()):.3g}, "
+            print(f"bSB N={n} R={R} split-bf16 after {K} steps: max |x - x_fp64| = {float(d.max()):.3g}, "
                   f"p99 {p99:.3g}, median {float(d.median()):.3g}, replicas off by > 1e-2: {off} of {R}")
             if K == 2:
                 assert float(d.max()) <= 1e-5
