@@ -294,16 +294,13 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->denergy, energy_slots(*prm) * (size_t)pl->R * sizeof(double));
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
   PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
-  // plain FP32 dSB and bSB whose rows fit one co-resident grid run every step in one launch
-  // (N=2000, 1000 steps: dSB 5.7 -> 2.2 ms, its signs one tagged word per CTA; bSB 6.3 -> 1.8 ms, x
-  // as sixteen tagged words per CTA read by sixteen threads together). aSB's FP64 sub-steps sit on
-  // each row's critical path there, and it measured a little slower that way (100 steps 0.84 against
-  // 0.78 ms), so it keeps one launch per step unless SB_PLAIN_PERSIST=1; SB_PLAIN_PERSIST=0 keeps one
-  // launch per step for every variant
+  // plain FP32 solves whose rows fit one co-resident grid run every step in one launch (N=2000,
+  // 1000 steps: dSB 5.7 -> 2.2 ms, its signs one tagged word per CTA; bSB 6.3 -> 1.5 ms and aSB
+  // 7.4 -> 2.6 ms, x as sixteen tagged words per CTA read by sixteen threads together, aSB's FP64
+  // sub-steps for a CTA's 16 rows in one warp); SB_PLAIN_PERSIST=0 keeps one launch per step
   if (mode == SB_FIELD_FP32 && !needs_trace(*prm) && prm->steps > 0) {
     const char *env = getenv("SB_PLAIN_PERSIST");
-    const bool by_default = prm->variant == SB_DSB || prm->variant == SB_BSB;
-    const bool want = env ? env[0] == '1' || (env[0] != '0' && by_default) : by_default;
+    const bool want = !(env && env[0] == '0');
     const int ctas = want ? sbk::plain_persist_ctas(pl->n, pl->R, pl->jp) : 0;
     if (ctas > 0) {
       pl->words_bytes = (size_t)2 * ctas * 128;  // one 128-byte line per CTA's word

@@ -598,6 +598,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   __shared__ uint32_t sbits[kPersistMaxJp / kPersistRows];  // dSB: the G words' sign bits
   __shared__ __align__(16) float xs[kPersistMaxJp];          // bSB / aSB: x(t) of every spin
   __shared__ uint32_t sout[kPersistRows];
+  __shared__ float sx[kPersistRows], sy[kPersistRows];  // aSB: the rows' x, y for the FP64 sub-steps
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c = blockIdx.x, r = blockIdx.y, G = gridDim.x;
   const int row = c * kPersistRows + warp;
@@ -748,14 +749,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (have) {
       if constexpr (VARIANT == 0) {
-        // aSB: the coupling kick, then the next step's local sub-steps (none after the last)
+        // aSB: the coupling kick; the next step's local sub-steps follow below
         y = __fmaf_rn(a.coeff, acc, y);
-        if (t + 1 < a.steps) {
-          // the FP64 sub-steps once per row (lane 0), not in every lane: FP64 is scarce on this part
-          if (lane == 0) asb_local(x, y, __fdiv_rn((float)(t + 1), (float)a.steps), a.m, a.mts_dt, a.detune, a.kerr);
-          x = __shfl_sync(0xffffffffu, x, 0);
-          y = __shfl_sync(0xffffffffu, y, 0);
-        }
       } else if constexpr (VARIANT == 3) {
         // NMFA sweep t (stage t / 2): the stage's first sweep draws its Gaussian pair
         float z;
@@ -768,7 +763,28 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
         sb_update(acc, hv, pump, a.c0, a.dt, a.dta0, x, y);
       }
     }
-    publish(t + 1);  // its barrier also ends this step's reads of sbits / xs
+    if constexpr (VARIANT == 0) {
+      if (t + 1 < a.steps) {
+        // aSB: the next step's FP64 local sub-steps (none after the last) for the CTA's 16 rows in
+        // 16 lanes of one warp, where one lane per row warp would issue 16 times the FP64 warp
+        // instructions (FP64 is scarce on this part); rows past n run on x = y = 0 and stay 0
+        if (lane == 0) {
+          sx[warp] = x;
+          sy[warp] = y;
+        }
+        __syncthreads();
+        if (warp == 0 && lane < kPersistRows) {
+          float lx = sx[lane], ly = sy[lane];
+          asb_local(lx, ly, __fdiv_rn((float)(t + 1), (float)a.steps), a.m, a.mts_dt, a.detune, a.kerr);
+          sx[lane] = lx;
+          sy[lane] = ly;
+        }
+        __syncthreads();
+        x = sx[warp];
+        y = sy[warp];
+      }
+    }
+    publish(t + 1);  // its barrier also ends this step's reads of sbits / xs (and sx, sy)
   }
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);

@@ -71,13 +71,13 @@ def test_dsb_one_launch_equals_per_step(ctx, n, R, steps, persist, monkeypatch):
 @pytest.mark.parametrize("variant,n,R,steps", [(sb.BSB, 2000, 1, 60), (sb.BSB, 300, 3, 40), (sb.ASB, 2048, 1, 30),
                                                (sb.ASB, 130, 2, 25)])
 def test_bsb_asb_one_launch_equals_per_step(variant, n, R, steps, monkeypatch):
-    """bSB (one launch by default) and aSB (the reference's update; one launch on request,
-    SB_PLAIN_PERSIST=1) in one cooperative launch exchange x itself (16 tagged words on a CTA's line):
-    bit for bit the one-launch-per-step kernel's trajectories and energies (SB_PLAIN_PERSIST=0)."""
+    """bSB and aSB (the reference's update, its FP64 sub-steps for a CTA's 16 rows in one warp) in
+    one cooperative launch, their default, exchange x itself (16 tagged words on a CTA's line): bit
+    for bit the one-launch-per-step kernel's trajectories and energies (SB_PLAIN_PERSIST=0)."""
     J = instances.complete_pm1(n, seed=n) if variant == sb.ASB else instances.gaussian(n, seed=n)[0]
     prob = sb.Problem.from_dense(J)
     prm = sb.Params.default(variant, steps=steps, replicas=R, seed=11, field_mode=sb.FIELD_FP32)
-    monkeypatch.setenv("SB_PLAIN_PERSIST", "1")
+    monkeypatch.delenv("SB_PLAIN_PERSIST", raising=False)
     ctx1 = sb.Context(0)
     try:
         res = ctx1.solve(prob, prm, want_state=True)
