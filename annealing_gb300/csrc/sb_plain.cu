@@ -576,8 +576,10 @@ int grid_for(size_t total) {
 // g = L + 32 k, k < kPersistGroups, the order dot_chunk sums in), its x, y in registers too. A
 // step needs sign(x(t)) of every spin; CTA c's 16 signs travel in one 64-bit word
 // (tag t + 1 << 32 | bit w = x_i <= 0) at words[t & 1][r][c]: the tag is the flag, so one L2 round
-// trip per step moves all the data. A CTA rewrites parity t & 1 with step t + 2 only after every
-// CTA has published step t + 1, which each did after reading all of step t's words.
+// trip per step moves all the data; the thread that polls a word writes its 16 signs into shared
+// memory as +-1.0, so the field sums the same products as the bSB / aSB form, which exchanges x
+// itself as sixteen tagged words per CTA. A CTA rewrites parity t & 1 with step t + 2 only after
+// every CTA has published step t + 1, which each did after reading all of step t's words.
 constexpr int kPersistThreads = 32 * kPersistRows;
 constexpr int kPersistGroups = kPersistMaxJp / 128;  // float4 groups per lane
 
@@ -595,8 +597,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
   // dSB exchanges signs: one word per CTA (tag << 32 | 16 sign bits). bSB / aSB exchange x: the 16
   // words of a CTA's line are its rows' (tag << 32 | bits of x), one written by each warp.
   constexpr bool kSigns = VARIANT == 2;
-  __shared__ uint32_t sbits[kPersistMaxJp / kPersistRows];  // dSB: the G words' sign bits
-  __shared__ __align__(16) float xs[kPersistMaxJp];          // bSB / aSB: x(t) of every spin
+  __shared__ __align__(16) float xs[kPersistMaxJp];  // x(t) of every spin (dSB: its sign, +-1)
   __shared__ uint32_t sout[kPersistRows];
   __shared__ float sx[kPersistRows], sy[kPersistRows];  // aSB: the rows' x, y for the FP64 sub-steps
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -648,10 +649,9 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
     if constexpr (kSigns) {
       if (lane == 0) sout[warp] = (!have || !(x > 0.0f)) ? 1u : 0u;  // sgn: x > 0 -> +1, else -1
       __syncthreads();
-      if (tid == 0) {
-        uint32_t b = 0;
-        for (int w = 0; w < kPersistRows; ++w) b |= sout[w] << w;
-        st_relaxed_u64(line, tag | b);
+      if (warp == 0) {
+        const uint32_t b = __ballot_sync(0xffffffffu, lane < kPersistRows && sout[lane] != 0u);
+        if (lane == 0) st_relaxed_u64(line, tag | b);
       }
     } else {
       if (lane == 0) st_relaxed_u64(line + warp, tag | __float_as_uint(have ? x : 0.0f));
@@ -671,14 +671,20 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
     } while ((uint32_t)(v >> 32) != (uint32_t)(t + 1));
     return true;
   };
-  // thread q < G: CTA q's word(s) of step t into shared memory; false when a wait gave up
+  // x(t) of every spin into xs (dSB: the signs as +-1.0); false when a wait gave up
   auto gather = [&](int t) -> bool {
     if constexpr (kSigns) {
+      // thread q < G polls CTA q's word and writes its 16 signs (bit w set: spin 16 q + w is -1)
       if (tid >= G) return true;
       const unsigned long long *src = wr + (size_t)(t & 1) * par + (size_t)tid * kLine;
       unsigned long long v;
       if (!poll(src, t, v)) return false;
-      sbits[tid] = (uint32_t)v & 0xFFFFu;
+      const uint32_t b = (uint32_t)v;
+      float4 *dst = reinterpret_cast<float4 *>(xs) + 4 * tid;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        dst[k] = make_float4((b >> (4 * k)) & 1u ? -1.0f : 1.0f, (b >> (4 * k + 1)) & 1u ? -1.0f : 1.0f,
+                             (b >> (4 * k + 2)) & 1u ? -1.0f : 1.0f, (b >> (4 * k + 3)) & 1u ? -1.0f : 1.0f);
       return true;
     } else {
       // sixteen threads read a CTA's line together (one 128-byte request per line and poll, where
@@ -729,20 +735,11 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
       const int g = lane + 32 * k;
       if (g < ng) {
         const float4 jv = jr[k];
-        if constexpr (kSigns) {
-          // bits 4 (g % 4) .. of CTA g / 4's word; sign -1 where the bit is set
-          const uint32_t nib = sbits[g >> 2] >> (4 * (g & 3));
-          acc = __fmaf_rn(jv.x, (nib & 1u) ? -1.0f : 1.0f, acc);
-          acc = __fmaf_rn(jv.y, (nib & 2u) ? -1.0f : 1.0f, acc);
-          acc = __fmaf_rn(jv.z, (nib & 4u) ? -1.0f : 1.0f, acc);
-          acc = __fmaf_rn(jv.w, (nib & 8u) ? -1.0f : 1.0f, acc);
-        } else {
-          const float4 xv = reinterpret_cast<const float4 *>(xs)[g];
-          acc = __fmaf_rn(jv.x, xv.x, acc);
-          acc = __fmaf_rn(jv.y, xv.y, acc);
-          acc = __fmaf_rn(jv.z, xv.z, acc);
-          acc = __fmaf_rn(jv.w, xv.w, acc);
-        }
+        const float4 xv = reinterpret_cast<const float4 *>(xs)[g];
+        acc = __fmaf_rn(jv.x, xv.x, acc);
+        acc = __fmaf_rn(jv.y, xv.y, acc);
+        acc = __fmaf_rn(jv.z, xv.z, acc);
+        acc = __fmaf_rn(jv.w, xv.w, acc);
       }
     }
 #pragma unroll
@@ -784,7 +781,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) plain_persist_kernel(Plain
         y = sy[warp];
       }
     }
-    publish(t + 1);  // its barrier also ends this step's reads of sbits / xs (and sx, sy)
+    publish(t + 1);  // its barrier also ends this step's reads of xs (and sx, sy)
   }
   if (!ok) {
     if (tid == 0) atomicOr(a.status, kErrWaitTimeout);
