@@ -295,7 +295,7 @@ sb_status plan_create(sb_ctx *ctx, const sb_problem *p, const sb_params *prm, sb
   PLAN_ALLOC(pl->dstatus, sizeof(uint32_t));
   PLAN_ALLOC(pl->dpump, (size_t)(prm->steps > 0 ? prm->steps : 1) * sizeof(float));
   // plain FP32 solves whose rows fit one co-resident grid run every step in one launch (N=2000,
-  // 1000 steps: dSB 5.7 -> 2.2 ms, its signs one tagged word per CTA; bSB 6.3 -> 1.5 ms and aSB
+  // 1000 steps: dSB 5.7 -> 1.6 ms, its signs one tagged word per CTA; bSB 6.3 -> 1.5 ms and aSB
   // 7.4 -> 2.6 ms, x as sixteen tagged words per CTA read by sixteen threads together, aSB's FP64
   // sub-steps for a CTA's 16 rows in one warp); SB_PLAIN_PERSIST=0 keeps one launch per step
   if (mode == SB_FIELD_FP32 && !needs_trace(*prm) && prm->steps > 0) {

@@ -79,7 +79,7 @@ NCU_TRAFFIC = {
     "plain-dsb": (16.03e6, "profiles/plain_step_kernel_plain_dsb_n2000.md"),
     # the same in one cooperative launch per solve: DRAM read + write per launch from a one-pass
     # capture (J read once; 16.06 MB read, 15.9 KB written)
-    "plain-dsb-persist": (16.08e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
+    "plain-dsb-persist": (16.07e6, "profiles/plain_persist_kernel_plain_dsb_n2000.md"),
     # batched bSB, N=8192, R=256, BF16 hi+lo with the field accumulated in K segments: bytes per SB
     # step (8-step capture of the step launch: 2.587 GB; 4 steps: 1.146 GB), times the launch's steps
     "batched-bsb": (2.587e9 / 8, "profiles/tc_sb_kernel_batched_bsb_n8192_r256.md"),
