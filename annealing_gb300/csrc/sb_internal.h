@@ -51,8 +51,8 @@ struct PlainStep {
 // [16 c, 16 c + 16) of J in registers (one row per warp; a lane holds the float4 groups g = lane +
 // 32 k, which is the per-step kernel's summation order) and replica r's x, y of those rows. A step
 // exchanges through one 128-byte line per CTA at words[parity][r][c]: dSB one word (step tag << 32 |
-// 16 sign bits), bSB / aSB sixteen (step tag << 32 | bits of x). Eligible when jp <= kPersistMaxJp
-// and G R CTAs (G = ceil(n / 16)) are co-resident.
+// 16 sign bits), bSB / aSB / NMFA sixteen (step tag << 32 | bits of x or of the state s). Eligible
+// when jp <= kPersistMaxJp and G R CTAs (G = ceil(n / 16)) are co-resident.
 struct PlainPersist {
   int variant;                // 0 aSB, 1 bSB (x exchanged), 2 dSB (signs exchanged), 3 NMFA (states exchanged)
   int n, R, jp, xp;

@@ -571,10 +571,11 @@ int grid_for(size_t total) {
 
 
 // ---------------------------------------------------------------------------------------------
-// Plain FP32 dSB, the whole solve in one cooperative launch (PlainPersist). Warp w of CTA (c, r)
-// owns row i = 16 c + w of replica r: its J row sits in the lanes' registers (lane L: float4 groups
-// g = L + 32 k, k < kPersistGroups, the order dot_chunk sums in), its x, y in registers too. A
-// step needs sign(x(t)) of every spin; CTA c's 16 signs travel in one 64-bit word
+// Plain FP32 solves (aSB, bSB, dSB, and NMFA sweeps), the whole solve in one cooperative launch
+// (PlainPersist). Warp w of CTA (c, r) owns row i = 16 c + w of replica r: its J row sits in the
+// lanes' registers (lane L: float4 groups g = L + 32 k, k < kPersistGroups, the order dot_chunk
+// sums in), its x, y in registers too. A dSB step needs sign(x(t)) of every spin; CTA c's 16 signs
+// travel in one 64-bit word
 // (tag t + 1 << 32 | bit w = x_i <= 0) at words[t & 1][r][c]: the tag is the flag, so one L2 round
 // trip per step moves all the data; the thread that polls a word writes its 16 signs into shared
 // memory as +-1.0, so the field sums the same products as the bSB / aSB form, which exchanges x
