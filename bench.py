@@ -17,6 +17,9 @@ one full solve (init, 2000 SB steps, final energies, best spins back to the host
          workload's distribution through sb_submit / sb_poll, p50 / p99 latency and served rate
   cpu_baseline  the multithreaded FP32 CPU port of the same step loop (oracle/sb_cpu_baseline.c)
          on this host's cores, on a bounded sample of the workload
+  plain_same_instance_as_reference_gpu  after the timed region: the plain FP32 path (aSB, the
+         reference's update, and dSB) on the instance the reference arm's reference_gpu_plain
+         times the reference program on (2000 spins, 1 replica, 1000 SB steps)
 
 Multi-GPU: the path shards by replicas / instances only; each rank runs its own solve (weak
 scaling) and the value is the total over ranks divided by the slowest rank's time.
@@ -322,6 +325,41 @@ def plain_fp32_comparison(sb, ctx, prob, plan, vcode, n, R, sb_steps, value, str
             "note": "same instance, replicas, SB steps and seed; one solve each"}
 
 
+def plain_same_instance(sb, ctx, stream, sb_steps=1000, runs=7):
+    """This library's plain FP32 path on the instance `reference_gpu_plain` times the reference
+    program on (complete +-1 graph of 2000 spins, seed 1234, one replica, 1000 SB steps): aSB (the
+    reference's update, its initial state) and dSB, each a whole solve from a plan (init, every
+    step, final energies), CUDA events on the launching stream, the median of `runs` after one
+    warm-up run."""
+    import torch
+
+    from annealing_gb300 import instances
+
+    spins = 2000
+    prob = sb.Problem.from_dense(instances.complete_pm1(spins, seed=1234))
+    out = {"instance": f"complete +-1 graph, {spins} spins, 1 replica, {sb_steps} SB steps (as reference_gpu_plain)"}
+    for name, vcode, init in (("asb", sb.ASB, sb.INIT_REFERENCE), ("dsb", sb.DSB, sb.INIT_UNIFORM)):
+        prm = sb.Params.default(vcode, steps=sb_steps, replicas=1, field_mode=sb.FIELD_FP32, init_mode=init)
+        plan = ctx.plan(prob, prm)
+        try:
+            plan.run(seed=1)
+            ts = []
+            for k in range(runs):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = plan.run(seed=2 + k)
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        finally:
+            plan.close()
+        ms = float(np.median(ts))
+        out[name] = {"ms_per_solve": ms, "ms_per_sb_step": ms / sb_steps,
+                     "spin_updates_per_s": spins * sb_steps / (ms * 1e-3),
+                     "sb_steps_per_launch": int(r.steps_per_launch), "kernel_launches": int(r.kernel_launches)}
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -490,6 +528,12 @@ def run_ours(args, rank, world, local_rank):
     }
     if field == "tc" and variant == "dsb" and world == 1:
         line["vs_plain_fp32"] = plain_fp32_comparison(sb, ctx, prob, plan, vcode, n, R, sb_steps, value, stream)
+    if args.workload == "batched-dsb" and world == 1:
+        # the plain path next to the reference program's GPU timing (the reference arm's reference_gpu_plain)
+        try:
+            line["plain_same_instance_as_reference_gpu"] = plain_same_instance(sb, ctx, stream)
+        except Exception as exc:  # a side figure: the line's own numbers stand without it
+            line["plain_same_instance_as_reference_gpu"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(args.workload, J, h).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
