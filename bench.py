@@ -337,7 +337,9 @@ def plain_same_instance(sb, ctx, stream, sb_steps=1000, runs=7):
 
     spins = 2000
     prob = sb.Problem.from_dense(instances.complete_pm1(spins, seed=1234))
-    out = {"instance": f"complete +-1 graph, {spins} spins, 1 replica, {sb_steps} SB steps (as reference_gpu_plain)"}
+    out = {"instance": f"complete +-1 graph, {spins} spins, 1 replica, {sb_steps} SB steps (as reference_gpu_plain)",
+           "note": "a timing figure: on this instance aSB's x overflows to NaN after ~300 steps (the CPU "
+                   "restatement of the reference's update does the same; its default is 100 steps)"}
     for name, vcode, init in (("asb", sb.ASB, sb.INIT_REFERENCE), ("dsb", sb.DSB, sb.INIT_UNIFORM)):
         prm = sb.Params.default(vcode, steps=sb_steps, replicas=1, field_mode=sb.FIELD_FP32, init_mode=init)
         plan = ctx.plan(prob, prm)
