@@ -247,6 +247,8 @@ def reference_gpu_plain(sb_steps=1000):
             "ms_per_sb_step_as_program": prog_ms, "ms_per_sb_step_device_only": dev_ms,
             "spin_updates_per_s_as_program": spins / (prog_ms * 1e-3),
             "spin_updates_per_s_device_only": spins / (dev_ms * 1e-3),
+            "divergence": "on this instance the aSB update overflows x to NaN after ~300 steps (as the CPU "
+                          "restatement of it does): a timing figure",
             "note": "as_program: an event pair and an event synchronize around every step, as m2_opt.cu:159-185 "
                     "(host wall time); device_only: the same launches back to back under one event pair"}
 
