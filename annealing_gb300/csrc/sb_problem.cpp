@@ -741,11 +741,17 @@ bool parse_num(Cursor &c, double &v) {
   return true;
 }
 
+// One edge line: indices clamped to int32 (anything outside [-1, 2^30] is out of range for every
+// N <= 65536 either way; the true extremes are kept per chunk for the index-base rule), the weight
+// as the float J stores, the chunk-local line number.
 struct Triple {
-  long long i, j;
-  double w;
-  int line;
+  int32_t i, j;
+  float w;
+  int32_t line;
 };
+inline int32_t clamp_index(long long v) {
+  return (int32_t)std::min<long long>(std::max<long long>(v, -1), 1 << 30);
+}
 
 }  // namespace
 
@@ -763,6 +769,17 @@ sb_status sbh::load_graph(const char *path, const sb_graph_opts *opts_in, sb_pro
   }
   std::vector<char> buf;
   {
+    // one read of the file's size, then whatever a growing file added
+    if (fseek(f, 0, SEEK_END) == 0) {
+      const long sz = ftell(f);
+      if (sz > 0 && fseek(f, 0, SEEK_SET) == 0) {
+        buf.resize((size_t)sz);
+        buf.resize(fread(buf.data(), 1, (size_t)sz, f));
+      } else {
+        fseek(f, 0, SEEK_SET);
+        buf.clear();
+      }
+    }
     char tmp[1 << 16];
     size_t got;
     while ((got = fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
@@ -796,42 +813,106 @@ sb_status sbh::load_graph(const char *path, const sb_graph_opts *opts_in, sb_pro
     err = "N out of range (1..65536): " + std::to_string(n);
     return SB_ERR_PARSE;
   }
-  std::vector<Triple> tr;
+  // The edge lines, parsed in chunks that end at line ends (a triple never spans lines) on the host
+  // pool. Each chunk keeps its triples in file order with chunk-local line numbers, its first parse
+  // error and the newlines it consumed; the fill below walks the chunks in order, so duplicates,
+  // conflicts, the index base and every error message are those of one pass over the file.
+  struct Chunk {
+    const char *b = nullptr, *e = nullptr;
+    std::vector<Triple> tr;
+    long long min_idx = (1LL << 40), max_idx = -1;
+    int lines = 0;     // newlines consumed
+    int err_line = 0;  // local line of the first parse error, with err_kind > 0
+    int err_kind = 0;  // 1 expected an index, 2 expected 'i j w', 3 indices must be integers
+    bool diag = false;  // a line i i h (a field)
+  };
+  const size_t rest = (size_t)(c.end - c.p);
+  const int pool = host_threads(1 << 20);
+  const int nchunks = (int)std::max<size_t>(1, std::min<size_t>((size_t)pool * 4, rest / (256 * 1024)));
+  std::vector<Chunk> chunks((size_t)nchunks);
+  {
+    const char *at = c.p;
+    for (int k = 0; k < nchunks; ++k) {
+      chunks[k].b = at;
+      const char *cut = k + 1 == nchunks ? c.end : c.p + rest / nchunks * (size_t)(k + 1);
+      if (cut < at) cut = at;
+      while (cut < c.end && cut[-1] != '\n') ++cut;  // the chunk ends just after a newline
+      chunks[k].e = cut;
+      at = cut;
+    }
+  }
+  auto parse_chunk = [&](int k) {
+    Chunk &ch = chunks[k];
+    Cursor q{ch.b, ch.e, 0};
+    for (;;) {
+      skip_space(q, false);
+      if (q.p >= q.end) break;
+      Triple t;
+      t.line = q.line;
+      double wi, wj, wv;
+      if (!parse_num(q, wi)) {
+        ch.err_line = q.line;
+        ch.err_kind = 1;
+        return;
+      }
+      skip_space(q, true);
+      if (q.p >= q.end || *q.p == '\n' || !parse_num(q, wj)) {
+        ch.err_line = t.line;
+        ch.err_kind = 2;
+        return;
+      }
+      skip_space(q, true);
+      if (q.p >= q.end || *q.p == '\n' || !parse_num(q, wv)) {
+        ch.err_line = t.line;
+        ch.err_kind = 2;
+        return;
+      }
+      if (wi != floor(wi) || wj != floor(wj)) {
+        ch.err_line = t.line;
+        ch.err_kind = 3;
+        return;
+      }
+      // bounded before the conversion (an index like 1e30 is out of range, not undefined)
+      const double lim = (double)(1LL << 41);
+      const long long ti = (long long)std::max(-lim, std::min(wi, lim));
+      const long long tj = (long long)std::max(-lim, std::min(wj, lim));
+      ch.min_idx = std::min(ch.min_idx, std::min(ti, tj));
+      ch.max_idx = std::max(ch.max_idx, std::max(ti, tj));
+      t.i = clamp_index(ti);
+      t.j = clamp_index(tj);
+      t.w = (float)wv;
+      if (ti == tj) ch.diag = true;
+      ch.tr.push_back(t);
+    }
+    ch.lines = q.line;
+  };
+  if (nchunks == 1)
+    parse_chunk(0);
+  else
+    parallel_run(nchunks, parse_chunk);
   long long min_idx = (1LL << 40), max_idx = -1;
-  for (;;) {
-    skip_space(c, false);
-    if (c.p >= c.end) break;
-    Triple t;
-    t.line = c.line;
-    double wi, wj;
-    if (!parse_num(c, wi)) {
-      err = "line " + std::to_string(c.line) + ": expected an index";
-      return SB_ERR_PARSE;
+  bool any = false, diag = false;
+  std::vector<int> line0((size_t)nchunks);  // the global line at each chunk's start
+  {
+    int ln = c.line;
+    for (int k = 0; k < nchunks; ++k) {
+      const Chunk &ch = chunks[k];
+      line0[k] = ln;
+      if (ch.err_kind) {
+        static const char *const what[4] = {"", "expected an index", "expected 'i j w'",
+                                            "indices must be integers"};
+        err = "line " + std::to_string(ln + ch.err_line) + ": " + what[ch.err_kind];
+        return SB_ERR_PARSE;
+      }
+      ln += ch.lines;
+      if (!ch.tr.empty()) any = true;
+      diag = diag || ch.diag;
+      min_idx = std::min(min_idx, ch.min_idx);
+      max_idx = std::max(max_idx, ch.max_idx);
     }
-    skip_space(c, true);
-    if (c.p >= c.end || *c.p == '\n' || !parse_num(c, wj)) {
-      err = "line " + std::to_string(t.line) + ": expected 'i j w'";
-      return SB_ERR_PARSE;
-    }
-    skip_space(c, true);
-    if (c.p >= c.end || *c.p == '\n' || !parse_num(c, t.w)) {
-      err = "line " + std::to_string(t.line) + ": expected 'i j w'";
-      return SB_ERR_PARSE;
-    }
-    if (wi != floor(wi) || wj != floor(wj)) {
-      err = "line " + std::to_string(t.line) + ": indices must be integers";
-      return SB_ERR_PARSE;
-    }
-    t.i = (long long)wi;
-    t.j = (long long)wj;
-    if (t.i < min_idx) min_idx = t.i;
-    if (t.j < min_idx) min_idx = t.j;
-    if (t.i > max_idx) max_idx = t.i;
-    if (t.j > max_idx) max_idx = t.j;
-    tr.push_back(t);
   }
   int base = opts.index_base;
-  if (base < 0) base = (!tr.empty() && max_idx == n && min_idx >= 1) ? 1 : 0;
+  if (base < 0) base = (any && max_idx == n && min_idx >= 1) ? 1 : 0;
   const size_t nn = (size_t)n * (size_t)n;
   float *J = (float *)calloc(nn, sizeof(float));
   if (!J) {
@@ -839,44 +920,76 @@ sb_status sbh::load_graph(const char *path, const sb_graph_opts *opts_in, sb_pro
     return SB_ERR_OOM;
   }
   float *h = nullptr;
-  for (const Triple &t : tr) {
-    const long long i = t.i - base, j = t.j - base;
-    if (i < 0 || j < 0 || i >= n || j >= n) {
+  if (diag) {
+    h = (float *)calloc((size_t)n, sizeof(float));
+    if (!h) {
       free(J);
-      free(h);
-      err = "line " + std::to_string(t.line) + ": index out of range for N=" + std::to_string(n);
-      return SB_ERR_PARSE;
+      err = "host allocation of h failed";
+      return SB_ERR_OOM;
     }
-    const float w = (float)t.w;
-    if (i == j) {
-      if (!h) {
-        h = (float *)calloc((size_t)n, sizeof(float));
-        if (!h) {
-          free(J);
-          err = "host allocation of h failed";
-          return SB_ERR_OOM;
+  }
+  // The fill: thread w owns rows [n w / nt, n (w + 1) / nt) and walks every triple in file order,
+  // writing only cells of its rows, so each cell sees its writes (and the strict check its earlier
+  // value) in file order. A thread stops at its first error; the earliest line over the threads is
+  // the error one pass in file order reports (an index out of range stops every thread there).
+  struct FillErr {
+    long long line = -1;
+    int kind = 0;  // 1 index out of range, 2 conflicting field, 3 conflicting weight
+    long long a = 0, b = 0;
+  };
+  const int nt = nchunks == 1 ? 1 : std::max(1, std::min(host_threads(1 << 20), (int)n));
+  std::vector<FillErr> ferr((size_t)nt);
+  auto fill = [&](int w) {
+    const long long r0 = n * w / nt, r1 = n * (w + 1) / nt;
+    FillErr &fe = ferr[w];
+    for (int k = 0; k < nchunks; ++k) {
+      for (const Triple &t : chunks[k].tr) {
+        const long long i = (long long)t.i - base, j = (long long)t.j - base;
+        if (i < 0 || j < 0 || i >= n || j >= n) {
+          fe = {(long long)line0[k] + t.line, 1, 0, 0};
+          return;
         }
+        const bool own_i = i >= r0 && i < r1;
+        if (i == j) {
+          if (own_i) {
+            if (opts.strict && h[i] != 0.0f && h[i] != t.w) {
+              fe = {(long long)line0[k] + t.line, 2, i, 0};
+              return;
+            }
+            h[i] = t.w;
+          }
+          continue;
+        }
+        if (own_i) {
+          float &a = J[(size_t)i * n + j];
+          if (opts.strict && a != 0.0f && a != t.w) {
+            fe = {(long long)line0[k] + t.line, 3, i, j};
+            return;
+          }
+          a = t.w;
+        }
+        if (j >= r0 && j < r1) J[(size_t)j * n + i] = t.w;
       }
-      if (opts.strict && h[i] != 0.0f && h[i] != w) {
-        free(J);
-        free(h);
-        err = "line " + std::to_string(t.line) + ": conflicting field for spin " +
-              std::to_string(i);
-        return SB_ERR_PARSE;
-      }
-      h[i] = w;
-      continue;
     }
-    float &a = J[(size_t)i * n + j];
-    if (opts.strict && a != 0.0f && a != w) {
-      free(J);
-      free(h);
-      err = "line " + std::to_string(t.line) + ": conflicting weight for edge " +
-            std::to_string(i) + "-" + std::to_string(j);
-      return SB_ERR_PARSE;
-    }
-    a = w;
-    J[(size_t)j * n + i] = w;
+  };
+  if (nt == 1)
+    fill(0);
+  else
+    parallel_run(nt, fill);
+  const FillErr *first = nullptr;
+  for (const FillErr &fe : ferr)
+    if (fe.kind && (!first || fe.line < first->line)) first = &fe;
+  if (first) {
+    free(J);
+    free(h);
+    const std::string at = "line " + std::to_string(first->line) + ": ";
+    if (first->kind == 1)
+      err = at + "index out of range for N=" + std::to_string(n);
+    else if (first->kind == 2)
+      err = at + "conflicting field for spin " + std::to_string(first->a);
+    else
+      err = at + "conflicting weight for edge " + std::to_string(first->a) + "-" + std::to_string(first->b);
+    return SB_ERR_PARSE;
   }
   out->n = (int32_t)n;
   out->J = J;

@@ -195,6 +195,59 @@ def test_graph_reader_errors(tmp_path):
         sb.Problem.load(write("3\n0 1 1\n0 1 -2\n"), strict=True)
 
 
+def test_graph_reader_large_file_in_file_order(tmp_path):
+    """Files of a few MB are parsed in chunks on several host threads and filled by row owners: the
+    couplings, fields, duplicates (the later line wins), index base and the line of the first error
+    (parse, range or strict conflict) are those of one pass in file order."""
+    rng = np.random.default_rng(5)
+    n, m = 700, 250_000
+    i = rng.integers(1, n + 1, m)
+    j = rng.integers(1, n + 1, m)
+    w = rng.integers(-3, 4, m)
+    i[-1], j[-1] = n, 1  # the largest index is N: 1-based
+    lines = [f"# generated\n{n} {m}\n"]
+    for k in range(m):
+        sep = "," if k % 89 == 0 else " "
+        lines.append(f"{i[k]}{sep}{j[k]}{sep}{w[k]}" + ("  # note" if k % 1000 == 3 else "") +
+                     ("\r\n" if k % 2 else "\n"))
+        if k % 7000 == 11:
+            lines.append("\n# a comment line\n")
+    path = str(tmp_path / "big.txt")
+    open(path, "w", newline="").write("".join(lines))
+    J = np.zeros((n, n), np.float32)
+    h = np.zeros(n, np.float32)
+    for a, b, v in zip(i - 1, j - 1, w):
+        if a == b:
+            h[a] = v
+        else:
+            J[a, b] = J[b, a] = v
+    p = sb.Problem.load(path)
+    np.testing.assert_array_equal(p.J, J)
+    np.testing.assert_array_equal(np.ctypeslib.as_array(p.s.h, shape=(n,)), h)
+    text = "".join(lines).split("\n")
+    # (index N + 1 with the base given: with the base detected it would make the file 0-based)
+    for bad, base in (("1 2", -1), ("1.5 2 3", -1), (f"1 {n + 1} 1", 1)):
+        at = len(text) * 3 // 4
+        while text[at].startswith("#") or not text[at].strip():
+            at += 1
+        t = list(text)
+        t[at] = bad
+        open(path, "w", newline="").write("\n".join(t))
+        with pytest.raises(sb.SBError) as e:
+            sb.Problem.load(path, index_base=base)
+        assert e.value.status == 3 and f"line {at + 1}:" in str(e.value), (bad, str(e.value))
+    # strict: the first conflicting line in file order, although the rows belong to other threads
+    t = list(text)
+    at = len(text) - 3
+    t.insert(at, f"{i[0]} {j[0]} {int(J[i[0] - 1, j[0] - 1]) + 10}")
+    open(path, "w", newline="").write("\n".join(t))
+    with pytest.raises(sb.SBError) as e:
+        sb.Problem.load(path, strict=True)
+    assert "conflicting" in str(e.value)
+    first = int(str(e.value).split("line ")[1].split(":")[0])
+    assert first <= at + 1  # an earlier duplicate with another weight may conflict first
+
+
 def test_footprint_is_positive_and_grows_with_replicas():
     J = instances.complete_pm1(256, 1)
     p = sb.Problem.from_dense(J)
