@@ -911,6 +911,7 @@ sb_status sbh::load_graph(const char *path, const sb_graph_opts *opts_in, sb_pro
       max_idx = std::max(max_idx, ch.max_idx);
     }
   }
+  std::vector<char>().swap(buf);  // the text is parsed: release it before J is allocated
   int base = opts.index_base;
   if (base < 0) base = (any && max_idx == n && min_idx >= 1) ? 1 : 0;
   const size_t nn = (size_t)n * (size_t)n;
