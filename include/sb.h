@@ -78,7 +78,10 @@ typedef enum sb_variant { SB_ASB = 0, SB_BSB = 1, SB_DSB = 2 } sb_variant;
 /* How the field J*v is computed.
  *  SB_FIELD_AUTO: tensor cores when replicas >= 32 and the problem allows an exact/declared
  *                 precision, otherwise the plain FP32 kernel.
- *  SB_FIELD_FP32: the plain fused FP32 kernel, one launch per step (the drop-in form).
+ *  SB_FIELD_FP32: the plain fused FP32 kernel (the drop-in form): the whole solve in one cooperative
+ *                 launch when the rows fit one co-resident grid (n <= 2048, ceil(n / 16) x replicas
+ *                 CTAs on the SMs, no energy trace), else one launch per step; the same bits either
+ *                 way (environment SB_PLAIN_PERSIST=0 keeps one launch per step).
  *  SB_FIELD_TC:   tcgen05 tensor cores. dSB with integer |J| <= 4 and n <= ~2300: packed E2M1
  *                 operands with J resident in shared memory, FP32 accumulation (bit-exact).
  *                 dSB with integer |J| <= 16: FP8 E4M3 operands (grouped batches and serving:
@@ -185,7 +188,8 @@ typedef struct sb_result {
   double device_ms;            /* CUDA-event time of init + step loop + final energy */
   double kernel_ms_avg;        /* profile == 1: average device time of one launch of the step kernel
                                   (the tensor-core kernel runs every step in one launch), else 0 */
-  int32_t steps_per_launch;    /* SB steps one step-kernel launch advances (1 plain, steps TC) */
+  int32_t steps_per_launch;    /* SB steps one step-kernel launch advances (1 for the per-step plain
+                                  kernel, steps for the one-launch plain solve and the TC kernel) */
   int64_t kernel_launches;     /* kernels this call launched on the device */
   double total_ms;             /* host wall time of the call, copies included */
   double spin_updates_per_s;   /* n * replicas * steps / (device_ms / 1e3) */
@@ -422,8 +426,9 @@ typedef struct sb_nmfa_params {
   float noise;              /* Gaussian noise scale sigma (Ising.cpp:12, SIGMA = 0.15) */
   float recombination;      /* alpha (Ising.cpp:11, ALPHA = 0.15) */
   uint32_t seed;            /* Ising.cpp:13, SEED = 1234 */
-  int32_t field_mode;       /* sb_field_mode. SB_FIELD_FP32: the fused FP32 kernel, one launch per sweep
-                               (bit-exact with the oracle). SB_FIELD_TC: one persistent tcgen05 launch,
+  int32_t field_mode;       /* sb_field_mode. SB_FIELD_FP32: the fused FP32 kernel, every sweep in one
+                               cooperative launch when the rows fit one co-resident grid, else one launch
+                               per sweep (bit-exact with the oracle either way). SB_FIELD_TC: one persistent tcgen05 launch,
                                the state as BF16 hi + lo against exact BF16 couplings (integer |J| <= 256),
                                FP32 accumulation; within a stated tolerance of the FP32 path.
                                SB_FIELD_AUTO: TC for 32 samples or more when it applies, else FP32. */
